@@ -1,0 +1,181 @@
+"""Generate the golden fixtures in tests/golden/ (run in a container that has the
+reference sources; the fixtures are committed so the tests need no reference).
+
+    python tests/golden/make_golden.py            # everything
+    python tests/golden/make_golden.py replay     # one group
+
+Groups
+  replay   -- the reference's own REWL_Walker (oracle/build_ref.py harness):
+              initial configuration after adjust_state_to_range, then K1 sweeps
+              at ln f = 1, then reset_histogram (REDUCE_LOGDOS) and K2 sweeps at
+              ln f = 1/2.  Records lattices, states, histograms, logDoS and
+              per-bin observables (src/REWL/wang_landau.hpp:51-120,
+              src/REWL/rewl_walker.hpp:79-158).
+  glazier  -- glazier::construct_windows windows (src/REWL/glazier.hpp:305-351).
+  rng      -- the first uniforms of random_number_generator<double>
+              (src/util/random_number_generators.hpp:14-31) for a few seeds.
+  normalize-- normalize_logDoS (src/util/array_shift.hpp:15-43).
+  exact    -- exact 2D Ising ln g(E) (oracle/beale.py) for L = 4..64.
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from oracle import beale, build_ref, pyoracle  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+ISING_CASES = [
+    # name, L, wmin, wmax, bw, seed, K1, K2
+    ("ising_L4_full", 4, -32, 36, 4, 101, 300, 300),
+    ("ising_L8_low", 8, -128, -20, 4, 12345, 100, 100),
+    ("ising_L16_c1w1", 16, -368, 224, 4, 7, 60, 60),
+    ("ising_L16_bw8", 16, -296, 200, 8, 5, 60, 60),
+    ("ising_L32_c2w3", 32, -1404, -536, 4, 3, 20, 20),
+]
+AT_CASES = [
+    # name, L, K, sigma_h, window lo (bins of 0.05 above E_allup), nbins, seed, K1, K2
+    ("at_L4_rf", 4, 0.5, 0.5, 400, 900, 3, 40, 40),
+    ("at_L8_rf", 8, 0.5, 0.5, 3000, 4000, 11, 25, 25),
+    ("at_L6_clean_K025", 6, 0.25, 0.0, 1000, 2000, 2, 30, 30),
+]
+
+
+def quantised_fields(rng, n, sigma):
+    return np.round(rng.normal(0.0, sigma, n) * 2.0**20) / 2.0**20
+
+
+def _stage(ref, orc):
+    c, g = ref.hist()
+    return dict(dofs=ref.dofs().astype(np.int8), state=ref.state(), counts=c, logdos=g, obs=ref.obs(),
+                draws=np.array(orc.draws(0), dtype=np.uint64))
+
+
+def _replay_case(model, name, L, K, wmin, wmax, bw, nb, seed, k1, k2, fields=None):
+    if model == "ising":
+        so = build_ref.build("ising", L, bw)
+    else:
+        so = build_ref.build("at", L, bw, K=K, fields=fields is not None)
+    ref = pyoracle.RefWalker(so, wmin, wmax, bw, nb, seed)
+    rng = np.random.default_rng(seed)
+    if fields is not None:
+        ref.import_disorder(fields)
+    d0 = rng.choice([-1.0, 1.0], size=ref.ndof)
+    ref.import_dofs(d0)
+    ref.adjust()
+    st0, dofs0 = ref.state().copy(), ref.dofs().copy()
+    # the port follows along so that the number of uniforms consumed is known
+    cfg = pyoracle.Config(model=pyoracle.MODEL_ISING if model == "ising" else pyoracle.MODEL_AT, L=L, K=K,
+                          escale_bits=0 if model == "ising" else 20, nwin=1, R=1, emin=wmin, emax=wmax, bw=bw,
+                          semantics=pyoracle.SEM_REFERENCE, observables=1)
+    orc = pyoracle.Oracle(cfg, fields=fields, init_dofs=dofs0)
+    orc.set_dofs(0, dofs0, int(st0[4]) if model != "ising" else 0)
+    orc.set_rng(0, seed, 1)
+    ref.walk(k1)
+    orc.run_sweeps(k1)
+    s1 = _stage(ref, orc)
+    ref.reset()
+    ref.set_lnf(0.5)
+    orc.reset(0, True)
+    orc.set_lnf(0, 0.5)
+    ref.walk(k2)
+    orc.run_sweeps(k2)
+    s2 = _stage(ref, orc)
+    c2, g2, _ = orc.tables(0)
+    assert np.array_equal(c2, s2["counts"]) and np.array_equal(g2, s2["logdos"]), name
+    data = dict(model=np.array(0 if model == "ising" else 1), L=np.array(L), K=np.array(K), bw=np.array(bw),
+                wmin=np.array(float(wmin)), wmax=np.array(float(wmax)), nbins=np.array(nb), seed=np.array(seed),
+                sweeps1=np.array(k1), sweeps2=np.array(k2), lnf1=np.array(1.0), lnf2=np.array(0.5),
+                fields=np.zeros(0) if fields is None else fields,
+                init_dofs_raw=d0.astype(np.int8), dofs0=dofs0.astype(np.int8), state0=st0,
+                adjust_draws=np.array(1))
+    for k, v in s1.items():
+        data[f"{k}1"] = v
+    for k, v in s2.items():
+        data[f"{k}2"] = v
+    np.savez_compressed(OUT / f"replay_{name}.npz", **data)
+    print("wrote", name, "state", s2["state"], "draws", s1["draws"], s2["draws"])
+
+
+def gen_replay():
+    for name, L, wmin, wmax, bw, seed, k1, k2 in ISING_CASES:
+        nb = int(round((wmax - wmin) / bw))
+        _replay_case("ising", name, L, 0.0, wmin, wmax, bw, nb, seed, k1, k2)
+    for name, L, K, sig, wlo, nb, seed, k1, k2 in AT_CASES:
+        N = L * L
+        emin = -(2.0 + K) * 2 * N
+        wmin, wmax = emin + wlo / 20.0, emin + (wlo + nb) / 20.0
+        rng = np.random.default_rng(seed + 1000)
+        fields = quantised_fields(rng, N, sig) if sig > 0 else None
+        _replay_case("at", name, L, K, wmin, wmax, 0.05, nb, seed, k1, k2, fields=fields)
+
+
+def gen_glazier():
+    so = build_ref.build("ising", 8, 4.0)
+    ref = pyoracle.RefWalker(so, -128, -20, 4.0, 27, 1)
+    cases = {
+        "C1_L16": (-512.0, 516.0, 4.0, 4, 1, 0.75),
+        "C2_L32": (-2048.0, 2052.0, 4.0, 16, 8, 0.75),
+        "L64_64w": (-8192.0, 8196.0, 4.0, 64, 8, 0.75),
+        "L24_16w": (-1152.0, 1156.0, 4.0, 16, 4, 0.75),
+        "ref_default_L24_bw8": (-1152.0, 0.0, 8.0, 8, 1, 0.75),
+        "at_L32_bw005": (-5120.0, 0.0, 0.05, 8, 4, 0.75),
+    }
+    out = {}
+    for k, (a, b, bw, n, r, ov) in cases.items():
+        mins, maxs, nb = ref.glazier(a, b, bw, n, r, ov)
+        out[k] = dict(args=[a, b, bw, n, r, ov], mins=[float(x) for x in mins], maxs=[float(x) for x in maxs],
+                      nbins=[int(x) for x in nb])
+    (OUT / "glazier.json").write_text(json.dumps(out, indent=1))
+    print("wrote glazier.json")
+
+
+def gen_rng():
+    so = build_ref.build("ising", 8, 4.0)
+    ref = pyoracle.RefWalker(so, -128, -20, 4.0, 27, 1)
+    import ctypes as C
+    out = {}
+    for seed in (1, 12345, 3141592653):
+        u = np.zeros(64)
+        ref.lib.ref_uniforms(seed, 64, u.ctypes.data_as(C.c_void_p))
+        out[str(seed)] = [float(x).hex() for x in u]
+    (OUT / "ref_uniforms.json").write_text(json.dumps(out, indent=1))
+    print("wrote ref_uniforms.json")
+
+
+def gen_normalize():
+    so = build_ref.build("ising", 8, 4.0)
+    ref = pyoracle.RefWalker(so, -128, -20, 4.0, 27, 1)
+    import ctypes as C
+    rng = np.random.default_rng(4)
+    cases = {}
+    for name, n, spp, N, emax in (("half", 60, 2.0, 64, 0.0), ("full", 61, 2.0, 64, 128.0), ("at", 300, 4.0, 36, 0.0)):
+        x = np.cumsum(rng.normal(0.3, 0.2, n))
+        y = x.copy()
+        ref.lib.ref_normalize_logdos(spp, N, emax, n, y.ctypes.data_as(C.c_void_p))
+        cases[name] = dict(states_per_site=spp, N=N, energy_max=emax, inp=[v.hex() for v in x], out=[v.hex() for v in y])
+    (OUT / "normalize.json").write_text(json.dumps(cases, indent=1))
+    print("wrote normalize.json")
+
+
+def gen_exact():
+    for L in (4, 6, 8, 16, 32, 64):
+        E, lng = beale.exact_lng(L)
+        extra = {}
+        if L <= 8:
+            g = beale.exact_dos(L)
+            extra["g_decimal"] = np.array([str(v) for v in g])
+        np.savez_compressed(OUT / f"exact_ising_L{L}.npz", E=E, lng=lng, **extra)
+        print("wrote exact L", L)
+
+
+if __name__ == "__main__":
+    groups = sys.argv[1:] or ["replay", "glazier", "rng", "normalize", "exact"]
+    for g in groups:
+        globals()[f"gen_{g}"]()
