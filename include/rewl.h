@@ -1,0 +1,217 @@
+/*
+ * rewl.h -- C ABI of the GB300 replica-exchange Wang-Landau (REWL) engine.
+ *
+ * One engine runs a batch of REWL instances on one GPU.  An instance is one
+ * model (2D Ising or 2D Ashkin-Teller with optional random Baxter fields) on an
+ * L x L periodic lattice, its energy range cut into overlapping windows
+ * (glazier, equal windows) with `replicas_per_window` walkers each.  Every
+ * walker of every instance advances inside the same kernel launches; replica
+ * exchange, window flatness, in-window averaging and the ln f schedule are
+ * device kernels.
+ *
+ * The reference (meese-wj/REWL_Simulator) has no FFI; its hot path is driven by
+ * REWL_simulation::simulate and the duck-typed Hamiltonian plugin surface.  Each
+ * entry point below names the reference interface it stands in for.
+ *
+ * Conventions: plain pointers and sizes; host buffers are owned by the caller
+ * and copied synchronously; the engine owns all device memory.  Every function
+ * returns REWL_OK or an error code; rewl_last_error_string() describes the last
+ * error of the calling thread.  An engine is driven by one host thread at a time.
+ */
+#ifndef REWL_GB300_H
+#define REWL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference has none: it prints and, once, calls exit(1),
+ * src/util/vector_matching.hpp:61-65) */
+#define REWL_OK 0
+#define REWL_EINVAL 22      /* bad descriptor or argument (incl. windows that do not overlap) */
+#define REWL_ENOMEM 12      /* device or host allocation failed */
+#define REWL_ETIMEDOUT 110  /* rewl_run_cycles deadline passed (host-side, no device wait) */
+#define REWL_EDEVICE 1001   /* CUDA runtime error */
+#define REWL_EBOUNDS 1002   /* a device-side bounds check fired (energy left its window) */
+#define REWL_ESTATE 1003    /* call not valid in the engine's current state */
+
+/* models (compile-time switch in the reference: src/Hamiltonians/model_hamiltonians.hpp:6-40) */
+#define REWL_MODEL_ISING2D 0
+#define REWL_MODEL_ASHKIN_TELLER2D 1
+
+/* flatness rules (src/REWL/rewl_histograms.hpp:115-152) */
+#define REWL_FLAT_MIN_OVER_MEAN 0   /* min H >= p * mean H over valid bins (the usual "flatness 0.8") */
+#define REWL_FLAT_MAX_MIN_RATIO 1   /* (max - min)/min <= p in float (reference classic rule) */
+#define REWL_FLAT_ALL_VISITED 2     /* every valid bin visited (reference ONE_OVER_T rule) */
+
+/* which bins count for flatness */
+#define REWL_MASK_STATIC 0          /* all bins except those holding only impossible energies */
+#define REWL_MASK_VISITED 1         /* additionally only bins some replica of the window ever visited */
+
+/* random streams */
+#define REWL_RNG_PHILOX 0           /* one Philox4x32-10 draw per attempted flip (production) */
+#define REWL_RNG_REPLAY 1           /* consume a caller-supplied uniform stream with the reference's
+                                       draw-on-demand rule (src/REWL/wang_landau.hpp:73) */
+
+typedef struct rewl_instance_desc {
+    int32_t model;                /* REWL_MODEL_* */
+    int32_t L;                    /* linear size, 2..128 (System_Parameters::L) */
+    double J;                     /* nearest-neighbour coupling (Ising: integer) */
+    double K;                     /* four-spin coupling (Ashkin-Teller only), multiple of 2^-20 */
+    const double* fields;         /* Ashkin-Teller Baxter field h_i per site, or NULL; rounded to 2^-20 */
+    double energy_min;            /* global energy range [energy_min, energy_max) */
+    double energy_max;
+    double bin_width;             /* Ising: power of two; Ashkin-Teller: 1/n or power of two */
+    int32_t num_windows;          /* glazier windows (src/REWL/glazier.hpp:70-115) */
+    int32_t replicas_per_window;  /* REWL_Parameters::replicas_per_window */
+    double window_overlap;        /* REWL_Parameters::window_overlap */
+    int32_t init_mode;            /* 0: spins uniform +-1 from the seed; 1: all +1 */
+    int32_t reserved;
+    uint64_t seed;                /* Philox key for this instance's walkers */
+} rewl_instance_desc;
+
+typedef struct rewl_batch_desc {
+    int32_t num_instances;
+    int32_t sweeps_per_exchange;  /* REWL_Parameters::sweeps_per_exchange */
+    int32_t sweeps_per_check;     /* REWL_Parameters::sweeps_per_check (multiple of sweeps_per_exchange) */
+    int32_t flatness_mode;        /* REWL_FLAT_* */
+    double flatness_param;        /* p of the flatness rule */
+    double lnf_initial;           /* REWL_Walker::incrementer initial value */
+    double lnf_final;             /* REWL_Parameters::final_increment */
+    int32_t mask_mode;            /* REWL_MASK_* */
+    int32_t one_over_t;           /* ONE_OVER_T_ALGORITHM switch for the ln f schedule */
+    int32_t reduce_logdos;        /* REDUCE_LOGDOS: subtract logdos[0] at each histogram reset */
+    int32_t rng_mode;             /* REWL_RNG_* */
+    int32_t device;               /* CUDA device ordinal */
+    int32_t walkers_per_block;    /* 0: automatic (autotuned); else 1, 2, 4 or 8 */
+    const rewl_instance_desc* instances;
+} rewl_batch_desc;
+
+typedef struct rewl_status {
+    int64_t sweeps;               /* sweeps done by every walker */
+    int64_t cycles;               /* check intervals completed */
+    int64_t flat_events;          /* windows that became flat (summed) */
+    int64_t windows_done;         /* windows with ln f < lnf_final */
+    int64_t windows_total;
+    int64_t exchanges_attempted;
+    int64_t exchanges_accepted;
+    int64_t attempted_flips;      /* single-spin(-flavour) attempts by all walkers */
+    int32_t all_done;
+    int32_t device_error;         /* device error word (0 = none) */
+} rewl_status;
+
+typedef struct rewl_engine rewl_engine;
+
+/* Build the batch on the device: windows, initial lattices, walk into windows.
+ * Replaces REWL_simulation's constructor + glazier + adjust_state_to_range
+ * (src/Simulation/rewl_simulation.hpp:69-108, src/REWL/rewl_walker.hpp:79-115,
+ *  src/Simulation/main.cpp:201-209). */
+int rewl_create(const rewl_batch_desc* desc, rewl_engine** out);
+
+/* Free every device allocation (REWL_simulation::~REWL_simulation). */
+int rewl_destroy(rewl_engine* eng);
+
+/* Text of the last error raised on the calling thread. */
+const char* rewl_last_error_string(void);
+
+/* Sizes and layout.  Walkers are numbered instance-major, then window, then replica
+ * (the reference's world rank order, src/REWL/mpi_rewl_comm_setup.hpp:26-77). */
+int rewl_num_walkers(const rewl_engine* eng, int32_t* num_walkers);
+int rewl_walker_info(const rewl_engine* eng, int32_t walker, int32_t* instance, int32_t* window, int32_t* replica);
+int rewl_window_info(const rewl_engine* eng, int32_t instance, int32_t window,
+                     double* energy_min, double* energy_max, int32_t* num_bins);
+
+/* Replace a walker's lattice: Ising N spins, Ashkin-Teller sigma plane then tau
+ * plane; each entry +1 or -1.  `flavour` is which_to_update (0 sigma, 1 tau).
+ * Replaces Hamiltonian::import_DoFs (src/Hamiltonians/Ising2d/ising2d_hamiltonian.hpp:127-133,
+ * src/Hamiltonians/Ashkin_Teller2d/ashkin_teller2d_hamiltonian.hpp:137-143).
+ * The energy must lie in the walker's window. */
+int rewl_import_dofs(rewl_engine* eng, int32_t walker, const int8_t* dofs, int32_t flavour);
+
+/* Replace an instance's Baxter fields (N doubles, rounded to 2^-20) and recompute
+ * every walker's energy.  Replaces Hamiltonian::import_disorder
+ * (src/Hamiltonians/Ashkin_Teller2d/ashkin_teller2d_hamiltonian.hpp:159-165). */
+int rewl_import_disorder(rewl_engine* eng, int32_t instance, const double* fields);
+
+/* Set the logDoS of every replica of a window (warm start); values are rounded
+ * to the engine's 2^-40 grid.  No reference counterpart (the reference starts at 0,
+ * src/REWL/rewl_histograms.hpp:42-50). */
+int rewl_set_logdos(rewl_engine* eng, int32_t instance, int32_t window, const double* logdos);
+
+/* Set ln f of a window (REWL_Walker::incrementer, src/REWL/rewl_walker.hpp:21). */
+int rewl_set_lnf(rewl_engine* eng, int32_t instance, int32_t window, double lnf);
+
+/* REWL_RNG_REPLAY only: the uniform stream a walker consumes, one value per
+ * uphill in-range attempt (random_number_generator::operator(),
+ * src/util/random_number_generators.hpp:29 as used at src/REWL/wang_landau.hpp:73). */
+int rewl_set_uniform_stream(rewl_engine* eng, int32_t walker, const double* uniforms, size_t count);
+
+/* Advance every walker by `num_sweeps` sweeps with no exchange and no flatness
+ * check (REWL_Walker::wang_landau_walk, src/REWL/rewl_walker.hpp:142-158). */
+int rewl_run_sweeps(rewl_engine* eng, int64_t num_sweeps);
+
+/* One replica-exchange round in the current even/odd direction, then flip the
+ * direction (REWL_simulation::replica_exchange_update, src/Simulation/rewl_simulation.hpp:228-346). */
+int rewl_exchange(rewl_engine* eng);
+
+/* Window flatness vote, in-window logDoS averaging, histogram reset
+ * (REDUCE_LOGDOS) and ln f update for every flat window
+ * (src/Simulation/rewl_simulation.hpp:361-470,541-600).  `num_flat` may be NULL. */
+int rewl_check_flat(rewl_engine* eng, int32_t* num_flat);
+
+/* Zero a window's histograms, optionally subtracting logdos[0] (rewl_histograms::reset_counts,
+ * src/REWL/rewl_histograms.hpp:83-95). */
+int rewl_reset_histograms(rewl_engine* eng, int32_t instance, int32_t window, int32_t reduce_logdos);
+
+/* Run up to `num_cycles` check intervals, each (sweeps_per_exchange sweeps +
+ * exchange) x (sweeps_per_check / sweeps_per_exchange) then the flatness step,
+ * stopping early once every window is done or `timeout_ms` (> 0) has passed.
+ * The main loop of REWL_simulation::simulate (src/Simulation/rewl_simulation.hpp:473-691). */
+int rewl_run_cycles(rewl_engine* eng, int64_t num_cycles, int64_t timeout_ms, rewl_status* status);
+
+/* Counters; synchronises the engine's stream. */
+int rewl_get_status(rewl_engine* eng, rewl_status* status);
+
+/* One walker's lattice (as rewl_import_dofs), state ([E, M] Ising; [E, sigma_mag,
+ * tau_mag, baxter, which_to_update] Ashkin-Teller), and its tables: per-stage counts,
+ * logDoS, cumulative visits.  Any output pointer may be NULL.
+ * (Hamiltonian::current_state / get_front_DoFs, rewl_histograms::export_logdos,
+ *  src/REWL/rewl_histograms.hpp:98-104) */
+int rewl_export_walker(rewl_engine* eng, int32_t walker, int8_t* dofs, double* state,
+                       uint64_t* counts, double* logdos, uint64_t* visits);
+
+/* A window's logDoS averaged over its replicas with cumulative-visit weights
+ * (the final average_and_redistribute_window, src/Simulation/rewl_simulation.hpp:687). */
+int rewl_export_window_logdos(rewl_engine* eng, int32_t instance, int32_t window, double* logdos);
+
+/* A window's valid-bin mask (1 byte per bin). */
+int rewl_export_window_mask(rewl_engine* eng, int32_t instance, int32_t window, uint8_t* mask);
+
+/* ln f and done flag of a window. */
+int rewl_window_state(rewl_engine* eng, int32_t instance, int32_t window, double* lnf, int32_t* done);
+
+/* Concatenate window logDoS tables into one ln g over the instance's energy
+ * range and normalise it so that sum_E g(E) = states_per_site^N (minus ln 2 when
+ * `half_spectrum`).  Restates concatenate_tables (multiple overlap) and
+ * normalize_logDoS (src/util/concatenate_rewl_tables.hpp:167-305,
+ * src/util/vector_matching.hpp:38-88, src/util/array_shift.hpp:15-43).
+ * Masked bins are left out.  On input *count is the capacity of energies/logdos;
+ * on output the number of values written. */
+int rewl_global_logdos(rewl_engine* eng, int32_t instance, int32_t half_spectrum,
+                       double* energies, double* logdos, int32_t* count);
+
+/* Device time spent in the sweep kernels since the last call (ms) and the
+ * number of sweep-kernel launches; timed with CUDA events on the engine stream. */
+int rewl_sweep_kernel_time(rewl_engine* eng, double* milliseconds, int64_t* launches);
+
+/* The CUDA stream the engine launches on (cudaStream_t as void*). */
+int rewl_get_stream(rewl_engine* eng, void** stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REWL_GB300_H */

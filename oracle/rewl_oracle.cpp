@@ -100,28 +100,38 @@ static inline uint32_t philox_word(uint64_t seed, uint32_t uid, uint64_t ctr, ui
 
 // ----------------------------------------------------------------------------
 // Deterministic -ln(u) for u = (2*(x>>1)+1) * 2^-32, float arithmetic only with
-// every rounding explicit (compiled with -ffp-contract=off).  ln m for
-// m in [sqrt(1/2), sqrt(2)] from the atanh series ln m = 2 atanh(s),
-// s = (m-1)/(m+1), truncated after s^9.
+// every rounding explicit (compiled with -ffp-contract=off).  For u > 1/sqrt(2)
+// the exact 1 - u is used; otherwise u = m 2^-k with m in [sqrt(1/2), sqrt(2)].
+// ln from the atanh series ln((1+s)/(1-s)) = 2 (s + s^3/3 + ... + s^9/9).
 // ----------------------------------------------------------------------------
 static inline float neglog_u32(uint32_t x)
 {
     const uint32_t v = x | 1u;
-    const int e = 31 - __builtin_clz(v);               // v in [2^e, 2^(e+1))
-    float m = (float)v;                                // round to nearest
-    uint32_t sb = (uint32_t)(127 - e) << 23;           // 2^-e
-    float scale; std::memcpy(&scale, &sb, 4);
-    m = m * scale;                                     // exact, m in [1,2]
-    int k = 32 - e;                                    // -ln u = k ln2 - ln m
-    if (m > 1.41421354f) { m = m * 0.5f; k -= 1; }
-    const float s = (m - 1.0f) / (m + 1.0f);
+    float s;
+    int k = 0;
+    if (v > 0xB504F333u)
+    {   // u > 1/sqrt(2): 1 - u = (2^32 - v) 2^-32 is exact; -ln u = 2 atanh(d / (2 - d))
+        const float d = (float)(0u - v) * 2.3283064365386963e-10f;
+        s = d / (2.0f - d);
+    }
+    else
+    {
+        const int e = 31 - __builtin_clz(v);           // v in [2^e, 2^(e+1))
+        float m = (float)v;                            // round to nearest
+        uint32_t sb = (uint32_t)(127 - e) << 23;       // 2^-e
+        float scale; std::memcpy(&scale, &sb, 4);
+        m = m * scale;                                 // exact, m in [1,2]
+        k = 32 - e;                                    // -ln u = k ln2 - ln m
+        if (m > 1.41421354f) { m = m * 0.5f; k -= 1; }
+        s = (1.0f - m) / (m + 1.0f);                   // -ln m = 2 atanh((1-m)/(1+m))
+    }
     const float s2 = s * s;
     float p = ::fmaf(s2, 0.111111112f, 0.142857149f);
     p = ::fmaf(p, s2, 0.200000003f);
     p = ::fmaf(p, s2, 0.333333343f);
     p = ::fmaf(p, s2, 1.0f);
     const float q = (2.0f * s) * p;
-    return ::fmaf((float)k, 0.693147182f, -q);
+    return ::fmaf((float)k, 0.693147182f, q);
 }
 
 // Smallest integer d (>= 1) with fl32(d * 2^-40) >= thr, for thr > 0.  Then

@@ -1,0 +1,95 @@
+"""Build and load the native engine library (librewl_gb300.so, in-tree).
+
+The library is compiled with nvcc for sm_103a only.  Loading never falls back
+to anything else: if the library is missing or cannot be loaded, an error is
+raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+INCLUDE = PKG.parent / "include"
+LIB = PKG / "librewl_gb300.so"
+SOURCES = [CSRC / "engine.cu"]
+DEPS = SOURCES + [CSRC / "rng.cuh", INCLUDE / "rewl.h"]
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found: the REWL engine needs the CUDA toolkit to build")
+    return cand
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile the engine into rewl_simulator_gb300/librewl_gb300.so."""
+    if LIB.exists() and not force:
+        newest = max(p.stat().st_mtime for p in DEPS)
+        if LIB.stat().st_mtime >= newest:
+            return LIB
+    tmp = LIB.with_name(f".librewl_gb300.{os.getpid()}.so")
+    cmd = [nvcc(), *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-shared",
+           "-I", str(INCLUDE), *map(str, SOURCES), "-o", str(tmp)]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB.exists():
+        raise RuntimeError(f"{LIB} is missing: build it with rewl_simulator_gb300.build() "
+                           "(the engine has no CPU fallback)")
+    lib = C.CDLL(str(LIB))
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def _declare(L: C.CDLL) -> None:
+    vp, i32, i64, u64, sz, dp = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_size_t, C.c_void_p
+    L.rewl_last_error_string.restype = C.c_char_p
+    sigs = {
+        "rewl_create": [vp, vp],
+        "rewl_destroy": [vp],
+        "rewl_num_walkers": [vp, vp],
+        "rewl_walker_info": [vp, i32, vp, vp, vp],
+        "rewl_window_info": [vp, i32, i32, vp, vp, vp],
+        "rewl_import_dofs": [vp, i32, vp, i32],
+        "rewl_import_disorder": [vp, i32, vp],
+        "rewl_set_logdos": [vp, i32, i32, vp],
+        "rewl_set_lnf": [vp, i32, i32, C.c_double],
+        "rewl_set_uniform_stream": [vp, i32, vp, sz],
+        "rewl_run_sweeps": [vp, i64],
+        "rewl_exchange": [vp],
+        "rewl_check_flat": [vp, vp],
+        "rewl_reset_histograms": [vp, i32, i32, i32],
+        "rewl_run_cycles": [vp, i64, i64, vp],
+        "rewl_get_status": [vp, vp],
+        "rewl_export_walker": [vp, i32, vp, vp, vp, vp, vp],
+        "rewl_export_window_logdos": [vp, i32, i32, vp],
+        "rewl_export_window_mask": [vp, i32, i32, vp],
+        "rewl_window_state": [vp, i32, i32, vp, vp],
+        "rewl_global_logdos": [vp, i32, i32, vp, vp, vp],
+        "rewl_sweep_kernel_time": [vp, vp, vp],
+        "rewl_get_stream": [vp, vp],
+    }
+    for name, args in sigs.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int

@@ -1,0 +1,1759 @@
+// GB300 replica-exchange Wang-Landau engine: host driver, device kernels and
+// the C ABI declared in include/rewl.h.
+//
+// Device layout (HBM), structure of arrays:
+//   walker slots  s = first_slot(instance) + window * R + replica
+//       slot_cfg[s]      configuration currently held by the slot (an exchange
+//                        swaps two entries instead of moving lattices)
+//       slot_tab[s]      offset of the slot's tables: g (int64, 2^-40 units),
+//                        H (uint32 per-stage counts), visits (uint64 cumulative)
+//       slot_sweeps[s]   sweeps done (Philox attempt counter base)
+//       slot_flavour[s]  Ashkin-Teller which_to_update
+//   configurations c: spins (int8; Ising N, Ashkin-Teller sigma plane then tau
+//       plane), energy (int64 units of 2^-escale), magnetisations (int32 x3)
+//   windows: ln f (int64 2^-40 units), done / 1/t flags, counters, valid-bin mask
+//
+// Kernels
+//   k_init          one thread per walker: initial spins from Philox, then the
+//                   deterministic walk into the window (rewl_walker.hpp:79-115)
+//   k_sweep_ising   one warp per walker; lattice, g and H staged in shared
+//                   memory; lanes precompute a row-aligned chunk of <= 32 sites
+//                   (energy change with and without the left neighbour flipped,
+//                   integer acceptance threshold), lane 0 resolves the serial
+//                   Wang-Landau chain in integer arithmetic only
+//   k_sweep_at      the same for Ashkin-Teller (one plane per pass, tables in
+//                   global memory)
+//   k_exchange      one thread per window pair (rewl_simulation.hpp:228-346)
+//   k_flat          one block per window: flatness vote, FP64 count-weighted
+//                   averaging, histogram reset, REDUCE_LOGDOS, ln f schedule
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rewl.h"
+#include "rng.cuh"
+
+using namespace rewl;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                 \
+    do {                                                                               \
+        cudaError_t _e = (expr);                                                       \
+        if (_e != cudaSuccess)                                                         \
+            return fail(REWL_EDEVICE, "%s: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                        __FILE__, __LINE__);                                           \
+    } while (0)
+
+constexpr int kMaxReplicas = 32;
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+enum : int { ERR_BOUNDS = 1, ERR_ADJUST = 2, ERR_REPLAY_EXHAUSTED = 4 };
+
+struct InstDev {
+    int32_t model, L, N, ndof;
+    int32_t nwin, R, first_win, first_slot;
+    int32_t bin_shift, escale, chunk, init_mode;
+    int64_t J_u, K_u;        // couplings in energy units
+    int64_t eglo_u;          // global range start in energy units
+    int64_t bin_mul;         // global bin = ((E - eglo_u) * bin_mul) >> bin_shift
+    int64_t field_off;       // offset into fields (int64 units per site) or -1
+    uint64_t seed;
+};
+
+struct WinDev {
+    int32_t inst, local, nb, pad;
+    int64_t gblo;            // first global bin
+    int64_t mask_off;        // offset into the mask array
+    int64_t elo_u;           // lower energy edge in units (exact when bin_mul == 1)
+};
+
+struct DevPtrs {
+    InstDev* inst;
+    WinDev* win;
+    int32_t* slot_inst;
+    int32_t* slot_win;
+    int32_t* slot_cfg;
+    int64_t* slot_tab;
+    int32_t* slot_nb;
+    int32_t* slot_flavour;
+    uint64_t* slot_sweeps;
+    int64_t* slot_draws;
+    int64_t* slot_thr_off;
+    int64_t* slot_thr_n;
+    int64_t* thr;            // replay thresholds
+    int64_t* cfg_off;
+    int8_t* spins;
+    int64_t* cfg_E;
+    int32_t* cfg_M;          // 3 per configuration
+    int64_t* fields;         // Baxter field per site (units)
+    int64_t* g;
+    uint32_t* H;
+    uint64_t* visits;
+    uint8_t* mask;
+    int64_t* win_lnf;
+    int32_t* win_done;
+    int32_t* win_oot;
+    uint64_t* win_iter;
+    uint64_t* win_sweepctr;
+    int32_t* pairs;          // exchange pair lists: (instance, lower window) for dir 0 then dir 1
+    int32_t* counters;       // [0] error word, [1] flat events (this call)
+    unsigned long long* stats;  // [0] exch attempted, [1] exch accepted
+};
+
+// --------------------------------------------------------------------------
+// Energies in integer units
+// --------------------------------------------------------------------------
+__host__ __device__ inline int nb_up(int i, int L) { int x = i % L, y = i / L; return (y == 0 ? L - 1 : y - 1) * L + x; }
+__host__ __device__ inline int nb_left(int i, int L) { int x = i % L, y = i / L; return y * L + (x == 0 ? L - 1 : x - 1); }
+__host__ __device__ inline int nb_right(int i, int L) { int x = i % L, y = i / L; return y * L + (x == L - 1 ? 0 : x + 1); }
+__host__ __device__ inline int nb_down(int i, int L) { int x = i % L, y = i / L; return (y == L - 1 ? 0 : y + 1) * L + x; }
+
+// Ising: E = -J sum_<ij> s_i s_j, recomputed as sum_i -1/2 s_i J sum_nb s_nb
+// (ising2d_hamiltonian.hpp:191-210); integer arithmetic, so exact.
+__host__ __device__ inline void ising_recalc(const int8_t* s, int L, int64_t J, int64_t& E, int32_t& M)
+{
+    const int N = L * L;
+    int64_t twiceE = 0; int32_t m = 0;
+    for (int i = 0; i < N; ++i) {
+        const int sum = s[nb_up(i, L)] + s[nb_left(i, L)] + s[nb_right(i, L)] + s[nb_down(i, L)];
+        twiceE -= (int64_t)s[i] * J * sum;
+        m += s[i];
+    }
+    E = twiceE / 2; M = m;
+}
+
+// Energy change of flipping spin a_i of plane `a` (other plane b) for the
+// Ashkin-Teller model H = -sum[J(s s' + t t') + K s t s' t'] - sum h s t
+// (ashkin_teller2d_hamiltonian.hpp:169-191,224-250).
+__host__ __device__ inline int64_t at_dE(const int8_t* a, const int8_t* b, int i, int L, int64_t J, int64_t K, int64_t h)
+{
+    const int u = nb_up(i, L), l = nb_left(i, L), r = nb_right(i, L), d = nb_down(i, L);
+    const int sa = a[u] + a[l] + a[r] + a[d];
+    const int sab = a[u] * b[u] + a[l] * b[l] + a[r] * b[r] + a[d] * b[d];
+    return 2 * (int64_t)a[i] * (h * b[i] + J * sa + K * (int64_t)b[i] * sab);
+}
+
+__host__ __device__ inline void at_recalc(const int8_t* s, const int8_t* t, int L, int64_t J, int64_t K,
+                                          const int64_t* h, int64_t& E, int32_t* M)
+{
+    const int N = L * L;
+    int64_t twiceE = 0; int32_t sm = 0, tm = 0, bx = 0;
+    for (int i = 0; i < N; ++i) {
+        const int u = nb_up(i, L), l = nb_left(i, L), r = nb_right(i, L), d = nb_down(i, L);
+        const int ss = s[u] + s[l] + s[r] + s[d];
+        const int tt = t[u] + t[l] + t[r] + t[d];
+        const int st = s[u] * t[u] + s[l] * t[l] + s[r] * t[r] + s[d] * t[d];
+        twiceE -= (int64_t)s[i] * J * ss + (int64_t)t[i] * J * tt + (int64_t)s[i] * t[i] * K * st;
+        if (h) twiceE -= 2 * h[i] * s[i] * t[i];
+        sm += s[i]; tm += t[i]; bx += s[i] * t[i];
+    }
+    E = twiceE / 2; M[0] = sm; M[1] = tm; M[2] = bx;
+}
+
+__host__ __device__ inline int64_t global_bin(const InstDev& I, int64_t E)
+{
+    return ((E - I.eglo_u) * I.bin_mul) >> I.bin_shift;
+}
+
+// --------------------------------------------------------------------------
+// k_init: initial configuration and the deterministic walk into the window
+// --------------------------------------------------------------------------
+__device__ bool adjust_walk(const InstDev& I, const WinDev& W, int8_t* sp, int64_t& E, int32_t* M, int32_t& flavour,
+                            const int64_t* h, uint32_t start, int64_t max_steps)
+{
+    const int L = I.L, N = I.N;
+    auto in_range = [&](int64_t e) { const int64_t b = global_bin(I, e) - W.gblo; return b >= 0 && b < W.nb; };
+    bool in = in_range(E);
+    int site = (int)start;
+    int64_t steps = 0;
+    while (!in) {
+        if (++steps > max_steps) return false;
+        ++site;
+        if (site == N) { site = 0; flavour ^= 1; }
+        int64_t dE;
+        int8_t* a;
+        if (I.model == REWL_MODEL_ISING2D) {
+            a = sp;
+            const int sum = sp[nb_up(site, L)] + sp[nb_left(site, L)] + sp[nb_right(site, L)] + sp[nb_down(site, L)];
+            dE = 2 * (int64_t)sp[site] * I.J_u * sum;
+        } else {
+            int8_t* s = sp; int8_t* t = sp + N;
+            a = flavour == 0 ? s : t;
+            int8_t* b = flavour == 0 ? t : s;
+            dE = at_dE(a, b, site, L, I.J_u, I.K_u, h ? h[site] : 0);
+            if (site == N - 1) flavour ^= 1;     // change_state toggles at the last site
+        }
+        const int64_t gb = global_bin(I, E) - W.gblo;
+        const bool too_low = gb < 0, too_high = gb >= W.nb;
+        const int64_t En = E + dE;
+        if ((too_low && En > E) || (too_high && En <= E)) {
+            E = En;
+            if (I.model == REWL_MODEL_ISING2D) { M[0] -= 2 * a[site]; a[site] = (int8_t)-a[site]; }
+            else {
+                // flavour was possibly toggled above; the flipped plane is the one chosen before the toggle
+                int8_t* s = sp; int8_t* t = sp + N;
+                const bool flipped_sigma = (a == s);
+                if (flipped_sigma) { M[0] -= 2 * s[site]; M[2] -= 2 * s[site] * t[site]; s[site] = (int8_t)-s[site]; }
+                else { M[1] -= 2 * t[site]; M[2] -= 2 * s[site] * t[site]; t[site] = (int8_t)-t[site]; }
+            }
+        }
+        in = in_range(E);
+    }
+    return true;
+}
+
+__global__ void k_init(DevPtrs P, int nslots, int init_mode_mask_unused)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    const int ii = P.slot_inst[s];
+    const InstDev I = P.inst[ii];
+    const WinDev W = P.win[P.slot_win[s]];
+    const int c = P.slot_cfg[s];
+    int8_t* sp = P.spins + P.cfg_off[c];
+    const uint32_t uid = (uint32_t)(s - I.first_slot);
+    const int64_t* h = I.field_off >= 0 ? P.fields + I.field_off : nullptr;
+    const int init_random = (int)(I.init_mode == 0);
+    for (int i = 0; i < I.ndof; ++i)
+        sp[i] = init_random ? ((philox_word(I.seed, uid, (uint64_t)i, kStreamInit) >> 31) ? -1 : 1) : 1;
+    int64_t E; int32_t M[3] = {0, 0, 0};
+    if (I.model == REWL_MODEL_ISING2D) ising_recalc(sp, I.L, I.J_u, E, M[0]);
+    else at_recalc(sp, sp + I.N, I.L, I.J_u, I.K_u, h, E, M);
+    int32_t flavour = 0;
+    const uint32_t start = mulhi32(philox_word(I.seed, uid, 0, kStreamAdjust), (uint32_t)I.N);
+    const int64_t cap = 4000LL * I.ndof;
+    bool ok = adjust_walk(I, W, sp, E, M, flavour, h, start, cap);
+    if (!ok) {
+        for (int i = 0; i < I.ndof; ++i) sp[i] = 1;
+        if (I.model == REWL_MODEL_ISING2D) ising_recalc(sp, I.L, I.J_u, E, M[0]);
+        else at_recalc(sp, sp + I.N, I.L, I.J_u, I.K_u, h, E, M);
+        flavour = 0;
+        ok = adjust_walk(I, W, sp, E, M, flavour, h, start, cap);
+        if (!ok) atomicOr(&P.counters[0], ERR_ADJUST);
+    }
+    P.cfg_E[c] = E;
+    P.cfg_M[3 * c] = M[0]; P.cfg_M[3 * c + 1] = M[1]; P.cfg_M[3 * c + 2] = M[2];
+    P.slot_flavour[s] = flavour;
+}
+
+// Recompute energies and magnetisations of given configurations (after imports).
+__global__ void k_recalc(DevPtrs P, const int32_t* cfgs, const int32_t* insts, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int c = cfgs[k];
+    const InstDev I = P.inst[insts[k]];
+    const int8_t* sp = P.spins + P.cfg_off[c];
+    const int64_t* h = I.field_off >= 0 ? P.fields + I.field_off : nullptr;
+    int64_t E; int32_t M[3] = {0, 0, 0};
+    if (I.model == REWL_MODEL_ISING2D) ising_recalc(sp, I.L, I.J_u, E, M[0]);
+    else at_recalc(sp, sp + I.N, I.L, I.J_u, I.K_u, h, E, M);
+    P.cfg_E[c] = E;
+    P.cfg_M[3 * c] = M[0]; P.cfg_M[3 * c + 1] = M[1]; P.cfg_M[3 * c + 2] = M[2];
+}
+
+// --------------------------------------------------------------------------
+// Sweep kernels
+// --------------------------------------------------------------------------
+struct SweepParams {
+    DevPtrs P;
+    const int32_t* slots;    // walkers of this launch
+    int nslots;
+    int nsweeps;
+    int smem_per_warp;       // bytes
+    int nbcap;               // table capacity per warp (Ising, shared memory)
+};
+
+// Per-warp staging of one chunk: energy change without / with the left
+// neighbour flipped, wrap correction (x = L-1 sees the row start), threshold.
+struct Stage {
+    long long T[32];
+    int d0[32];
+    int d1[32];
+    int wc[32];
+};
+
+template <bool REPLAY>
+__global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int li = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (li >= p.nslots) return;
+    const DevPtrs& P = p.P;
+    const int s = p.slots[li];
+    const InstDev I = P.inst[P.slot_inst[s]];
+    const int w = P.slot_win[s];
+    const WinDev W = P.win[w];
+    const int L = I.L, N = I.N, C = I.chunk, nb = W.nb;
+    unsigned char* base = smem + (size_t)wib * p.smem_per_warp;
+    long long* gs = reinterpret_cast<long long*>(base);
+    uint32_t* Hs = reinterpret_cast<uint32_t*>(gs + p.nbcap);
+    Stage* st = reinterpret_cast<Stage*>(Hs + p.nbcap);
+    int8_t* lat = reinterpret_cast<int8_t*>(st + 1);
+
+    const int cfg = P.slot_cfg[s];
+    int8_t* gl = P.spins + P.cfg_off[cfg];
+    for (int i = lane; i < N; i += 32) lat[i] = gl[i];
+    long long* gg = reinterpret_cast<long long*>(P.g + P.slot_tab[s]);
+    uint32_t* gH = P.H + P.slot_tab[s];
+    for (int b = lane; b < nb; b += 32) { gs[b] = gg[b]; Hs[b] = gH[b]; }
+    __syncwarp();
+
+    const int J = (int)I.J_u;
+    const int sh = I.bin_shift;
+    const int Ewlo = (int)W.elo_u;
+    const long long lnf = P.win_lnf[w];
+    const uint64_t sweeps0 = P.slot_sweeps[s];
+    const uint32_t uid = (uint32_t)(s - I.first_slot);
+    const uint64_t seed = I.seed;
+
+    int E = 0, M = 0, b = 0;
+    long long gc = 0;
+    long long draws = 0, thr_off = 0, thr_n = 0;
+    int err = 0;
+    if (lane == 0) {
+        E = (int)P.cfg_E[cfg];
+        M = P.cfg_M[3 * cfg];
+        b = (E - Ewlo) >> sh;
+        if (b < 0 || b >= nb) { err = ERR_BOUNDS; b = 0; }
+        gc = gs[b];
+        if (REPLAY) { draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
+    }
+    err = __shfl_sync(kFull, err, 0);
+    if (err) {
+        if (lane == 0) atomicOr(&P.counters[0], err);
+        return;
+    }
+
+    for (int sw = 0; sw < p.nsweeps; ++sw) {
+        const uint64_t A0 = (sweeps0 + (uint64_t)sw) * (uint64_t)N;
+        for (int c0 = 0; c0 < N; c0 += C) {
+            int si = 0;
+            if (lane < C) {
+                const int i = c0 + lane;
+                si = lat[i];
+                const int left = lat[nb_left(i, L)], right = lat[nb_right(i, L)];
+                const int sum = lat[nb_up(i, L)] + left + right + lat[nb_down(i, L)];
+                const int d0 = 2 * J * si * sum;
+                st->d0[lane] = d0;
+                st->d1[lane] = lane > 0 ? d0 - 4 * J * si * left : d0;
+                st->wc[lane] = (C == L && lane == L - 1) ? -4 * J * si * right : 0;
+                if (!REPLAY) {
+                    const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)i, kStreamWL);
+                    st->T[lane] = accept_threshold(neglog_u32(word));
+                }
+            }
+            __syncwarp();
+            unsigned acc = 0;
+            if (lane == 0) {
+                for (int j = 0; j < C; ++j) {
+                    int dE = (j > 0 && ((acc >> (j - 1)) & 1u)) ? st->d1[j] : st->d0[j];
+                    dE += (acc & 1u) ? st->wc[j] : 0;
+                    const int En = E + dE;
+                    const int bn = (En - Ewlo) >> sh;
+                    const bool inr = (unsigned)bn < (unsigned)nb;
+                    const long long gn = gs[inr ? bn : b];
+                    const long long d = gn - gc;
+                    bool a;
+                    if (!REPLAY) {
+                        a = inr && (d < st->T[j]);
+                    } else {
+                        if (inr && d > 0) {
+                            if (draws >= thr_n) { err = ERR_REPLAY_EXHAUSTED; a = false; }
+                            else { a = d < P.thr[thr_off + draws]; ++draws; }
+                        } else a = inr;
+                    }
+                    if (a) { E = En; b = bn; gc = gn; acc |= 1u << j; }
+                    gc += lnf;
+                    gs[b] = gc;
+                    Hs[b] += 1u;
+                }
+            }
+            acc = __shfl_sync(kFull, acc, 0);
+            const unsigned plus = __ballot_sync(kFull, lane < C && si > 0);
+            if (lane < C && ((acc >> lane) & 1u)) lat[c0 + lane] = (int8_t)(-si);
+            if (lane == 0) M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus));
+            __syncwarp();
+        }
+    }
+    // write back
+    for (int i = lane; i < N; i += 32) gl[i] = lat[i];
+    uint64_t* gv = P.visits + P.slot_tab[s];
+    for (int k = lane; k < nb; k += 32) {
+        const uint32_t hn = Hs[k], ho = gH[k];
+        gv[k] += (uint64_t)(hn - ho);
+        gH[k] = hn;
+        gg[k] = gs[k];
+    }
+    if (lane == 0) {
+        P.cfg_E[cfg] = E;
+        P.cfg_M[3 * cfg] = M;
+        P.slot_sweeps[s] = sweeps0 + (uint64_t)p.nsweeps;
+        if (REPLAY) P.slot_draws[s] = draws;
+        if (err) atomicOr(&P.counters[0], err);
+    }
+}
+
+// Ashkin-Teller: sweep = sigma pass then tau pass (wang_landau.hpp:109-119); the
+// flavour toggles after each pass.  Tables stay in global memory.
+struct StageAT {
+    long long T[32];
+    long long d0[32];
+    long long d1[32];
+    long long wc[32];
+};
+
+template <bool REPLAY>
+__global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int li = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (li >= p.nslots) return;
+    const DevPtrs& P = p.P;
+    const int s = p.slots[li];
+    const InstDev I = P.inst[P.slot_inst[s]];
+    const int w = P.slot_win[s];
+    const WinDev W = P.win[w];
+    const int L = I.L, N = I.N, C = I.chunk, nb = W.nb;
+    unsigned char* base = smem + (size_t)wib * p.smem_per_warp;
+    StageAT* st = reinterpret_cast<StageAT*>(base);
+    int8_t* sig = reinterpret_cast<int8_t*>(st + 1);
+    int8_t* tau = sig + N;
+    const int64_t* hf = I.field_off >= 0 ? P.fields + I.field_off : nullptr;
+
+    const int cfg = P.slot_cfg[s];
+    int8_t* gl = P.spins + P.cfg_off[cfg];
+    for (int i = lane; i < 2 * N; i += 32) sig[i] = gl[i];
+    long long* gg = reinterpret_cast<long long*>(P.g + P.slot_tab[s]);
+    uint32_t* gH = P.H + P.slot_tab[s];
+    uint64_t* gv = P.visits + P.slot_tab[s];
+    __syncwarp();
+
+    const long long J = I.J_u, K = I.K_u;
+    const long long lnf = P.win_lnf[w];
+    const uint64_t sweeps0 = P.slot_sweeps[s];
+    const uint32_t uid = (uint32_t)(s - I.first_slot);
+    const uint64_t seed = I.seed;
+    const long long eglo = I.eglo_u, mul = I.bin_mul, gblo = W.gblo;
+    const int sh = I.bin_shift;
+    int flavour = P.slot_flavour[s];
+
+    long long E = 0;
+    int sm = 0, tm = 0, bx = 0, b = 0;
+    long long gc = 0;
+    long long draws = 0, thr_off = 0, thr_n = 0;
+    int err = 0;
+    if (lane == 0) {
+        E = P.cfg_E[cfg];
+        sm = P.cfg_M[3 * cfg]; tm = P.cfg_M[3 * cfg + 1]; bx = P.cfg_M[3 * cfg + 2];
+        const long long gb = (((E - eglo) * mul) >> sh) - gblo;
+        if (gb < 0 || gb >= nb) err = ERR_BOUNDS;
+        b = (int)(err ? 0 : gb);
+        gc = gg[b];
+        if (REPLAY) { draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
+    }
+    err = __shfl_sync(kFull, err, 0);
+    if (err) {
+        if (lane == 0) atomicOr(&P.counters[0], err);
+        return;
+    }
+
+    for (int sw = 0; sw < p.nsweeps; ++sw) {
+        for (int pass = 0; pass < 2; ++pass) {
+            int8_t* A = flavour == 0 ? sig : tau;
+            int8_t* B = flavour == 0 ? tau : sig;
+            const uint64_t A0 = ((sweeps0 + (uint64_t)sw) * 2u + (uint64_t)pass) * (uint64_t)N;
+            for (int c0 = 0; c0 < N; c0 += C) {
+                int ai = 0, bi = 0;
+                if (lane < C) {
+                    const int i = c0 + lane;
+                    ai = A[i]; bi = B[i];
+                    const int l = nb_left(i, L), r = nb_right(i, L);
+                    const long long d0 = at_dE(A, B, i, L, J, K, hf ? hf[i] : 0);
+                    st->d0[lane] = d0;
+                    st->d1[lane] = lane > 0 ? d0 - 4 * (long long)ai * A[l] * (J + K * (long long)bi * B[l]) : d0;
+                    st->wc[lane] = (C == L && lane == L - 1) ? -4 * (long long)ai * A[r] * (J + K * (long long)bi * B[r]) : 0;
+                    if (!REPLAY) {
+                        const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)i, kStreamWL);
+                        st->T[lane] = accept_threshold(neglog_u32(word));
+                    }
+                }
+                __syncwarp();
+                unsigned acc = 0;
+                if (lane == 0) {
+                    for (int j = 0; j < C; ++j) {
+                        long long dE = (j > 0 && ((acc >> (j - 1)) & 1u)) ? st->d1[j] : st->d0[j];
+                        dE += (acc & 1u) ? st->wc[j] : 0;
+                        const long long En = E + dE;
+                        const long long bn = (((En - eglo) * mul) >> sh) - gblo;
+                        const bool inr = bn >= 0 && bn < nb;
+                        const long long gn = gg[inr ? bn : b];
+                        const long long d = gn - gc;
+                        bool a;
+                        if (!REPLAY) {
+                            a = inr && (d < st->T[j]);
+                        } else {
+                            if (inr && d > 0) {
+                                if (draws >= thr_n) { err = ERR_REPLAY_EXHAUSTED; a = false; }
+                                else { a = d < P.thr[thr_off + draws]; ++draws; }
+                            } else a = inr;
+                        }
+                        if (a) { E = En; b = (int)bn; gc = gn; acc |= 1u << j; }
+                        gc += lnf;
+                        gg[b] = gc;
+                        gH[b] += 1u;
+                        gv[b] += 1u;
+                    }
+                }
+                acc = __shfl_sync(kFull, acc, 0);
+                const unsigned aplus = __ballot_sync(kFull, lane < C && ai > 0);
+                const unsigned abplus = __ballot_sync(kFull, lane < C && ai * bi > 0);
+                if (lane < C && ((acc >> lane) & 1u)) A[c0 + lane] = (int8_t)(-ai);
+                if (lane == 0) {
+                    const int da = -2 * ((int)__popc(acc & aplus) - (int)__popc(acc & ~aplus));
+                    const int db = -2 * ((int)__popc(acc & abplus) - (int)__popc(acc & ~abplus));
+                    if (flavour == 0) sm += da; else tm += da;
+                    bx += db;
+                }
+                __syncwarp();
+            }
+            flavour ^= 1;
+        }
+    }
+    for (int i = lane; i < 2 * N; i += 32) gl[i] = sig[i];
+    if (lane == 0) {
+        P.cfg_E[cfg] = E;
+        P.cfg_M[3 * cfg] = sm; P.cfg_M[3 * cfg + 1] = tm; P.cfg_M[3 * cfg + 2] = bx;
+        P.slot_sweeps[s] = sweeps0 + (uint64_t)p.nsweeps;
+        P.slot_flavour[s] = flavour;
+        if (REPLAY) P.slot_draws[s] = draws;
+        if (err) atomicOr(&P.counters[0], err);
+    }
+}
+
+// --------------------------------------------------------------------------
+// Replica exchange: one thread per (instance, lower window) pair of the round
+// --------------------------------------------------------------------------
+__device__ inline int64_t slot_local_bin(const DevPtrs& P, const InstDev& I, int slot, int64_t E)
+{
+    const WinDev& W = P.win[P.slot_win[slot]];
+    return global_bin(I, E) - W.gblo;
+}
+
+__device__ inline void touch(const DevPtrs& P, const InstDev& I, int slot)
+{
+    const int c = P.slot_cfg[slot];
+    const int64_t b = slot_local_bin(P, I, slot, P.cfg_E[c]);
+    const int w = P.slot_win[slot];
+    if (b < 0 || b >= P.slot_nb[slot]) { atomicOr(&P.counters[0], ERR_BOUNDS); return; }
+    const int64_t o = P.slot_tab[slot] + b;
+    P.g[o] += P.win_lnf[w];
+    P.H[o] += 1u;
+    P.visits[o] += 1u;
+}
+
+__global__ void k_exchange(DevPtrs P, const int32_t* pairs, int npairs, uint64_t round)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npairs) return;
+    const int ii = pairs[2 * k], lw = pairs[2 * k + 1];
+    const InstDev I = P.inst[ii];
+    const int R = I.R;
+    int perm[kMaxReplicas];
+    for (int r = 0; r < R; ++r) perm[r] = r;
+    const uint32_t xuid = 0x80000000u | (uint32_t)ii;
+    const uint32_t w3 = (uint32_t)((round << 8) ^ (uint64_t)lw);
+    for (int i = R - 1; i >= 1; --i) {
+        const uint32_t word = philox_word(I.seed, xuid, (uint64_t)(R - 1 - i), kStreamExchange, w3);
+        const int j = (int)mulhi32(word, (uint32_t)(i + 1));
+        const int t = perm[i]; perm[i] = perm[j]; perm[j] = t;
+    }
+    unsigned long long att = 0, accn = 0;
+    for (int r = 0; r < R; ++r) {
+        const int lo = I.first_slot + lw * R + r;
+        const int hi = I.first_slot + (lw + 1) * R + perm[r];
+        const int cl = P.slot_cfg[lo], ch = P.slot_cfg[hi];
+        const int64_t El = P.cfg_E[cl], Eh = P.cfg_E[ch];
+        const int64_t bl_l = slot_local_bin(P, I, lo, El), bl_h = slot_local_bin(P, I, lo, Eh);
+        const int64_t bh_l = slot_local_bin(P, I, hi, El), bh_h = slot_local_bin(P, I, hi, Eh);
+        ++att;
+        bool accept = false;
+        if (bl_l < 0 || bl_l >= P.slot_nb[lo] || bh_h < 0 || bh_h >= P.slot_nb[hi]) {
+            atomicOr(&P.counters[0], ERR_BOUNDS);    // a walker outside its own window: skip the pair
+            continue;
+        }
+        if (bl_h >= 0 && bl_h < P.slot_nb[lo] && bh_l >= 0 && bh_l < P.slot_nb[hi]) {
+            const int64_t* gl = P.g + P.slot_tab[lo];
+            const int64_t* gh = P.g + P.slot_tab[hi];
+            const int64_t a = gl[bl_h] - gl[bl_l];
+            const int64_t c = gh[bh_l] - gh[bh_h];
+            const int64_t d = (a > 0 ? a : 0) + (c > 0 ? c : 0);
+            const uint32_t word = philox_word(I.seed, xuid, (uint64_t)(32 + r), kStreamExchange, w3);
+            accept = d < accept_threshold(neglog_u32(word));
+        }
+        if (accept) { P.slot_cfg[lo] = ch; P.slot_cfg[hi] = cl; ++accn; }
+        touch(P, I, lo);
+        touch(P, I, hi);
+    }
+    atomicAdd(&P.stats[0], att);
+    atomicAdd(&P.stats[1], accn);
+}
+
+// --------------------------------------------------------------------------
+// Flatness, averaging, reset, ln f: one block per window
+// --------------------------------------------------------------------------
+struct FlatParams {
+    DevPtrs P;
+    int nwin_total;
+    int flat_mode;
+    int mask_mode;
+    int one_over_t;
+    int reduce;
+    uint64_t flat_num, flat_den;   // min * n * den >= num * sum
+    float flat_param_f;
+    double lnf_final;
+    uint64_t sweeps_since_check;
+};
+
+struct OpMin { __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a < b ? a : b; } };
+struct OpMax { __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a > b ? a : b; } };
+struct OpAdd { __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return a + b; } };
+
+template <typename T, typename Op>
+__device__ T block_reduce(T v, Op op, T* sh, T identity)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_down_sync(kFull, v, o));
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    if (wid == 0) {
+        v = lane < nw ? sh[lane] : identity;
+        for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_down_sync(kFull, v, o));
+        if (lane == 0) sh[0] = v;
+    }
+    __syncthreads();
+    const T r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__device__ inline bool bin_valid(const DevPtrs& P, const WinDev& W, int first_slot_of_win, int R, int b, int mask_mode)
+{
+    if (!P.mask[W.mask_off + b]) return false;
+    if (mask_mode == REWL_MASK_VISITED) {
+        for (int r = 0; r < R; ++r)
+            if (P.visits[P.slot_tab[first_slot_of_win + r] + b]) return true;
+        return false;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
+{
+    __shared__ unsigned long long red_u[32];
+    __shared__ int flat_sh;
+    __shared__ long long g0_sh[kMaxReplicas];
+    const DevPtrs& P = fp.P;
+    const int w = blockIdx.x;
+    const WinDev W = P.win[w];
+    const InstDev I = P.inst[W.inst];
+    const int R = I.R;
+    const int first = I.first_slot + W.local * R;
+    const int nb = W.nb;
+
+    if (threadIdx.x == 0) { P.win_sweepctr[w] += fp.sweeps_since_check; flat_sh = 1; }
+    __syncthreads();
+
+    for (int r = 0; r < R; ++r) {
+        const uint32_t* H = P.H + P.slot_tab[first + r];
+        unsigned long long mn = ~0ull, mx = 0, sum = 0, n = 0, zero = 0;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            if (!bin_valid(P, W, first, R, b, fp.mask_mode)) continue;
+            const unsigned long long h = H[b];
+            mn = h < mn ? h : mn; mx = h > mx ? h : mx; sum += h; ++n; zero += (h == 0);
+        }
+        mn = block_reduce(mn, OpMin(), red_u, ~0ull);
+        mx = block_reduce(mx, OpMax(), red_u, 0ull);
+        sum = block_reduce(sum, OpAdd(), red_u, 0ull);
+        n = block_reduce(n, OpAdd(), red_u, 0ull);
+        zero = block_reduce(zero, OpAdd(), red_u, 0ull);
+        if (threadIdx.x == 0) {
+            bool f;
+            if (fp.flat_mode == REWL_FLAT_ALL_VISITED) f = P.win_oot[w] ? true : (zero == 0);
+            else if (n == 0 || mn == 0) f = false;
+            else if (fp.flat_mode == REWL_FLAT_MAX_MIN_RATIO)
+                f = __fdiv_rn(__ull2float_rn(mx - mn), __ull2float_rn(mn)) <= fp.flat_param_f;
+            else
+                f = (unsigned __int128)mn * n * fp.flat_den >= (unsigned __int128)fp.flat_num * sum;
+            if (!f) flat_sh = 0;
+        }
+        __syncthreads();
+    }
+    if (!flat_sh) return;
+
+    // count-weighted average of the replicas' logDoS (rewl_simulation.hpp:361-454)
+    if (R > 1) {
+        const double inv = 1.0 / kLogdosScale;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            unsigned long long tot = 0;
+            for (int r = 0; r < R; ++r) tot += P.H[P.slot_tab[first + r] + b];
+            long long avg;
+            if (tot == 0) avg = P.g[P.slot_tab[first] + b];
+            else {
+                double acc = 0.0;
+                const double dtot = __ull2double_rn(tot);
+                for (int r = 0; r < R; ++r) {
+                    const int64_t o = P.slot_tab[first + r] + b;
+                    const double wt = __ddiv_rn(__uint2double_rn(P.H[o]), dtot);
+                    const double gr = __dmul_rn(__ll2double_rn(P.g[o]), inv);
+                    acc = __dadd_rn(acc, __dmul_rn(wt, gr));
+                }
+                avg = __double2ll_rn(__dmul_rn(acc, kLogdosScale));
+            }
+            for (int r = 0; r < R; ++r) P.g[P.slot_tab[first + r] + b] = avg;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < R) g0_sh[threadIdx.x] = P.g[P.slot_tab[first + threadIdx.x]];
+    __syncthreads();
+    for (int r = 0; r < R; ++r) {
+        const int64_t o = P.slot_tab[first + r];
+        const long long red = fp.reduce ? g0_sh[r] : 0;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) { P.H[o + b] = 0; P.g[o + b] -= red; }
+    }
+    if (threadIdx.x == 0) {
+        const uint64_t t = P.win_sweepctr[w] * P.win_iter[w];
+        long long lnf = P.win_lnf[w];
+        int oot = P.win_oot[w];
+        if (fp.one_over_t && !oot && t > 0 && __ll2double_rn(lnf) <= __ddiv_rn(kLogdosScale, __ull2double_rn(t))) oot = 1;
+        if (oot && t > 0) lnf = (long long)((((unsigned long long)1 << kLogdosBits) + t / 2) / t);
+        else lnf = lnf >> 1;
+        P.win_lnf[w] = lnf;
+        P.win_oot[w] = oot;
+        P.win_done[w] = (__ll2double_rn(lnf) / kLogdosScale) < fp.lnf_final ? 1 : 0;
+        P.win_iter[w] += 1;
+        P.win_sweepctr[w] = 0;
+        atomicAdd(&P.counters[1], 1);
+    }
+}
+
+__global__ void k_reset_window(DevPtrs P, int w, int reduce)
+{
+    const WinDev W = P.win[w];
+    const InstDev I = P.inst[W.inst];
+    const int first = I.first_slot + W.local * I.R;
+    for (int r = 0; r < I.R; ++r) {
+        const int64_t o = P.slot_tab[first + r];
+        const long long g0 = P.g[o];
+        __syncthreads();
+        for (int b = threadIdx.x; b < W.nb; b += blockDim.x) { P.H[o + b] = 0; if (reduce) P.g[o + b] -= g0; }
+        __syncthreads();
+    }
+}
+
+// --------------------------------------------------------------------------
+// Host side
+// --------------------------------------------------------------------------
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        n = count;
+        if (count == 0) return REWL_OK;
+        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) return fail(REWL_ENOMEM, "cudaMalloc of %zu bytes failed", count * sizeof(T));
+        return REWL_OK;
+    }
+    void free_()
+    {
+        if (p) cudaFree(p);
+        p = nullptr; n = 0;
+    }
+};
+
+struct HostInst {
+    rewl_instance_desc d;
+    InstDev dev;
+    std::vector<double> fields;     // quantised
+    double bw;
+    std::vector<WinDev> wins;
+    std::vector<double> wmin, wmax;
+};
+
+struct Launch {
+    int model;
+    std::vector<int32_t> slots;
+    int smem_per_warp;
+    int nbcap;
+    int wpb;
+    DBuf<int32_t> d_slots;
+};
+
+} // namespace
+
+struct rewl_engine {
+    rewl_batch_desc desc;
+    std::vector<HostInst> inst;
+    int nslots = 0, nwin_total = 0;
+    std::vector<int32_t> h_slot_inst, h_slot_win, h_slot_nb;
+    std::vector<int64_t> h_slot_tab;
+    std::vector<int64_t> h_cfg_off;
+    std::vector<WinDev> h_wins;
+    int64_t table_total = 0, spin_total = 0, mask_total = 0;
+    std::vector<int32_t> pairs_dir[2];
+    int direction = 0;
+    uint64_t exch_round = 0;
+    uint64_t sweeps_since_check = 0;
+    int64_t sweeps_total = 0, cycles = 0, flat_events = 0, flips_total = 0;
+    int64_t flips_per_sweep = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<Launch> launches;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    int64_t kernel_launches = 0;
+
+    DBuf<InstDev> d_inst;
+    DBuf<WinDev> d_win;
+    DBuf<int32_t> slot_inst, slot_win, slot_cfg, slot_nb, slot_flavour, pairs[2];
+    DBuf<int64_t> slot_tab, slot_draws, slot_thr_off, slot_thr_n, cfg_off, cfg_E, fields, g, win_lnf;
+    DBuf<uint64_t> slot_sweeps, visits, win_iter, win_sweepctr;
+    DBuf<int8_t> spins;
+    DBuf<int32_t> cfg_M, win_done, win_oot, counters;
+    DBuf<uint32_t> H;
+    DBuf<uint8_t> mask;
+    DBuf<unsigned long long> stats;
+    DBuf<int64_t> thr;
+    std::vector<int64_t> h_thr_off, h_thr_n;
+    std::vector<int64_t> h_fields;
+    std::vector<uint8_t> h_mask;
+
+    DevPtrs ptrs() const
+    {
+        DevPtrs P;
+        P.inst = d_inst.p; P.win = d_win.p;
+        P.slot_inst = slot_inst.p; P.slot_win = slot_win.p; P.slot_cfg = slot_cfg.p; P.slot_tab = slot_tab.p;
+        P.slot_nb = slot_nb.p; P.slot_flavour = slot_flavour.p; P.slot_sweeps = slot_sweeps.p;
+        P.slot_draws = slot_draws.p; P.slot_thr_off = slot_thr_off.p; P.slot_thr_n = slot_thr_n.p; P.thr = thr.p;
+        P.cfg_off = cfg_off.p; P.spins = spins.p; P.cfg_E = cfg_E.p; P.cfg_M = cfg_M.p; P.fields = fields.p;
+        P.g = g.p; P.H = H.p; P.visits = visits.p; P.mask = mask.p;
+        P.win_lnf = win_lnf.p; P.win_done = win_done.p; P.win_oot = win_oot.p; P.win_iter = win_iter.p;
+        P.win_sweepctr = win_sweepctr.p; P.pairs = nullptr; P.counters = counters.p; P.stats = stats.p;
+        return P;
+    }
+
+    void release()
+    {
+        d_inst.free_(); d_win.free_();
+        slot_inst.free_(); slot_win.free_(); slot_cfg.free_(); slot_nb.free_(); slot_flavour.free_();
+        pairs[0].free_(); pairs[1].free_();
+        slot_tab.free_(); slot_draws.free_(); slot_thr_off.free_(); slot_thr_n.free_(); cfg_off.free_();
+        cfg_E.free_(); fields.free_(); g.free_(); win_lnf.free_(); slot_sweeps.free_(); visits.free_();
+        win_iter.free_(); win_sweepctr.free_(); spins.free_(); cfg_M.free_(); win_done.free_(); win_oot.free_();
+        counters.free_(); H.free_(); mask.free_(); stats.free_(); thr.free_();
+        for (auto& l : launches) l.d_slots.free_();
+        for (auto e : ev_pool) cudaEventDestroy(e);
+        ev_pool.clear();
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+namespace {
+
+bool is_pow2_multiple(double v, int escale, int& shift)
+{
+    const double u = std::ldexp(v, escale);
+    if (u < 1.0 || u != std::floor(u)) return false;
+    const long long x = (long long)u;
+    if (x & (x - 1)) return false;
+    shift = 0;
+    while ((1LL << shift) < x) ++shift;
+    return true;
+}
+
+int largest_chunk(int L)
+{
+    for (int c = std::min(L, 32); c >= 1; --c)
+        if (L % c == 0) return c;
+    return 1;
+}
+
+// glazier::construct_windows, EQUAL_WINDOWS branch (src/REWL/glazier.hpp:305-351),
+// followed by snapping each window onto the exact global bin grid.
+void make_windows(const rewl_instance_desc& d, std::vector<double>& mins, std::vector<double>& maxs,
+                  std::vector<int64_t>& gblo, std::vector<int>& nbins)
+{
+    const int nw = d.num_windows;
+    const double gmin = d.energy_min, gmax = d.energy_max, bw = d.bin_width, ov = d.window_overlap;
+    mins.assign(nw, 0); maxs.assign(nw, 0); gblo.assign(nw, 0); nbins.assign(nw, 0);
+    const double denom = 1 + (nw - 1) * (1 - ov);
+    const double size = (gmax - gmin) / denom;
+    std::vector<double> raw_min(nw);
+    for (int k = 0; k < nw; ++k) {
+        double wmin = gmin + (double)k * (1 - ov) * size;
+        double wmax = wmin + size;
+        if (k != 0) wmin = raw_min[k - 1] + bw * (double)((size_t)((wmin - raw_min[k - 1]) / bw));
+        size_t nb = (size_t)std::ceil((wmax - wmin) / bw);
+        wmax = wmin + bw * (double)nb;
+        while (wmax > gmax) wmax -= bw;
+        raw_min[k] = wmin;
+        gblo[k] = (int64_t)std::llround((wmin - gmin) / bw);
+        nbins[k] = (int)(std::llround((wmax - gmin) / bw) - gblo[k]);
+        mins[k] = gmin + bw * (double)gblo[k];
+        maxs[k] = gmin + bw * (double)(gblo[k] + nbins[k]);
+    }
+}
+
+void static_mask(const rewl_instance_desc& d, double wmin, int nb, uint8_t* m)
+{
+    for (int b = 0; b < nb; ++b) m[b] = 1;
+    if (d.model != REWL_MODEL_ISING2D) return;
+    // Ising on an L x L torus: E = -2N + 4 and E = 2N - 4 never occur; all
+    // energies are -2N + 4k (with J = 1; scaled by |J| in general).
+    const double N = (double)d.L * d.L, J = std::fabs(d.J);
+    for (int b = 0; b < nb; ++b) {
+        const double lo = wmin + d.bin_width * b, hi = lo + d.bin_width;
+        bool any = false;
+        for (double e = std::ceil((lo + 2 * N * J) / (4 * J)) * 4 * J - 2 * N * J; e < hi; e += 4 * J) {
+            if (e < -2 * N * J || e > 2 * N * J) continue;
+            if (e == -2 * N * J + 4 * J || e == 2 * N * J - 4 * J) continue;
+            any = true;
+        }
+        m[b] = any ? 1 : 0;
+    }
+}
+
+template <typename T>
+int upload(DBuf<T>& b, const std::vector<T>& v, cudaStream_t s)
+{
+    int rc = b.alloc(v.size());
+    if (rc) return rc;
+    if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return REWL_OK;
+}
+
+int build_host(rewl_engine* e)
+{
+    const rewl_batch_desc& D = e->desc;
+    if (D.num_instances < 1 || !D.instances) return fail(REWL_EINVAL, "no instances");
+    if (D.sweeps_per_exchange < 1 || D.sweeps_per_check < D.sweeps_per_exchange || D.sweeps_per_check % D.sweeps_per_exchange)
+        return fail(REWL_EINVAL, "sweeps_per_check must be a positive multiple of sweeps_per_exchange");
+    if (!(D.lnf_initial > 0) || !(D.lnf_final > 0)) return fail(REWL_EINVAL, "ln f must be positive");
+    if (D.flatness_mode < 0 || D.flatness_mode > 2) return fail(REWL_EINVAL, "bad flatness mode");
+    if (D.mask_mode < 0 || D.mask_mode > 1) return fail(REWL_EINVAL, "bad mask mode");
+    if (D.rng_mode != REWL_RNG_PHILOX && D.rng_mode != REWL_RNG_REPLAY) return fail(REWL_EINVAL, "bad rng mode");
+    if (D.walkers_per_block != 0 && D.walkers_per_block != 1 && D.walkers_per_block != 2 && D.walkers_per_block != 4 && D.walkers_per_block != 8)
+        return fail(REWL_EINVAL, "walkers_per_block must be 0, 1, 2, 4 or 8");
+    int slot = 0, win = 0;
+    int64_t tab = 0, spin = 0, maskoff = 0, fieldoff = 0;
+    std::vector<int64_t> h_fields;
+    std::vector<uint8_t> h_mask;
+    e->inst.resize(D.num_instances);
+    for (int ii = 0; ii < D.num_instances; ++ii) {
+        const rewl_instance_desc& d = D.instances[ii];
+        HostInst& H = e->inst[ii];
+        H.d = d;
+        if (d.model != REWL_MODEL_ISING2D && d.model != REWL_MODEL_ASHKIN_TELLER2D) return fail(REWL_EINVAL, "instance %d: bad model", ii);
+        if (d.L < 2 || d.L > 128) return fail(REWL_EINVAL, "instance %d: L must be in [2, 128]", ii);
+        if (d.num_windows < 1 || d.replicas_per_window < 1 || d.replicas_per_window > kMaxReplicas)
+            return fail(REWL_EINVAL, "instance %d: need >= 1 window and 1..%d replicas", ii, kMaxReplicas);
+        if (!(d.window_overlap >= 0 && d.window_overlap < 1)) return fail(REWL_EINVAL, "instance %d: overlap must be in [0,1)", ii);
+        if (!(d.energy_max > d.energy_min) || !(d.bin_width > 0)) return fail(REWL_EINVAL, "instance %d: bad energy range", ii);
+        if (d.init_mode != 0 && d.init_mode != 1) return fail(REWL_EINVAL, "instance %d: bad init mode", ii);
+        InstDev I{};
+        I.model = d.model; I.L = d.L; I.N = d.L * d.L; I.ndof = d.model == REWL_MODEL_ISING2D ? I.N : 2 * I.N;
+        I.nwin = d.num_windows; I.R = d.replicas_per_window; I.first_win = win; I.first_slot = slot;
+        I.seed = d.seed; I.chunk = largest_chunk(d.L); I.init_mode = d.init_mode;
+        int shift = 0;
+        if (d.model == REWL_MODEL_ISING2D) {
+            if (d.J != std::floor(d.J) || d.J == 0 || std::fabs(d.J) > 1024) return fail(REWL_EINVAL, "instance %d: Ising J must be a non-zero integer", ii);
+            if (d.fields) return fail(REWL_EINVAL, "instance %d: random fields are supported for the Ashkin-Teller model only", ii);
+            I.escale = 0; I.J_u = (int64_t)d.J; I.K_u = 0;
+            if (!is_pow2_multiple(d.bin_width, 0, shift)) return fail(REWL_EINVAL, "instance %d: Ising bin width must be a power of two >= 1", ii);
+            I.bin_mul = 1; I.bin_shift = shift;
+            if (d.energy_min != std::floor(d.energy_min)) return fail(REWL_EINVAL, "instance %d: energy_min must be an integer", ii);
+            if (std::fabs(d.energy_min) + std::fabs(d.energy_max) > 1e8) return fail(REWL_EINVAL, "instance %d: energy range too large", ii);
+        } else {
+            I.escale = 20;
+            const double Ju = std::ldexp(d.J, 20), Ku = std::ldexp(d.K, 20);
+            if (Ju != std::floor(Ju) || Ku != std::floor(Ku)) return fail(REWL_EINVAL, "instance %d: J and K must be multiples of 2^-20", ii);
+            I.J_u = (int64_t)Ju; I.K_u = (int64_t)Ku;
+            const double inv = 1.0 / d.bin_width;
+            if (is_pow2_multiple(d.bin_width, 20, shift)) { I.bin_mul = 1; I.bin_shift = shift; }
+            else if (std::fabs(inv - std::nearbyint(inv)) < 1e-9 * inv && inv <= 4096) { I.bin_mul = (int64_t)std::llround(inv); I.bin_shift = 20; }
+            else return fail(REWL_EINVAL, "instance %d: Ashkin-Teller bin width must be 1/n or a power of two", ii);
+            const double emu = std::ldexp(d.energy_min, 20);
+            if (emu != std::floor(emu)) return fail(REWL_EINVAL, "instance %d: energy_min must be a multiple of 2^-20", ii);
+        }
+        I.eglo_u = (int64_t)std::llround(std::ldexp(d.energy_min, I.escale));
+        if (d.fields) {
+            I.field_off = fieldoff;
+            H.fields.resize(I.N);
+            for (int i = 0; i < I.N; ++i) {
+                const double q = std::nearbyint(std::ldexp(d.fields[i], 20));
+                if (!std::isfinite(q) || std::fabs(q) > 1e15) return fail(REWL_EINVAL, "instance %d: bad field value", ii);
+                H.fields[i] = std::ldexp(q, -20);
+                h_fields.push_back((int64_t)q);
+            }
+            fieldoff += I.N;
+        } else I.field_off = -1;
+        std::vector<double> mins, maxs; std::vector<int64_t> gblo; std::vector<int> nbins;
+        make_windows(d, mins, maxs, gblo, nbins);
+        for (int k = 0; k < d.num_windows; ++k) {
+            if (nbins[k] < 1) return fail(REWL_EINVAL, "instance %d: window %d is empty", ii, k);
+            if (k > 0 && gblo[k] >= gblo[k - 1] + nbins[k - 1]) return fail(REWL_EINVAL, "instance %d: windows %d and %d do not overlap", ii, k - 1, k);
+        }
+        H.bw = d.bin_width;
+        H.wmin = mins; H.wmax = maxs;
+        for (int k = 0; k < d.num_windows; ++k) {
+            WinDev W{};
+            W.inst = ii; W.local = k; W.nb = nbins[k]; W.gblo = gblo[k]; W.mask_off = maskoff;
+            W.elo_u = I.eglo_u + (I.bin_mul == 1 ? (gblo[k] << I.bin_shift) : 0);
+            std::vector<uint8_t> m(nbins[k]);
+            static_mask(d, mins[k], nbins[k], m.data());
+            h_mask.insert(h_mask.end(), m.begin(), m.end());
+            maskoff += nbins[k];
+            H.wins.push_back(W);
+            e->h_wins.push_back(W);
+            for (int r = 0; r < d.replicas_per_window; ++r) {
+                e->h_slot_inst.push_back(ii);
+                e->h_slot_win.push_back(win + k);
+                e->h_slot_nb.push_back(nbins[k]);
+                e->h_slot_tab.push_back(tab);
+                tab += nbins[k];
+                e->h_cfg_off.push_back(spin);
+                spin += I.ndof;
+            }
+        }
+        if (d.model == REWL_MODEL_ISING2D) {
+            // integer arithmetic in int32 inside the kernel
+            const double emax_abs = 2.0 * I.N * std::fabs(d.J);
+            if (emax_abs > 1e9 || std::fabs(d.energy_min) > 1e9 || std::fabs(d.energy_max) > 1e9)
+                return fail(REWL_EINVAL, "instance %d: energies exceed int32", ii);
+        }
+        H.dev = I;
+        slot += d.num_windows * d.replicas_per_window;
+        win += d.num_windows;
+        e->flips_per_sweep += (int64_t)d.num_windows * d.replicas_per_window * I.ndof;
+    }
+    e->nslots = slot; e->nwin_total = win;
+    e->table_total = tab; e->spin_total = spin; e->mask_total = maskoff;
+    // exchange pair lists
+    for (int dir = 0; dir < 2; ++dir) {
+        e->pairs_dir[dir].clear();
+        for (int ii = 0; ii < D.num_instances; ++ii)
+            for (int lw = dir; lw + 1 < D.instances[ii].num_windows; lw += 2) { e->pairs_dir[dir].push_back(ii); e->pairs_dir[dir].push_back(lw); }
+    }
+    e->h_fields = std::move(h_fields);
+    e->h_mask = std::move(h_mask);
+    return REWL_OK;
+}
+
+int upload_all(rewl_engine* e)
+{
+    const rewl_batch_desc& D = e->desc;
+    const int slot = e->nslots, win = e->nwin_total;
+    const int64_t tab = e->table_total, spin = e->spin_total;
+    cudaStream_t s = e->stream;
+    std::vector<InstDev> hinst;
+    for (auto& H : e->inst) hinst.push_back(H.dev);
+    int rc;
+    if ((rc = upload(e->d_inst, hinst, s)) || (rc = upload(e->d_win, e->h_wins, s)) ||
+        (rc = upload(e->slot_inst, e->h_slot_inst, s)) || (rc = upload(e->slot_win, e->h_slot_win, s)) ||
+        (rc = upload(e->slot_nb, e->h_slot_nb, s)) || (rc = upload(e->slot_tab, e->h_slot_tab, s)) ||
+        (rc = upload(e->cfg_off, e->h_cfg_off, s)) || (rc = upload(e->fields, e->h_fields, s)) ||
+        (rc = upload(e->mask, e->h_mask, s)) || (rc = upload(e->pairs[0], e->pairs_dir[0], s)) ||
+        (rc = upload(e->pairs[1], e->pairs_dir[1], s)))
+        return rc;
+    std::vector<int32_t> cfg(slot);
+    for (int i = 0; i < slot; ++i) cfg[i] = i;
+    if ((rc = upload(e->slot_cfg, cfg, s))) return rc;
+    if ((rc = e->slot_flavour.alloc(slot)) || (rc = e->slot_sweeps.alloc(slot)) || (rc = e->slot_draws.alloc(slot)) ||
+        (rc = e->slot_thr_off.alloc(slot)) || (rc = e->slot_thr_n.alloc(slot)) || (rc = e->cfg_E.alloc(slot)) ||
+        (rc = e->cfg_M.alloc(3 * (size_t)slot)) || (rc = e->spins.alloc(spin)) || (rc = e->g.alloc(tab)) ||
+        (rc = e->H.alloc(tab)) || (rc = e->visits.alloc(tab)) || (rc = e->win_lnf.alloc(win)) ||
+        (rc = e->win_done.alloc(win)) || (rc = e->win_oot.alloc(win)) || (rc = e->win_iter.alloc(win)) ||
+        (rc = e->win_sweepctr.alloc(win)) || (rc = e->counters.alloc(4)) || (rc = e->stats.alloc(2)))
+        return rc;
+    CUDA_TRY(cudaMemsetAsync(e->slot_sweeps.p, 0, slot * sizeof(uint64_t), s));
+    CUDA_TRY(cudaMemsetAsync(e->slot_draws.p, 0, slot * sizeof(int64_t), s));
+    CUDA_TRY(cudaMemsetAsync(e->slot_thr_off.p, 0, slot * sizeof(int64_t), s));
+    CUDA_TRY(cudaMemsetAsync(e->slot_thr_n.p, 0, slot * sizeof(int64_t), s));
+    if (tab) {
+        CUDA_TRY(cudaMemsetAsync(e->g.p, 0, tab * sizeof(int64_t), s));
+        CUDA_TRY(cudaMemsetAsync(e->H.p, 0, tab * sizeof(uint32_t), s));
+        CUDA_TRY(cudaMemsetAsync(e->visits.p, 0, tab * sizeof(uint64_t), s));
+    }
+    std::vector<int64_t> lnf(win, (int64_t)std::llround(D.lnf_initial * kLogdosScale));
+    CUDA_TRY(cudaMemcpyAsync(e->win_lnf.p, lnf.data(), win * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemsetAsync(e->win_done.p, 0, win * sizeof(int32_t), s));
+    CUDA_TRY(cudaMemsetAsync(e->win_oot.p, 0, win * sizeof(int32_t), s));
+    std::vector<uint64_t> ones(win, 1);
+    CUDA_TRY(cudaMemcpyAsync(e->win_iter.p, ones.data(), win * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemsetAsync(e->win_sweepctr.p, 0, win * sizeof(uint64_t), s));
+    CUDA_TRY(cudaMemsetAsync(e->counters.p, 0, 4 * sizeof(int32_t), s));
+    CUDA_TRY(cudaMemsetAsync(e->stats.p, 0, 2 * sizeof(unsigned long long), s));
+    return REWL_OK;
+}
+
+int plan_launches(rewl_engine* e)
+{
+    // one launch per model; shared memory sized for the largest walker of the launch
+    const int nsm_guess = 152;
+    for (int model = 0; model < 2; ++model) {
+        Launch l;
+        l.model = model;
+        int maxN = 0, maxnb = 0;
+        for (int s = 0; s < e->nslots; ++s) {
+            const HostInst& H = e->inst[e->h_slot_inst[s]];
+            if (H.d.model != model) continue;
+            l.slots.push_back(s);
+            maxN = std::max(maxN, H.dev.N);
+            maxnb = std::max(maxnb, e->h_slot_nb[s]);
+        }
+        if (l.slots.empty()) continue;
+        if (model == REWL_MODEL_ISING2D) {
+            l.nbcap = (maxnb + 1) & ~1;
+            l.smem_per_warp = (int)(l.nbcap * 12 + sizeof(Stage) + ((maxN + 15) & ~15));
+        } else {
+            l.nbcap = 0;
+            l.smem_per_warp = (int)(sizeof(StageAT) + ((2 * maxN + 15) & ~15));
+        }
+        l.smem_per_warp = (l.smem_per_warp + 15) & ~15;
+        int wpb = e->desc.walkers_per_block;
+        if (wpb == 0) {
+            // few walkers: one warp per block spreads them over the SMs;
+            // many walkers: pack warps to amortise the block's resources
+            const int n = (int)l.slots.size();
+            wpb = n <= nsm_guess * 2 ? 1 : n <= nsm_guess * 8 ? 2 : 4;
+        }
+        while (wpb > 1 && (size_t)wpb * l.smem_per_warp > 200 * 1024) wpb >>= 1;
+        if ((size_t)l.smem_per_warp > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory (limit 220 KiB)", l.smem_per_warp);
+        l.wpb = wpb;
+        int rc = upload(l.d_slots, l.slots, e->stream);
+        if (rc) return rc;
+        e->launches.push_back(std::move(l));
+    }
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_at<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_at<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    return REWL_OK;
+}
+
+int check_device_error(rewl_engine* e)
+{
+    int32_t h[4];
+    CUDA_TRY(cudaMemcpyAsync(h, e->counters.p, sizeof h, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    if (h[0] & ERR_BOUNDS) return fail(REWL_EBOUNDS, "a walker's energy left its window (device error word %d)", h[0]);
+    if (h[0] & ERR_ADJUST) return fail(REWL_EINVAL, "a walker could not reach its window");
+    if (h[0] & ERR_REPLAY_EXHAUSTED) return fail(REWL_EINVAL, "replay uniform stream exhausted");
+    return REWL_OK;
+}
+
+cudaEvent_t next_event(rewl_engine* e)
+{
+    if (e->ev_used == e->ev_pool.size()) {
+        cudaEvent_t ev;
+        cudaEventCreate(&ev);
+        e->ev_pool.push_back(ev);
+    }
+    return e->ev_pool[e->ev_used++];
+}
+
+int launch_sweeps(rewl_engine* e, int nsweeps)
+{
+    const DevPtrs P = e->ptrs();
+    const bool replay = e->desc.rng_mode == REWL_RNG_REPLAY;
+    cudaEventRecord(next_event(e), e->stream);
+    for (auto& l : e->launches) {
+        SweepParams sp;
+        sp.P = P; sp.slots = l.d_slots.p; sp.nslots = (int)l.slots.size(); sp.nsweeps = nsweeps;
+        sp.smem_per_warp = l.smem_per_warp; sp.nbcap = l.nbcap;
+        const int blocks = (sp.nslots + l.wpb - 1) / l.wpb;
+        const size_t smem = (size_t)l.wpb * l.smem_per_warp;
+        if (l.model == REWL_MODEL_ISING2D) {
+            if (replay) k_sweep_ising<true><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+            else k_sweep_ising<false><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+        } else {
+            if (replay) k_sweep_at<true><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+            else k_sweep_at<false><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+        }
+        CUDA_TRY(cudaGetLastError());
+        e->kernel_launches++;
+    }
+    cudaEventRecord(next_event(e), e->stream);
+    e->sweeps_total += nsweeps;
+    e->sweeps_since_check += nsweeps;
+    e->flips_total += (int64_t)nsweeps * e->flips_per_sweep;
+    return REWL_OK;
+}
+
+int launch_exchange(rewl_engine* e)
+{
+    const int dir = e->direction;
+    const int npairs = (int)e->pairs_dir[dir].size() / 2;
+    if (npairs > 0) {
+        k_exchange<<<(npairs + 127) / 128, 128, 0, e->stream>>>(e->ptrs(), e->pairs[dir].p, npairs, e->exch_round);
+        CUDA_TRY(cudaGetLastError());
+    }
+    e->direction ^= 1;
+    e->exch_round++;
+    return REWL_OK;
+}
+
+int launch_flat(rewl_engine* e)
+{
+    FlatParams fp;
+    fp.P = e->ptrs();
+    fp.nwin_total = e->nwin_total;
+    fp.flat_mode = e->desc.flatness_mode;
+    fp.mask_mode = e->desc.mask_mode;
+    fp.one_over_t = e->desc.one_over_t;
+    fp.reduce = e->desc.reduce_logdos;
+    fp.flat_den = 1000000;
+    fp.flat_num = (uint64_t)std::llround(e->desc.flatness_param * 1e6);
+    fp.flat_param_f = (float)e->desc.flatness_param;
+    fp.lnf_final = e->desc.lnf_final;
+    fp.sweeps_since_check = e->sweeps_since_check;
+    e->sweeps_since_check = 0;
+    k_flat<<<e->nwin_total, 256, 0, e->stream>>>(fp);
+    CUDA_TRY(cudaGetLastError());
+    return REWL_OK;
+}
+
+bool valid_walker(const rewl_engine* e, int w) { return e && w >= 0 && w < e->nslots; }
+
+int window_index(const rewl_engine* e, int ii, int w)
+{
+    if (!e || ii < 0 || ii >= (int)e->inst.size()) return -1;
+    if (w < 0 || w >= e->inst[ii].d.num_windows) return -1;
+    return e->inst[ii].dev.first_win + w;
+}
+
+// ------------------------------------------------------------------------
+// Host restatement of concatenate_tables (multiple overlap) for the logDoS
+// (src/util/concatenate_rewl_tables.hpp:167-305) with derivative_of_vector
+// (src/util/numerical_derivatives.hpp:47-70) and the concatenation-point
+// search (src/util/vector_matching.hpp:38-88).
+// ------------------------------------------------------------------------
+double derivative(size_t i, const std::vector<double>& f, const std::vector<double>& a)
+{
+    const size_t n = f.size();
+    if (i == 0) return (f[1] - f[0]) / (a[1] - a[0]);
+    if (i == n - 1) return (f[i] - f[i - 1]) / (a[i] - a[i - 1]);
+    if (i == 1 || i == n - 2) return (f[i + 1] - f[i - 1]) / (2. * (a[i] - a[i - 1]));
+    return (-f[i + 2] + 8. * f[i + 1] - 8. * f[i - 1] + f[i - 2]) / (12. * (a[i] - a[i - 1]));
+}
+
+int concatenate(const std::vector<std::vector<double>>& E, const std::vector<std::vector<double>>& G,
+                std::vector<double>& fe, std::vector<double>& fg)
+{
+    fe = E[0]; fg = G[0];
+    for (size_t w = 1; w < E.size(); ++w) {
+        const auto& er = E[w]; const auto& gr = G[w];
+        if (er.size() < 2 || fe.size() < 2) return fail(REWL_EINVAL, "window %zu has fewer than 2 valid bins", w);
+        long left_start = -1;
+        for (long k = (long)fe.size() - 1; k >= 0; --k) if (fe[k] == er[0]) { left_start = k; break; }
+        if (left_start < 0) return fail(REWL_EINVAL, "windows %zu and %zu do not overlap", w - 1, w);
+        const size_t nleft = fe.size();
+        if (nleft - (size_t)left_start > er.size()) return fail(REWL_EINVAL, "window %zu lies inside window %zu", w, w - 1);
+        double beta_diff = std::fabs(derivative((size_t)left_start, fg, fe) - derivative(0, gr, er));
+        size_t cl = (size_t)left_start;
+        for (size_t idx = 1; idx != nleft - (size_t)left_start; ++idx) {
+            const double lb = derivative((size_t)left_start + idx, fg, fe), rb = derivative(idx, gr, er);
+            if ((std::fabs(lb - rb) + 0.5) < (beta_diff + 0.5)) { beta_diff = std::fabs(lb - rb); cl = (size_t)left_start + idx; }
+        }
+        double shifter = 0;
+        size_t right_idx = 0;
+        for (size_t idx = (size_t)left_start; idx != fe.size(); ++idx) {
+            right_idx = idx - (size_t)left_start;
+            if (idx == cl) shifter = fg[idx] - gr[right_idx];
+            else if (idx > cl) fg[idx] = gr[right_idx] + shifter;
+        }
+        for (size_t idx = right_idx + 1; idx < er.size(); ++idx) { fe.push_back(er[idx]); fg.push_back(gr[idx] + shifter); }
+    }
+    return REWL_OK;
+}
+
+} // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char* rewl_last_error_string(void) { return g_last_error.c_str(); }
+
+int rewl_create(const rewl_batch_desc* desc, rewl_engine** out)
+{
+    if (!desc || !out) return fail(REWL_EINVAL, "null argument");
+    *out = nullptr;
+    rewl_engine* e = new rewl_engine();
+    e->desc = *desc;
+    int rc = build_host(e);               // descriptor validation and layout: host only
+    if (rc) { delete e; return rc; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { delete e; return fail(REWL_EDEVICE, "no CUDA device"); }
+    if (desc->device < 0 || desc->device >= ndev) { delete e; return fail(REWL_EINVAL, "device %d out of range", desc->device); }
+    if (cudaSetDevice(desc->device) != cudaSuccess || cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete e; return fail(REWL_EDEVICE, "cannot open device %d", desc->device);
+    }
+    rc = upload_all(e);
+    if (!rc) rc = plan_launches(e);
+    if (!rc) {
+        k_init<<<(e->nslots + 63) / 64, 64, 0, e->stream>>>(e->ptrs(), e->nslots, 0);
+        cudaError_t ce = cudaGetLastError();
+        if (ce != cudaSuccess) rc = fail(REWL_EDEVICE, "k_init launch: %s", cudaGetErrorString(ce));
+    }
+    if (!rc) rc = check_device_error(e);
+    if (rc) { e->release(); delete e; return rc; }
+    *out = e;
+    return REWL_OK;
+}
+
+int rewl_destroy(rewl_engine* e)
+{
+    if (!e) return REWL_OK;
+    cudaSetDevice(e->desc.device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    e->release();
+    delete e;
+    return REWL_OK;
+}
+
+int rewl_num_walkers(const rewl_engine* e, int32_t* n)
+{
+    if (!e || !n) return fail(REWL_EINVAL, "null argument");
+    *n = e->nslots;
+    return REWL_OK;
+}
+
+int rewl_walker_info(const rewl_engine* e, int32_t w, int32_t* inst, int32_t* win, int32_t* rep)
+{
+    if (!valid_walker(e, w)) return fail(REWL_EINVAL, "walker %d out of range", w);
+    const int ii = e->h_slot_inst[w];
+    const WinDev& W = e->h_wins[e->h_slot_win[w]];
+    if (inst) *inst = ii;
+    if (win) *win = W.local;
+    if (rep) *rep = (w - e->inst[ii].dev.first_slot) % e->inst[ii].dev.R;
+    return REWL_OK;
+}
+
+int rewl_window_info(const rewl_engine* e, int32_t ii, int32_t w, double* emin, double* emax, int32_t* nb)
+{
+    const int wi = window_index(e, ii, w);
+    if (wi < 0) return fail(REWL_EINVAL, "window (%d, %d) out of range", ii, w);
+    if (emin) *emin = e->inst[ii].wmin[w];
+    if (emax) *emax = e->inst[ii].wmax[w];
+    if (nb) *nb = e->h_wins[wi].nb;
+    return REWL_OK;
+}
+
+int rewl_import_dofs(rewl_engine* e, int32_t w, const int8_t* dofs, int32_t flavour)
+{
+    if (!valid_walker(e, w) || !dofs) return fail(REWL_EINVAL, "bad walker or null dofs");
+    if (flavour != 0 && flavour != 1) return fail(REWL_EINVAL, "flavour must be 0 or 1");
+    const int ii = e->h_slot_inst[w];
+    const InstDev& I = e->inst[ii].dev;
+    for (int i = 0; i < I.ndof; ++i)
+        if (dofs[i] != 1 && dofs[i] != -1) return fail(REWL_EINVAL, "spins must be +1 or -1");
+    cudaSetDevice(e->desc.device);
+    int32_t cfg;
+    CUDA_TRY(cudaMemcpyAsync(&cfg, e->slot_cfg.p + w, sizeof cfg, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    CUDA_TRY(cudaMemcpyAsync(e->spins.p + e->h_cfg_off[cfg], dofs, I.ndof, cudaMemcpyHostToDevice, e->stream));
+    CUDA_TRY(cudaMemcpyAsync(e->slot_flavour.p + w, &flavour, sizeof flavour, cudaMemcpyHostToDevice, e->stream));
+    int32_t* tmp = nullptr;
+    CUDA_TRY(cudaMalloc(&tmp, 2 * sizeof(int32_t)));
+    int32_t hv[2] = {cfg, ii};
+    CUDA_TRY(cudaMemcpyAsync(tmp, hv, sizeof hv, cudaMemcpyHostToDevice, e->stream));
+    k_recalc<<<1, 32, 0, e->stream>>>(e->ptrs(), tmp, tmp + 1, 1);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    cudaFree(tmp);
+    // the energy must be inside the walker's window
+    int64_t E;
+    CUDA_TRY(cudaMemcpy(&E, e->cfg_E.p + cfg, sizeof E, cudaMemcpyDeviceToHost));
+    const WinDev& W = e->h_wins[e->h_slot_win[w]];
+    const int64_t gb = (((E - I.eglo_u) * I.bin_mul) >> I.bin_shift) - W.gblo;
+    if (gb < 0 || gb >= W.nb) return fail(REWL_EINVAL, "imported configuration has energy outside the walker's window");
+    return REWL_OK;
+}
+
+int rewl_import_disorder(rewl_engine* e, int32_t ii, const double* fields)
+{
+    if (!e || ii < 0 || ii >= (int)e->inst.size() || !fields) return fail(REWL_EINVAL, "bad instance or null fields");
+    HostInst& H = e->inst[ii];
+    if (H.dev.model != REWL_MODEL_ASHKIN_TELLER2D || H.dev.field_off < 0)
+        return fail(REWL_EINVAL, "instance %d was created without fields", ii);
+    std::vector<int64_t> q(H.dev.N);
+    for (int i = 0; i < H.dev.N; ++i) {
+        const double v = std::nearbyint(std::ldexp(fields[i], 20));
+        if (!std::isfinite(v)) return fail(REWL_EINVAL, "bad field value");
+        q[i] = (int64_t)v; H.fields[i] = std::ldexp(v, -20);
+    }
+    cudaSetDevice(e->desc.device);
+    CUDA_TRY(cudaMemcpyAsync(e->fields.p + H.dev.field_off, q.data(), q.size() * 8, cudaMemcpyHostToDevice, e->stream));
+    const int n = H.dev.nwin * H.dev.R;
+    std::vector<int32_t> cfgs(n), insts(n, ii);
+    CUDA_TRY(cudaMemcpyAsync(cfgs.data(), e->slot_cfg.p + H.dev.first_slot, n * 4, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    int32_t* tmp = nullptr;
+    CUDA_TRY(cudaMalloc(&tmp, 2 * n * sizeof(int32_t)));
+    CUDA_TRY(cudaMemcpyAsync(tmp, cfgs.data(), n * 4, cudaMemcpyHostToDevice, e->stream));
+    CUDA_TRY(cudaMemcpyAsync(tmp + n, insts.data(), n * 4, cudaMemcpyHostToDevice, e->stream));
+    k_recalc<<<(n + 63) / 64, 64, 0, e->stream>>>(e->ptrs(), tmp, tmp + n, n);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    cudaFree(tmp);
+    return REWL_OK;
+}
+
+int rewl_set_logdos(rewl_engine* e, int32_t ii, int32_t w, const double* logdos)
+{
+    const int wi = window_index(e, ii, w);
+    if (wi < 0 || !logdos) return fail(REWL_EINVAL, "bad window or null logdos");
+    const int nb = e->h_wins[wi].nb;
+    std::vector<int64_t> q(nb);
+    for (int b = 0; b < nb; ++b) {
+        if (!std::isfinite(logdos[b]) || std::fabs(logdos[b]) > 1e6) return fail(REWL_EINVAL, "logdos values must be finite and |g| <= 1e6");
+        q[b] = (int64_t)std::nearbyint(logdos[b] * kLogdosScale);
+    }
+    cudaSetDevice(e->desc.device);
+    const InstDev& I = e->inst[ii].dev;
+    for (int r = 0; r < I.R; ++r) {
+        const int s = I.first_slot + w * I.R + r;
+        CUDA_TRY(cudaMemcpyAsync(e->g.p + e->h_slot_tab[s], q.data(), nb * 8, cudaMemcpyHostToDevice, e->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return REWL_OK;
+}
+
+int rewl_set_lnf(rewl_engine* e, int32_t ii, int32_t w, double lnf)
+{
+    const int wi = window_index(e, ii, w);
+    if (wi < 0 || !(lnf > 0) || lnf > 64) return fail(REWL_EINVAL, "bad window or ln f");
+    const int64_t q = (int64_t)std::llround(lnf * kLogdosScale);
+    cudaSetDevice(e->desc.device);
+    CUDA_TRY(cudaMemcpyAsync(e->win_lnf.p + wi, &q, 8, cudaMemcpyHostToDevice, e->stream));
+    const int32_t done = (lnf < e->desc.lnf_final) ? 1 : 0;
+    CUDA_TRY(cudaMemcpyAsync(e->win_done.p + wi, &done, 4, cudaMemcpyHostToDevice, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return REWL_OK;
+}
+
+int rewl_set_uniform_stream(rewl_engine* e, int32_t w, const double* u, size_t n)
+{
+    if (!valid_walker(e, w) || (!u && n)) return fail(REWL_EINVAL, "bad walker or null stream");
+    if (e->desc.rng_mode != REWL_RNG_REPLAY) return fail(REWL_ESTATE, "engine was not created in replay mode");
+    // accept <=> u < exp(-dg) for the float dg; since exp(-f) falls with f, the
+    // accepted floats are those below tau = the smallest float with exp(-tau) <= u
+    std::vector<int64_t> T(n);
+    for (size_t k = 0; k < n; ++k) {
+        const double x = u[k];
+        if (!(x >= 0.0 && x < 1.0)) return fail(REWL_EINVAL, "uniform %zu not in [0,1)", k);
+        if (x == 0.0) { T[k] = INT64_MAX; continue; }
+        float f = (float)(-std::log(x));
+        if (!(f > 0)) f = 1e-30f;
+        while (f > 0 && !(std::exp(-(double)f) > x)) f = std::nextafter(f, 0.0f);
+        while (std::exp(-(double)std::nextafter(f, INFINITY)) > x) f = std::nextafter(f, INFINITY);
+        const float tau = std::nextafter(f, INFINITY);
+        T[k] = (tau < 1e-30f) ? 1 : accept_threshold(tau);
+    }
+    cudaSetDevice(e->desc.device);
+    // append to the walker-private table (reallocate the pool)
+    const size_t old = e->thr.n;
+    std::vector<int64_t> all(old + n);
+    if (old) CUDA_TRY(cudaMemcpy(all.data(), e->thr.p, old * 8, cudaMemcpyDeviceToHost));
+    std::copy(T.begin(), T.end(), all.begin() + old);
+    e->thr.free_();
+    int rc = e->thr.alloc(all.size());
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpy(e->thr.p, all.data(), all.size() * 8, cudaMemcpyHostToDevice));
+    const int64_t off = (int64_t)old, cnt = (int64_t)n, zero = 0;
+    CUDA_TRY(cudaMemcpy(e->slot_thr_off.p + w, &off, 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(e->slot_thr_n.p + w, &cnt, 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(e->slot_draws.p + w, &zero, 8, cudaMemcpyHostToDevice));
+    return REWL_OK;
+}
+
+int rewl_run_sweeps(rewl_engine* e, int64_t n)
+{
+    if (!e || n < 0) return fail(REWL_EINVAL, "bad arguments");
+    cudaSetDevice(e->desc.device);
+    while (n > 0) {
+        const int chunk = (int)std::min<int64_t>(n, 1 << 20);
+        int rc = launch_sweeps(e, chunk);
+        if (rc) return rc;
+        n -= chunk;
+    }
+    return check_device_error(e);
+}
+
+int rewl_exchange(rewl_engine* e)
+{
+    if (!e) return fail(REWL_EINVAL, "null engine");
+    cudaSetDevice(e->desc.device);
+    int rc = launch_exchange(e);
+    if (rc) return rc;
+    return check_device_error(e);
+}
+
+int rewl_check_flat(rewl_engine* e, int32_t* num_flat)
+{
+    if (!e) return fail(REWL_EINVAL, "null engine");
+    cudaSetDevice(e->desc.device);
+    CUDA_TRY(cudaMemsetAsync(e->counters.p + 1, 0, 4, e->stream));
+    int rc = launch_flat(e);
+    if (rc) return rc;
+    int32_t h[2];
+    CUDA_TRY(cudaMemcpyAsync(h, e->counters.p, sizeof h, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->flat_events += h[1];
+    e->cycles++;
+    if (num_flat) *num_flat = h[1];
+    return check_device_error(e);
+}
+
+int rewl_reset_histograms(rewl_engine* e, int32_t ii, int32_t w, int32_t reduce)
+{
+    const int wi = window_index(e, ii, w);
+    if (wi < 0) return fail(REWL_EINVAL, "bad window");
+    cudaSetDevice(e->desc.device);
+    k_reset_window<<<1, 256, 0, e->stream>>>(e->ptrs(), wi, reduce);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return REWL_OK;
+}
+
+int rewl_get_status(rewl_engine* e, rewl_status* st)
+{
+    if (!e || !st) return fail(REWL_EINVAL, "null argument");
+    cudaSetDevice(e->desc.device);
+    std::vector<int32_t> done(e->nwin_total);
+    unsigned long long stats[2];
+    int32_t counters[4];
+    CUDA_TRY(cudaMemcpyAsync(done.data(), e->win_done.p, done.size() * 4, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaMemcpyAsync(stats, e->stats.p, sizeof stats, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaMemcpyAsync(counters, e->counters.p, sizeof counters, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    std::memset(st, 0, sizeof *st);
+    st->sweeps = e->sweeps_total;
+    st->cycles = e->cycles;
+    st->flat_events = e->flat_events;
+    st->windows_total = e->nwin_total;
+    for (int d : done) st->windows_done += d;
+    st->all_done = st->windows_done == st->windows_total;
+    st->exchanges_attempted = (int64_t)stats[0];
+    st->exchanges_accepted = (int64_t)stats[1];
+    st->attempted_flips = e->flips_total;
+    st->device_error = counters[0];
+    return REWL_OK;
+}
+
+int rewl_run_cycles(rewl_engine* e, int64_t ncycles, int64_t timeout_ms, rewl_status* st)
+{
+    if (!e || ncycles < 0) return fail(REWL_EINVAL, "bad arguments");
+    cudaSetDevice(e->desc.device);
+    const auto t0 = std::chrono::steady_clock::now();
+    const int se = e->desc.sweeps_per_exchange, rounds = e->desc.sweeps_per_check / se;
+    int rc = REWL_OK;
+    for (int64_t c = 0; c < ncycles; ++c) {
+        for (int r = 0; r < rounds; ++r) {
+            if ((rc = launch_sweeps(e, se))) return rc;
+            if ((rc = launch_exchange(e))) return rc;
+        }
+        int32_t nflat = 0;
+        if ((rc = rewl_check_flat(e, &nflat))) return rc;
+        rewl_status s;
+        if ((rc = rewl_get_status(e, &s))) return rc;
+        if (st) *st = s;
+        if (s.all_done) break;
+        if (timeout_ms > 0) {
+            const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+            if (ms > timeout_ms) return fail(REWL_ETIMEDOUT, "run_cycles deadline of %lld ms passed", (long long)timeout_ms);
+        }
+    }
+    if (st) return rewl_get_status(e, st);
+    return REWL_OK;
+}
+
+int rewl_export_walker(rewl_engine* e, int32_t w, int8_t* dofs, double* state, uint64_t* counts, double* logdos, uint64_t* visits)
+{
+    if (!valid_walker(e, w)) return fail(REWL_EINVAL, "walker %d out of range", w);
+    cudaSetDevice(e->desc.device);
+    const int ii = e->h_slot_inst[w];
+    const InstDev& I = e->inst[ii].dev;
+    int32_t cfg, flav;
+    CUDA_TRY(cudaMemcpyAsync(&cfg, e->slot_cfg.p + w, 4, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaMemcpyAsync(&flav, e->slot_flavour.p + w, 4, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    if (dofs) CUDA_TRY(cudaMemcpyAsync(dofs, e->spins.p + e->h_cfg_off[cfg], I.ndof, cudaMemcpyDeviceToHost, e->stream));
+    int64_t E; int32_t M[3];
+    CUDA_TRY(cudaMemcpyAsync(&E, e->cfg_E.p + cfg, 8, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaMemcpyAsync(M, e->cfg_M.p + 3 * cfg, 12, cudaMemcpyDeviceToHost, e->stream));
+    const int nb = e->h_slot_nb[w];
+    const int64_t off = e->h_slot_tab[w];
+    std::vector<int64_t> g(nb); std::vector<uint32_t> h(nb);
+    CUDA_TRY(cudaMemcpyAsync(g.data(), e->g.p + off, nb * 8, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaMemcpyAsync(h.data(), e->H.p + off, nb * 4, cudaMemcpyDeviceToHost, e->stream));
+    if (visits) CUDA_TRY(cudaMemcpyAsync(visits, e->visits.p + off, nb * 8, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    if (state) {
+        const double Ed = std::ldexp((double)E, -I.escale);
+        if (I.model == REWL_MODEL_ISING2D) { state[0] = Ed; state[1] = M[0]; }
+        else { state[0] = Ed; state[1] = M[0]; state[2] = M[1]; state[3] = M[2]; state[4] = flav; }
+    }
+    if (counts) for (int b = 0; b < nb; ++b) counts[b] = h[b];
+    if (logdos) for (int b = 0; b < nb; ++b) logdos[b] = (double)g[b] / kLogdosScale;
+    return REWL_OK;
+}
+
+int rewl_export_window_logdos(rewl_engine* e, int32_t ii, int32_t w, double* out)
+{
+    const int wi = window_index(e, ii, w);
+    if (wi < 0 || !out) return fail(REWL_EINVAL, "bad window or null output");
+    cudaSetDevice(e->desc.device);
+    const InstDev& I = e->inst[ii].dev;
+    const int nb = e->h_wins[wi].nb, R = I.R;
+    std::vector<int64_t> g((size_t)R * nb);
+    std::vector<uint64_t> v((size_t)R * nb);
+    for (int r = 0; r < R; ++r) {
+        const int s = I.first_slot + w * R + r;
+        CUDA_TRY(cudaMemcpyAsync(g.data() + (size_t)r * nb, e->g.p + e->h_slot_tab[s], nb * 8, cudaMemcpyDeviceToHost, e->stream));
+        CUDA_TRY(cudaMemcpyAsync(v.data() + (size_t)r * nb, e->visits.p + e->h_slot_tab[s], nb * 8, cudaMemcpyDeviceToHost, e->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    for (int b = 0; b < nb; ++b) {
+        double tot = 0;
+        for (int r = 0; r < R; ++r) tot += (double)v[(size_t)r * nb + b];
+        double acc = 0;
+        if (tot == 0 || R == 1) acc = (double)g[b] / kLogdosScale;
+        else for (int r = 0; r < R; ++r) acc = acc + ((double)v[(size_t)r * nb + b] / tot) * ((double)g[(size_t)r * nb + b] / kLogdosScale);
+        out[b] = acc;
+    }
+    return REWL_OK;
+}
+
+int rewl_export_window_mask(rewl_engine* e, int32_t ii, int32_t w, uint8_t* out)
+{
+    const int wi = window_index(e, ii, w);
+    if (wi < 0 || !out) return fail(REWL_EINVAL, "bad window or null output");
+    cudaSetDevice(e->desc.device);
+    const WinDev& W = e->h_wins[wi];
+    const InstDev& I = e->inst[ii].dev;
+    CUDA_TRY(cudaMemcpyAsync(out, e->mask.p + W.mask_off, W.nb, cudaMemcpyDeviceToHost, e->stream));
+    std::vector<uint64_t> v((size_t)I.R * W.nb);
+    for (int r = 0; r < I.R; ++r)
+        CUDA_TRY(cudaMemcpyAsync(v.data() + (size_t)r * W.nb, e->visits.p + e->h_slot_tab[I.first_slot + w * I.R + r], W.nb * 8, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    if (e->desc.mask_mode == REWL_MASK_VISITED)
+        for (int b = 0; b < W.nb; ++b) {
+            bool any = false;
+            for (int r = 0; r < I.R; ++r) any |= v[(size_t)r * W.nb + b] != 0;
+            if (!any) out[b] = 0;
+        }
+    return REWL_OK;
+}
+
+int rewl_window_state(rewl_engine* e, int32_t ii, int32_t w, double* lnf, int32_t* done)
+{
+    const int wi = window_index(e, ii, w);
+    if (wi < 0) return fail(REWL_EINVAL, "bad window");
+    cudaSetDevice(e->desc.device);
+    int64_t q; int32_t d;
+    CUDA_TRY(cudaMemcpyAsync(&q, e->win_lnf.p + wi, 8, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaMemcpyAsync(&d, e->win_done.p + wi, 4, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    if (lnf) *lnf = (double)q / kLogdosScale;
+    if (done) *done = d;
+    return REWL_OK;
+}
+
+int rewl_global_logdos(rewl_engine* e, int32_t ii, int32_t half_spectrum, double* energies, double* logdos, int32_t* count)
+{
+    if (!e || ii < 0 || ii >= (int)e->inst.size() || !count) return fail(REWL_EINVAL, "bad arguments");
+    const HostInst& H = e->inst[ii];
+    std::vector<std::vector<double>> Es, Gs;
+    for (int w = 0; w < H.d.num_windows; ++w) {
+        const int nb = H.wins[w].nb;
+        std::vector<double> g(nb); std::vector<uint8_t> m(nb);
+        int rc = rewl_export_window_logdos(e, ii, w, g.data());
+        if (!rc) rc = rewl_export_window_mask(e, ii, w, m.data());
+        if (rc) return rc;
+        std::vector<double> ee, gg;
+        for (int b = 0; b < nb; ++b)
+            if (m[b]) { ee.push_back(H.wmin[w] + H.bw * b); gg.push_back(g[b]); }
+        Es.push_back(ee); Gs.push_back(gg);
+    }
+    std::vector<double> fe, fg;
+    int rc = concatenate(Es, Gs, fe, fg);
+    if (rc) return rc;
+    // normalize_logDoS: sum_E g(E) = states_per_site^N (halved for a half spectrum)
+    double mx = fg.empty() ? 0 : fg[0];
+    for (double v : fg) mx = std::max(mx, v);
+    double sum = 0;
+    for (double v : fg) sum += std::exp(-(mx - v));
+    const double lse = std::log(sum) + mx;
+    const double states = H.dev.model == REWL_MODEL_ISING2D ? 2.0 : 4.0;
+    const double shift = (double)H.dev.N * std::log(states) - lse - (half_spectrum ? std::log(2.0) : 0.0);
+    if ((int)fe.size() > *count) { *count = (int)fe.size(); return fail(REWL_EINVAL, "output capacity too small (%zu needed)", fe.size()); }
+    for (size_t k = 0; k < fe.size(); ++k) { if (energies) energies[k] = fe[k]; if (logdos) logdos[k] = fg[k] + shift; }
+    *count = (int)fe.size();
+    return REWL_OK;
+}
+
+int rewl_sweep_kernel_time(rewl_engine* e, double* ms, int64_t* launches)
+{
+    if (!e) return fail(REWL_EINVAL, "null engine");
+    cudaSetDevice(e->desc.device);
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    double total = 0;
+    for (size_t k = 0; k + 1 < e->ev_used; k += 2) {
+        float t = 0;
+        CUDA_TRY(cudaEventElapsedTime(&t, e->ev_pool[k], e->ev_pool[k + 1]));
+        total += t;
+    }
+    if (ms) *ms = total;
+    if (launches) *launches = e->kernel_launches;
+    e->ev_used = 0;
+    e->kernel_launches = 0;
+    return REWL_OK;
+}
+
+int rewl_get_stream(rewl_engine* e, void** stream)
+{
+    if (!e || !stream) return fail(REWL_EINVAL, "null argument");
+    *stream = (void*)e->stream;
+    return REWL_OK;
+}
+
+} // extern "C"

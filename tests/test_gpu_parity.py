@@ -1,0 +1,161 @@
+"""GPU engine (through the C ABI) against the reference and the CPU oracle.
+
+* Replay parity: fed the reference walker's own uniform stream, the CUDA sweep
+  kernels must reproduce the reference's lattices, energies, magnetisations,
+  histograms and logDoS bit for bit (golden fixtures from the reference's
+  REWL_Walker, tests/golden/make_golden.py).
+* Engine-semantics parity: with Philox streams, a multi-window, multi-replica
+  REWL run on the GPU (sweeps, replica exchange, flatness, averaging, ln f) must
+  match the CPU oracle bit for bit after every check interval.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+REPLAY = sorted(p.name for p in GOLDEN.glob("replay_*.npz"))
+
+
+def _engine_layout(dofs_ref: np.ndarray, model: int) -> np.ndarray:
+    if model == 0:
+        return dofs_ref.astype(np.int8)
+    return np.concatenate([dofs_ref[0::2], dofs_ref[1::2]]).astype(np.int8)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", REPLAY)
+def test_replay_matches_reference(engine_lib, oracle_lib, name):
+    rg, po = engine_lib, oracle_lib
+    z = np.load(GOLDEN / name)
+    model = int(z["model"])
+    fields = z["fields"] if z["fields"].size else None
+    ins = rg.Instance(model=model, L=int(z["L"]), J=1.0, K=float(z["K"]) if model else 0.0, fields=fields,
+                      energy_min=float(z["wmin"]), energy_max=float(z["wmax"]), bin_width=float(z["bw"]),
+                      num_windows=1, replicas_per_window=1, init_mode=1, seed=1)
+    b = rg.Batch(instances=[ins], rng_mode=rg.RNG_REPLAY, lnf_initial=float(z["lnf1"]), lnf_final=1e-9)
+    with rg.Engine(b) as eng:
+        which = int(z["state0"][4]) if model else 0
+        eng.import_dofs(0, _engine_layout(z["dofs0"], model), which)
+        skip = int(z["adjust_draws"])
+        need = int(z["draws2"]) + 64
+        u = po.mt64_uniforms(int(z["seed"]), need)[skip:]
+        eng.set_uniform_stream(0, u)
+        st0 = eng.export_walker(0)
+        np.testing.assert_array_equal(st0["state"], z["state0"])
+        for stage in (1, 2):
+            if stage == 2:
+                eng.reset_histograms(0, 0, True)
+                eng.set_lnf(0, 0, float(z["lnf2"]))
+            eng.run_sweeps(int(z[f"sweeps{stage}"]))
+            out = eng.export_walker(0)
+            np.testing.assert_array_equal(out["counts"], z[f"counts{stage}"])
+            np.testing.assert_array_equal(out["logdos"], z[f"logdos{stage}"])
+            np.testing.assert_array_equal(out["state"], z[f"state{stage}"])
+            np.testing.assert_array_equal(out["dofs"], _engine_layout(z[f"dofs{stage}"], model))
+
+
+def _pair(rg, po, model, L, emin, emax, bw, nwin, R, se, sc, seed, K=0.5, fields=None, flat=0.8,
+          mask=0, lnf0=1.0, overlap=0.75, flat_mode=0):
+    ins = rg.Instance(model=model, L=L, J=1.0, K=K if model else 0.0, fields=fields, energy_min=emin,
+                      energy_max=emax, bin_width=bw, num_windows=nwin, replicas_per_window=R,
+                      window_overlap=overlap, init_mode=0, seed=seed)
+    b = rg.Batch(instances=[ins], sweeps_per_exchange=se, sweeps_per_check=sc, flatness_mode=flat_mode,
+                 flatness_param=flat, lnf_initial=lnf0, lnf_final=1e-7, mask_mode=mask)
+    eng = rg.Engine(b)
+    cfg = po.Config(model=model, L=L, K=K, escale_bits=0 if model == 0 else 20, nwin=nwin, R=R,
+                    sweeps_per_exchange=se, sweeps_per_check=sc, emin=emin, emax=emax, bw=bw, overlap=overlap,
+                    lnf0=lnf0, lnf_final=1e-7, flat_param=flat, flat_mode=flat_mode, mask_mode=mask,
+                    semantics=po.SEM_ENGINE, seed=seed)
+    orc = po.Oracle(cfg, fields=fields)
+    return eng, orc
+
+
+def _compare(eng, orc, tag):
+    for s in range(orc.num_walkers):
+        out = eng.export_walker(s)
+        c, g, v = orc.tables(s)
+        np.testing.assert_array_equal(out["dofs"], orc.dofs(s), err_msg=f"{tag} walker {s} dofs")
+        np.testing.assert_array_equal(out["state"], orc.state(s), err_msg=f"{tag} walker {s} state")
+        np.testing.assert_array_equal(out["counts"], c, err_msg=f"{tag} walker {s} counts")
+        np.testing.assert_array_equal(out["visits"], v, err_msg=f"{tag} walker {s} visits")
+        np.testing.assert_array_equal(out["logdos"], g, err_msg=f"{tag} walker {s} logdos")
+    for w in range(orc.cfg.nwin):
+        lnf, done = eng.window_state(0, w)
+        assert lnf == orc.lnf(w * orc.cfg.R), f"{tag} window {w} lnf"
+        assert done == bool(orc.done_flags()[w]), f"{tag} window {w} done"
+
+
+CASES = [
+    # model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles
+    ("ising_L8_3x2", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 6),
+    ("ising_L6_2x3", 0, 6, -72.0, 76.0, 4.0, 2, 3, 20, 40, 5, 8),
+    ("ising_L12_4x2_bw8", 0, 12, -288.0, 296.0, 8.0, 4, 2, 10, 20, 3, 5),
+    ("ising_L40_3x2", 0, 40, -3200.0, -2000.0, 4.0, 3, 2, 4, 8, 9, 3),
+    ("ising_L64_2x2", 0, 64, -8192.0, -7000.0, 4.0, 2, 2, 2, 4, 2, 2),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_engine_matches_oracle_ising(engine_lib, oracle_lib, case):
+    _, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles = case
+    eng, orc = _pair(engine_lib, oracle_lib, model, L, emin, emax, bw, nwin, R, se, sc, seed)
+    try:
+        _compare(eng, orc, "init")
+        for k in range(cycles):
+            eng.run_cycles(1)
+            orc.cycle()
+            _compare(eng, orc, f"cycle {k}")
+        st = eng.status()
+        att, acc = orc.exchange_stats()
+        assert (st.exchanges_attempted, st.exchanges_accepted) == (att, acc)
+        if L <= 12:
+            assert st.exchanges_accepted > 0
+    finally:
+        eng.close()
+        orc.close()
+
+
+AT_CASES = [
+    # name, L, K, sigma_h, bw, nwin, R, se, sc, seed, cycles, mask
+    ("at_L4_rf", 4, 0.5, 0.5, 0.05, 2, 2, 20, 40, 7, 4, 1),
+    ("at_L6_clean_bw025", 6, 0.25, 0.0, 0.25, 3, 2, 10, 20, 3, 4, 1),
+    ("at_L8_rf_bw05", 8, 0.5, 0.3, 0.5, 2, 2, 5, 10, 13, 3, 1),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", AT_CASES, ids=[c[0] for c in AT_CASES])
+def test_engine_matches_oracle_at(engine_lib, oracle_lib, case):
+    _, L, K, sig, bw, nwin, R, se, sc, seed, cycles, mask = case
+    N = L * L
+    emin = -(2.0 + K) * 2 * N
+    rng = np.random.default_rng(seed)
+    fields = np.round(rng.normal(0, sig, N) * 2**20) / 2**20 if sig > 0 else None
+    eng, orc = _pair(engine_lib, oracle_lib, 1, L, emin, 0.0, bw, nwin, R, se, sc, seed, K=K, fields=fields,
+                     mask=mask)
+    try:
+        _compare(eng, orc, "init")
+        for k in range(cycles):
+            eng.run_cycles(1)
+            orc.cycle()
+            _compare(eng, orc, f"cycle {k}")
+    finally:
+        eng.close()
+        orc.close()
+
+
+@pytest.mark.gpu
+def test_ising_L8_converges_to_exact(engine_lib):
+    rg = engine_lib
+    z = np.load(GOLDEN / "exact_ising_L8.npz")
+    ins = rg.Instance(model=0, L=8, energy_min=-128.0, energy_max=132.0, bin_width=4.0, num_windows=2,
+                      replicas_per_window=4, seed=21)
+    b = rg.Batch(instances=[ins], sweeps_per_exchange=100, sweeps_per_check=200, lnf_final=1e-5)
+    with rg.Engine(b) as eng:
+        st = eng.simulate(max_cycles=200000, timeout_ms=300000)
+        assert st.all_done
+        E, g = eng.global_logdos(0)
+        np.testing.assert_array_equal(E, z["E"])
+        err = np.abs(g - z["lng"]).max()
+        assert err < 0.05, err
