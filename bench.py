@@ -1,0 +1,346 @@
+#!/usr/bin/env python3
+"""Benchmark of the REWL hot path on GB300.
+
+Workload (the batched configuration the headline metric is quoted on): 2D Ising,
+L = 32 periodic, J = 1, energy levels -2048..2048 step 4 (bins of width 4 over
+[-2048, 2052)), 16 equal windows at 75 % overlap x 8 walkers = 128 walkers in one
+launch, int8 spins, replica exchange every 500 sweeps, flatness (min >= 0.8 mean)
+checked every 1000 sweeps, ln f halved from 1 towards 1e-8, int64 logDoS in 2^-40
+units.  Inputs are synthetic (spins drawn from the seed).
+
+A step is one check interval: 2 x (500 sweeps of all 128 walkers + one replica
+exchange round) + the flatness / averaging / ln f kernel, i.e. 131,072,000
+attempted single-spin flips.  `value` is attempted flips per second over the
+whole job (device time, CUDA events on the engine's stream, L2 flushed between
+steps by a 256 MiB write).  `e2e` runs the same steps through the public API with
+the walker state host-resident in pinned memory: restore (H2D) + step +
+snapshot (D2H) per step, wall clock.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}] [--tta]
+
+--impl reference times the CPU restatement of the reference's hot path (the
+oracle port, reference semantics: mt19937_64 streams, draw-on-demand, FP64
+logDoS) on all host cores for the same workload; under torchrun only rank 0 runs.
+--tta additionally measures the GPU wall time until the concatenated, normalised
+ln g is within 1e-2 of the exact density of states.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "time to ln g within 1e-2 of exact, MLP warm-start vs plain WL, 1 GB300; flips/s"
+WORKLOAD = dict(name="ising2d_L32_16win_x8walkers_rewl", model="ising2d", L=32, energy_min=-2048.0,
+                energy_max=2052.0, bin_width=4.0, num_windows=16, replicas_per_window=8, window_overlap=0.75,
+                sweeps_per_exchange=500, sweeps_per_check=1000, lnf_initial=1.0, lnf_final=1e-8,
+                flatness="min >= 0.8 mean over valid bins")
+BYTES_PER_FLIP = 46        # algorithmic bytes per attempted Ising flip (5+1 B spins, 24 B logDoS, 16 B histogram)
+FLIPS_PER_STEP = WORKLOAD["sweeps_per_check"] * WORKLOAD["num_windows"] * WORKLOAD["replicas_per_window"] * 32 * 32
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """dram bytes per sweep-kernel launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "sweep_ising_L32_rewl.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_batch(rg, seed: int, device: int):
+    w = WORKLOAD
+    ins = rg.Instance(model=rg.MODEL_ISING2D, L=w["L"], energy_min=w["energy_min"], energy_max=w["energy_max"],
+                      bin_width=w["bin_width"], num_windows=w["num_windows"],
+                      replicas_per_window=w["replicas_per_window"], window_overlap=w["window_overlap"], seed=seed)
+    return rg.Batch(instances=[ins], sweeps_per_exchange=w["sweeps_per_exchange"],
+                    sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
+                    lnf_final=w["lnf_final"], device=device)
+
+
+# --------------------------------------------------------------------------- CPU leg
+def cpu_port_rate(target_seconds: float, threads: int, steps: int | None = None, warmup: int = 0):
+    """Flips/s of the oracle port (reference semantics) on `threads` host threads."""
+    from oracle import pyoracle as po
+    w = WORKLOAD
+    cfg = po.Config(model=po.MODEL_ISING, L=w["L"], nwin=w["num_windows"], R=w["replicas_per_window"],
+                    sweeps_per_exchange=w["sweeps_per_exchange"], sweeps_per_check=w["sweeps_per_check"],
+                    emin=w["energy_min"], emax=w["energy_max"], bw=w["bin_width"], overlap=w["window_overlap"],
+                    lnf0=w["lnf_initial"], lnf_final=w["lnf_final"], semantics=po.SEM_REFERENCE, nthreads=threads,
+                    seed=2024)
+    orc = po.Oracle(cfg)
+    flips_per_sweep = w["num_windows"] * w["replicas_per_window"] * w["L"] ** 2
+    for _ in range(warmup):
+        orc.run_sweeps(w["sweeps_per_exchange"])
+    times = []
+    done_steps = 0
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        orc.cycle()
+        times.append(time.perf_counter() - t0)
+        done_steps += 1
+        if steps is not None:
+            if done_steps >= steps:
+                break
+        elif time.perf_counter() - t_start >= target_seconds:
+            break
+    orc.close()
+    total = sum(times)
+    rate = done_steps * w["sweeps_per_check"] * flips_per_sweep / total
+    return rate, done_steps, total, times
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    rate, n, total, times = cpu_port_rate(0, threads, steps=args.steps, warmup=args.warmup)
+    line = {
+        "metric": METRIC, "value": rate, "unit": "flips/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / n, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD["name"], **{k: v for k, v in WORKLOAD.items() if k != "name"},
+                   "step": "one check interval: 2 x (500 sweeps + exchange) + flatness/averaging/ln f"},
+        "cpu_baseline": {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} check intervals of the full workload (each 1000 sweeps x 128 walkers)"},
+        "e2e": {"value": rate, "unit": "flips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------- GPU leg
+def time_to_accuracy(rg, device: int, tol: float = 1e-2, max_seconds: float = 1800.0):
+    z = np.load(ROOT / "tests" / "golden" / "exact_ising_L32.npz")
+    exact = z["lng"]
+    batch = make_batch(rg, seed=777, device=device)
+    t0 = time.perf_counter()
+    with rg.Engine(batch) as eng:
+        while True:
+            st = eng.run_cycles(1)
+            E, g = eng.global_logdos(0)
+            err = float(np.abs(g - exact).max()) if len(g) == len(exact) else float("inf")
+            el = time.perf_counter() - t0
+            if err <= tol or st.all_done or el > max_seconds:
+                lnf, _ = eng.window_state(0, 0)
+                return {"seconds": el, "max_abs_dlng": err, "reached": err <= tol, "sweeps": st.sweeps,
+                        "flips": st.attempted_flips, "lnf_window0": lnf, "tolerance": tol}
+
+
+def run_gpu(args):
+    import torch
+    import rewl_simulator_gb300 as rg
+
+    rank, world, local = dist_env()
+    device = local
+    torch.cuda.set_device(device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", device))
+    rg.build()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    batch = make_batch(rg, seed=1000 + rank, device=device)
+    eng = rg.Engine(batch)
+    stream = torch.cuda.ExternalStream(eng.stream_handle(), device=torch.device("cuda", device))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            eng.run_cycles(1)
+        eng.sweep_kernel_time()
+        st0 = eng.status()
+        barrier()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        sampler = ClockSampler(device)
+        with sampler:
+            for k in range(args.steps):
+                flush.zero_()
+                evs[k][0].record(stream)
+                eng.run_cycles(1)
+                evs[k][1].record(stream)
+            torch.cuda.synchronize()
+        barrier()
+        step_ms = [a.elapsed_time(b) for a, b in evs]
+        st1 = eng.status()
+        kern_ms, kern_launches = eng.sweep_kernel_time()
+    total_ms = sum(step_ms)
+    flips = st1.attempted_flips - st0.attempted_flips
+    launches = st1.kernel_launches - st0.kernel_launches
+
+    # end to end through the public API with host-resident walker state (pinned)
+    nbytes = eng.snapshot_size()
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    eng.snapshot_into(host.data_ptr(), nbytes)
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        eng.restore_from(host.data_ptr(), nbytes)
+        eng.run_cycles(1)
+        eng.snapshot_into(host.data_ptr(), nbytes)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_rate = e2e_steps * FLIPS_PER_STEP / e2e_s
+    eng.close()
+
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms, float(flips), e2e_s, float(e2e_steps * FLIPS_PER_STEP)], device=f"cuda:{device}",
+                         dtype=torch.float64)
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        tsum = t.clone()
+        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        total_ms, e2e_s = float(tmax[0]), float(tmax[2])
+        flips, e2e_flips = float(tsum[1]), float(tsum[3])
+        e2e_rate = e2e_flips / e2e_s
+    value = flips / (total_ms * 1e-3)
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_kind = peaks()
+    avg_launch_ms = kern_ms / max(kern_launches, 1)
+    flips_per_launch = WORKLOAD["sweeps_per_exchange"] * WORKLOAD["num_windows"] * WORKLOAD["replicas_per_window"] * 32 * 32
+    achieved = BYTES_PER_FLIP * flips_per_launch / (avg_launch_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "flips/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": {"workload": WORKLOAD["name"], **{k: v for k, v in WORKLOAD.items() if k != "name"},
+                   "step": "one check interval: 2 x (500 sweeps + exchange) + flatness/averaging/ln f",
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"instances x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic_per_launch(),
+                     "kernel": "k_sweep_ising", "bytes_per_flip": BYTES_PER_FLIP,
+                     "avg_launch_ms": avg_launch_ms, "flips_per_launch": flips_per_launch},
+        "e2e": {"value": e2e_rate, "unit": "flips/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": e2e_steps},
+        "clocks": sampler.summary(),
+        "gpu_launches": int(launches),
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, n, total, _ = cpu_port_rate(args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
+                                "sample": f"{n} check intervals of the same workload ({total:.1f} s)"}
+    if args.tta:
+        line["time_to_accuracy"] = time_to_accuracy(rg, device)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--tta", action="store_true", help="also measure GPU time to max|d ln g| <= 1e-2")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -99,6 +99,7 @@ typedef struct rewl_status {
     int64_t exchanges_attempted;
     int64_t exchanges_accepted;
     int64_t attempted_flips;      /* single-spin(-flavour) attempts by all walkers */
+    int64_t kernel_launches;      /* engine kernels launched since creation */
     int32_t all_done;
     int32_t device_error;         /* device error word (0 = none) */
 } rewl_status;
@@ -206,6 +207,17 @@ int rewl_global_logdos(rewl_engine* eng, int32_t instance, int32_t half_spectrum
 /* Device time spent in the sweep kernels since the last call (ms) and the
  * number of sweep-kernel launches; timed with CUDA events on the engine stream. */
 int rewl_sweep_kernel_time(rewl_engine* eng, double* milliseconds, int64_t* launches);
+
+/* Checkpoint / resume of every mutable device array (lattices, energies, slot
+ * mapping, tables, ln f and schedule state, counters).  The reference has no
+ * checkpointing (it only prints histograms, src/REWL/rewl_histograms.hpp:155-170).
+ * rewl_snapshot_size gives the byte count; rewl_snapshot copies the state into
+ * `buffer` (device -> host), rewl_restore copies it back into an engine created
+ * from the same descriptor.  Copies are issued on the engine stream; pinned host
+ * buffers make them asynchronous DMA transfers.  Both calls synchronise. */
+int rewl_snapshot_size(const rewl_engine* eng, size_t* bytes);
+int rewl_snapshot(rewl_engine* eng, void* buffer, size_t bytes);
+int rewl_restore(rewl_engine* eng, const void* buffer, size_t bytes);
 
 /* The CUDA stream the engine launches on (cudaStream_t as void*). */
 int rewl_get_stream(rewl_engine* eng, void** stream);

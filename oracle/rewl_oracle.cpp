@@ -333,30 +333,33 @@ static Binning make_binning(const Config& c)
     return b;
 }
 
-// glazier::construct_windows with EQUAL_WINDOWS (src/REWL/glazier.hpp:305-351).
+// glazier::construct_windows with EQUAL_WINDOWS (src/REWL/glazier.hpp:305-351),
+// in units of bins: each window starts on the global bin grid at the previous
+// start plus the whole bins to its nominal start and covers its nominal width
+// in whole bins, clipped to the global range.  Identical to the reference for
+// integer widths; exact for fractional ones.
 struct WinDef { double min, max; size_t nbins; int64_t gb_lo; };
 
 static std::vector<WinDef> make_windows(const Config& c, const Binning& bn)
 {
     std::vector<WinDef> w(c.nwin);
+    const int64_t G = (int64_t)std::llround((c.emax - c.emin) / c.bw);
     const double denom = 1 + (c.nwin - 1) * (1 - c.overlap);
     const double size = (c.emax - c.emin) / denom;
+    const double eps = 1e-9;
     for (int k = 0; k < c.nwin; ++k)
     {
-        double wmin = c.emin + (double)k * (1 - c.overlap) * size;
-        double wmax = wmin + size;
-        if (k != 0)
-            wmin = w[k - 1].min + c.bw * (double)((size_t)((wmin - w[k - 1].min) / c.bw));
-        size_t nb = (size_t)std::ceil((wmax - wmin) / c.bw);
-        wmax = wmin + c.bw * (double)nb;
-        while (wmax > c.emax) wmax -= c.bw;
-        nb = (size_t)((wmax - wmin) / c.bw);
-        w[k].min = wmin; w[k].max = wmax; w[k].nbins = nb;
-        // snap onto the exact global bin grid
-        w[k].gb_lo = (int64_t)std::llround((wmin - c.emin) / c.bw);
-        w[k].nbins = (size_t)std::llround((wmax - c.emin) / c.bw) - (size_t)w[k].gb_lo;
-        w[k].min = c.emin + c.bw * (double)w[k].gb_lo;
-        w[k].max = c.emin + c.bw * (double)(w[k].gb_lo + (int64_t)w[k].nbins);
+        const double raw_min = c.emin + (double)k * (1 - c.overlap) * size;
+        const double raw_max = raw_min + size;
+        int64_t lo = 0;
+        if (k != 0) lo = w[k - 1].gb_lo + (int64_t)std::floor((raw_min - w[k - 1].min) / c.bw + eps);
+        const double wmin = c.emin + c.bw * (double)lo;
+        int64_t hi = lo + (int64_t)std::ceil((raw_max - wmin) / c.bw - eps);
+        if (hi > G) hi = G;
+        w[k].gb_lo = lo;
+        w[k].nbins = (size_t)(hi - lo);
+        w[k].min = wmin;
+        w[k].max = c.emin + c.bw * (double)hi;
     }
     (void)bn;
     return w;
@@ -365,7 +368,7 @@ static std::vector<WinDef> make_windows(const Config& c, const Binning& bn)
 // ----------------------------------------------------------------------------
 // One walker slot (window w, replica r).
 // ----------------------------------------------------------------------------
-template <class M> struct Walker
+template <class M> struct alignas(128) Walker
 {
     M sys;
     int win = 0, rep = 0; uint32_t uid = 0;
@@ -422,6 +425,9 @@ template <> void init_model<AshkinTeller>(Sim<AshkinTeller>& S, AshkinTeller& m,
     m.spin.assign(2 * m.N, 1.0);
     if (fields) m.field.assign(fields, fields + m.N);
 }
+
+static inline void set_flavour(Ising&, int) {}
+static inline void set_flavour(AshkinTeller& m, int f) { m.st.which = f; }
 
 // adjust_state_to_range (src/REWL/rewl_walker.hpp:79-115); returns false when
 // the deterministic walk did not reach the window within max_steps.
@@ -491,6 +497,8 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
             Walker<M>& k = S->wk[(size_t)w * R + r];
             k.win = w; k.rep = r; k.uid = (uint32_t)(w * R + r);
             k.gb_lo = S->wins[w].gb_lo; k.nb = S->wins[w].nbins;
+            // spare capacity keeps neighbouring walkers' hot entries on separate cache lines
+            k.count.reserve(k.nb + 32); k.visits.reserve(k.nb + 32); k.logdos.reserve(k.nb + 32);
             k.count.assign(k.nb, 0); k.visits.assign(k.nb, 0); k.logdos.assign(k.nb, 0.0);
             k.obs.assign(k.nb * M::num_obs, 0.0);
             k.lnf = c.lnf0;
@@ -523,6 +531,7 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
             {   // stuck in a local extremum: restart from the all +1 state and walk up
                 std::fill(k.sys.spin.begin(), k.sys.spin.end(), 1.0);
                 k.sys.recalculate();
+                set_flavour(k.sys, 0);
                 if (!adjust(*S, k, start, cap)) { delete S; return nullptr; }
             }
         }

@@ -88,6 +88,9 @@ def _declare(L: C.CDLL) -> None:
         "rewl_global_logdos": [vp, i32, i32, vp, vp, vp],
         "rewl_sweep_kernel_time": [vp, vp, vp],
         "rewl_get_stream": [vp, vp],
+        "rewl_snapshot_size": [vp, vp],
+        "rewl_snapshot": [vp, vp, sz],
+        "rewl_restore": [vp, vp, sz],
     }
     for name, args in sigs.items():
         f = getattr(L, name)

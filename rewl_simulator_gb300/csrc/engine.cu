@@ -836,7 +836,8 @@ struct rewl_engine {
     std::vector<Launch> launches;
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
-    int64_t kernel_launches = 0;
+    int64_t kernel_launches = 0;        // sweep-kernel launches since the last timing read
+    int64_t launches_total = 0;         // every engine kernel since creation
 
     DBuf<InstDev> d_inst;
     DBuf<WinDev> d_win;
@@ -905,29 +906,37 @@ int largest_chunk(int L)
 }
 
 // glazier::construct_windows, EQUAL_WINDOWS branch (src/REWL/glazier.hpp:305-351),
-// followed by snapping each window onto the exact global bin grid.
-void make_windows(const rewl_instance_desc& d, std::vector<double>& mins, std::vector<double>& maxs,
-                  std::vector<int64_t>& gblo, std::vector<int>& nbins)
+// carried out in units of bins: window k starts at the previous window's start
+// plus the whole bins up to its nominal start, and spans the whole bins that
+// cover its nominal width, clipped to the global range.  For integer widths
+// this is the reference's arithmetic exactly; for fractional widths it avoids
+// the bin the reference's double ceil/clip can lose.
+int make_windows(const rewl_instance_desc& d, std::vector<double>& mins, std::vector<double>& maxs,
+                 std::vector<int64_t>& gblo, std::vector<int>& nbins)
 {
     const int nw = d.num_windows;
     const double gmin = d.energy_min, gmax = d.energy_max, bw = d.bin_width, ov = d.window_overlap;
     mins.assign(nw, 0); maxs.assign(nw, 0); gblo.assign(nw, 0); nbins.assign(nw, 0);
+    const double span = (gmax - gmin) / bw;
+    const int64_t G = (int64_t)std::llround(span);
+    if (std::fabs(span - (double)G) > 1e-6 * std::max(1.0, span) || G < 1) return -1;
     const double denom = 1 + (nw - 1) * (1 - ov);
     const double size = (gmax - gmin) / denom;
-    std::vector<double> raw_min(nw);
+    const double eps = 1e-9;
     for (int k = 0; k < nw; ++k) {
-        double wmin = gmin + (double)k * (1 - ov) * size;
-        double wmax = wmin + size;
-        if (k != 0) wmin = raw_min[k - 1] + bw * (double)((size_t)((wmin - raw_min[k - 1]) / bw));
-        size_t nb = (size_t)std::ceil((wmax - wmin) / bw);
-        wmax = wmin + bw * (double)nb;
-        while (wmax > gmax) wmax -= bw;
-        raw_min[k] = wmin;
-        gblo[k] = (int64_t)std::llround((wmin - gmin) / bw);
-        nbins[k] = (int)(std::llround((wmax - gmin) / bw) - gblo[k]);
-        mins[k] = gmin + bw * (double)gblo[k];
-        maxs[k] = gmin + bw * (double)(gblo[k] + nbins[k]);
+        const double raw_min = gmin + (double)k * (1 - ov) * size;
+        const double raw_max = raw_min + size;
+        int64_t lo = 0;
+        if (k != 0) lo = gblo[k - 1] + (int64_t)std::floor((raw_min - mins[k - 1]) / bw + eps);
+        const double wmin = gmin + bw * (double)lo;
+        int64_t hi = lo + (int64_t)std::ceil((raw_max - wmin) / bw - eps);
+        if (hi > G) hi = G;
+        gblo[k] = lo;
+        nbins[k] = (int)(hi - lo);
+        mins[k] = wmin;
+        maxs[k] = gmin + bw * (double)hi;
     }
+    return 0;
 }
 
 void static_mask(const rewl_instance_desc& d, double wmin, int nb, uint8_t* m)
@@ -1024,7 +1033,8 @@ int build_host(rewl_engine* e)
             fieldoff += I.N;
         } else I.field_off = -1;
         std::vector<double> mins, maxs; std::vector<int64_t> gblo; std::vector<int> nbins;
-        make_windows(d, mins, maxs, gblo, nbins);
+        if (make_windows(d, mins, maxs, gblo, nbins))
+            return fail(REWL_EINVAL, "instance %d: the energy range is not a whole number of bins", ii);
         for (int k = 0; k < d.num_windows; ++k) {
             if (nbins[k] < 1) return fail(REWL_EINVAL, "instance %d: window %d is empty", ii, k);
             if (k > 0 && gblo[k] >= gblo[k - 1] + nbins[k - 1]) return fail(REWL_EINVAL, "instance %d: windows %d and %d do not overlap", ii, k - 1, k);
@@ -1208,6 +1218,7 @@ int launch_sweeps(rewl_engine* e, int nsweeps)
         }
         CUDA_TRY(cudaGetLastError());
         e->kernel_launches++;
+        e->launches_total++;
     }
     cudaEventRecord(next_event(e), e->stream);
     e->sweeps_total += nsweeps;
@@ -1223,6 +1234,7 @@ int launch_exchange(rewl_engine* e)
     if (npairs > 0) {
         k_exchange<<<(npairs + 127) / 128, 128, 0, e->stream>>>(e->ptrs(), e->pairs[dir].p, npairs, e->exch_round);
         CUDA_TRY(cudaGetLastError());
+        e->launches_total++;
     }
     e->direction ^= 1;
     e->exch_round++;
@@ -1246,6 +1258,7 @@ int launch_flat(rewl_engine* e)
     e->sweeps_since_check = 0;
     k_flat<<<e->nwin_total, 256, 0, e->stream>>>(fp);
     CUDA_TRY(cudaGetLastError());
+    e->launches_total++;
     return REWL_OK;
 }
 
@@ -1576,6 +1589,7 @@ int rewl_get_status(rewl_engine* e, rewl_status* st)
     st->exchanges_accepted = (int64_t)stats[1];
     st->attempted_flips = e->flips_total;
     st->device_error = counters[0];
+    st->kernel_launches = e->launches_total;
     return REWL_OK;
 }
 
@@ -1746,6 +1760,73 @@ int rewl_sweep_kernel_time(rewl_engine* e, double* ms, int64_t* launches)
     if (launches) *launches = e->kernel_launches;
     e->ev_used = 0;
     e->kernel_launches = 0;
+    return REWL_OK;
+}
+
+namespace {
+struct SnapPart { void* dev; size_t bytes; };
+
+std::vector<SnapPart> snapshot_parts(rewl_engine* e)
+{
+    auto P = [](auto& b) { return SnapPart{(void*)b.p, b.n * sizeof(*b.p)}; };
+    return {P(e->slot_cfg), P(e->slot_flavour), P(e->slot_sweeps), P(e->slot_draws), P(e->cfg_E), P(e->cfg_M),
+            P(e->spins), P(e->g), P(e->H), P(e->visits), P(e->win_lnf), P(e->win_done), P(e->win_oot),
+            P(e->win_iter), P(e->win_sweepctr), P(e->stats)};
+}
+
+struct SnapHeader {
+    uint64_t magic, bytes, exch_round, sweeps_since_check;
+    int64_t sweeps_total, cycles, flat_events, flips_total;
+    int32_t direction, nslots, nwin, pad;
+};
+constexpr uint64_t kSnapMagic = 0x5245574C534E4150ull;   // "REWLSNAP"
+} // namespace
+
+int rewl_snapshot_size(const rewl_engine* e, size_t* bytes)
+{
+    if (!e || !bytes) return fail(REWL_EINVAL, "null argument");
+    size_t n = sizeof(SnapHeader);
+    for (auto& p : snapshot_parts(const_cast<rewl_engine*>(e))) n += (p.bytes + 15) & ~size_t(15);
+    *bytes = n;
+    return REWL_OK;
+}
+
+int rewl_snapshot(rewl_engine* e, void* buffer, size_t bytes)
+{
+    size_t need = 0;
+    if (int rc = rewl_snapshot_size(e, &need)) return rc;
+    if (!buffer || bytes < need) return fail(REWL_EINVAL, "snapshot buffer too small (%zu bytes needed)", need);
+    cudaSetDevice(e->desc.device);
+    SnapHeader h{kSnapMagic, need, e->exch_round, e->sweeps_since_check, e->sweeps_total, e->cycles, e->flat_events,
+                 e->flips_total, e->direction, e->nslots, e->nwin_total, 0};
+    std::memcpy(buffer, &h, sizeof h);
+    char* dst = static_cast<char*>(buffer) + sizeof h;
+    for (auto& p : snapshot_parts(e)) {
+        if (p.bytes) CUDA_TRY(cudaMemcpyAsync(dst, p.dev, p.bytes, cudaMemcpyDeviceToHost, e->stream));
+        dst += (p.bytes + 15) & ~size_t(15);
+    }
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return REWL_OK;
+}
+
+int rewl_restore(rewl_engine* e, const void* buffer, size_t bytes)
+{
+    size_t need = 0;
+    if (int rc = rewl_snapshot_size(e, &need)) return rc;
+    if (!buffer || bytes < need) return fail(REWL_EINVAL, "snapshot buffer too small (%zu bytes needed)", need);
+    SnapHeader h;
+    std::memcpy(&h, buffer, sizeof h);
+    if (h.magic != kSnapMagic || h.bytes != need || h.nslots != e->nslots || h.nwin != e->nwin_total)
+        return fail(REWL_EINVAL, "snapshot does not match this engine's layout");
+    cudaSetDevice(e->desc.device);
+    const char* src = static_cast<const char*>(buffer) + sizeof h;
+    for (auto& p : snapshot_parts(e)) {
+        if (p.bytes) CUDA_TRY(cudaMemcpyAsync(p.dev, src, p.bytes, cudaMemcpyHostToDevice, e->stream));
+        src += (p.bytes + 15) & ~size_t(15);
+    }
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->exch_round = h.exch_round; e->sweeps_since_check = h.sweeps_since_check; e->sweeps_total = h.sweeps_total;
+    e->cycles = h.cycles; e->flat_events = h.flat_events; e->flips_total = h.flips_total; e->direction = h.direction;
     return REWL_OK;
 }
 

@@ -60,7 +60,8 @@ class _Status(C.Structure):
     _fields_ = [("sweeps", C.c_int64), ("cycles", C.c_int64), ("flat_events", C.c_int64),
                 ("windows_done", C.c_int64), ("windows_total", C.c_int64),
                 ("exchanges_attempted", C.c_int64), ("exchanges_accepted", C.c_int64),
-                ("attempted_flips", C.c_int64), ("all_done", C.c_int32), ("device_error", C.c_int32)]
+                ("attempted_flips", C.c_int64), ("kernel_launches", C.c_int64), ("all_done", C.c_int32),
+                ("device_error", C.c_int32)]
 
 
 @dataclass
@@ -116,6 +117,7 @@ class Status:
     exchanges_attempted: int
     exchanges_accepted: int
     attempted_flips: int
+    kernel_launches: int
     all_done: bool
     device_error: int
 
@@ -260,8 +262,8 @@ class Engine:
     @staticmethod
     def _status(st: _Status) -> Status:
         return Status(st.sweeps, st.cycles, st.flat_events, st.windows_done, st.windows_total,
-                      st.exchanges_attempted, st.exchanges_accepted, st.attempted_flips, bool(st.all_done),
-                      st.device_error)
+                      st.exchanges_attempted, st.exchanges_accepted, st.attempted_flips, st.kernel_launches,
+                      bool(st.all_done), st.device_error)
 
     # -- exports ------------------------------------------------------------------
     def export_walker(self, walker: int):
@@ -307,6 +309,28 @@ class Engine:
         ms, n = C.c_double(), C.c_int64()
         self._check(self.lib.rewl_sweep_kernel_time(self.h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def snapshot_size(self) -> int:
+        n = C.c_size_t()
+        self._check(self.lib.rewl_snapshot_size(self.h, C.byref(n)))
+        return n.value
+
+    def snapshot_into(self, ptr: int, nbytes: int) -> None:
+        """Copy the full device state into host memory at `ptr` (checkpoint)."""
+        self._check(self.lib.rewl_snapshot(self.h, C.c_void_p(ptr), nbytes))
+
+    def restore_from(self, ptr: int, nbytes: int) -> None:
+        """Load a state written by snapshot_into (resume)."""
+        self._check(self.lib.rewl_restore(self.h, C.c_void_p(ptr), nbytes))
+
+    def snapshot(self) -> np.ndarray:
+        buf = np.zeros(self.snapshot_size(), dtype=np.uint8)
+        self.snapshot_into(buf.ctypes.data, buf.nbytes)
+        return buf
+
+    def restore(self, buf: np.ndarray) -> None:
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        self.restore_from(buf.ctypes.data, buf.nbytes)
 
     def stream_handle(self) -> int:
         s = C.c_void_p()

@@ -135,3 +135,19 @@ def test_normalize_logdos():
         y = [float.fromhex(v) for v in c["out"]]
         got = normalize_logdos(c["states_per_site"], c["N"], c["energy_max"], x)
         assert [v.hex() for v in got] == [v.hex() for v in y], name
+
+
+def test_oracle_windows_equal_reference_glazier(oracle_lib):
+    """Windows of the oracle (and, by the same code, the engine) equal the reference's
+    glazier output for integer bin widths."""
+    po = oracle_lib
+    cases = json.loads((GOLDEN / "glazier.json").read_text())
+    for name in ("C1_L16", "C2_L32", "L24_16w"):
+        gmin, gmax, bw, n, r, ov = cases[name]["args"]
+        L = {"C1_L16": 16, "C2_L32": 32, "L24_16w": 24}[name]
+        cfg = po.Config(model=0, L=L, nwin=n, R=1, emin=gmin, emax=gmax, bw=bw, overlap=ov, init_mode=1)
+        orc = po.Oracle(cfg)
+        for k in range(n):
+            mn, mx, lo, nb = orc.windows[k]
+            assert (mn, mx, nb) == (cases[name]["mins"][k], cases[name]["maxs"][k], cases[name]["nbins"][k]), (name, k)
+        orc.close()
