@@ -317,7 +317,7 @@ def run_gpu(args):
         line["cpu_baseline"] = {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
                                 "sample": f"{n} check intervals of the same workload ({total:.1f} s)"}
     if args.tta:
-        line["time_to_accuracy"] = time_to_accuracy(rg, device)
+        line["time_to_accuracy"] = time_to_accuracy(rg, device, max_seconds=args.tta_seconds)
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -332,6 +332,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--tta", action="store_true", help="also measure GPU time to max|d ln g| <= 1e-2")
+    ap.add_argument("--tta-seconds", type=float, default=1800.0, help="give up the time-to-accuracy run after this")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

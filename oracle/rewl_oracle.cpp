@@ -502,7 +502,7 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
             k.count.assign(k.nb, 0); k.visits.assign(k.nb, 0); k.logdos.assign(k.nb, 0.0);
             k.obs.assign(k.nb * M::num_obs, 0.0);
             k.lnf = c.lnf0;
-            k.lnf_u = (int64_t)std::llround(c.lnf0 * QSCALE);
+            k.lnf_u = std::max<int64_t>(1, (int64_t)std::llround(c.lnf0 * QSCALE));
             init_model<M>(*S, k.sys, fields);
             const size_t nd = k.sys.num_dof();
             if (init_dofs) { for (size_t i = 0; i < nd; ++i) k.sys.spin[i] = init_dofs[i]; }
@@ -772,6 +772,7 @@ template <class M> static int flat_step(Sim<M>& S)
             {
                 if (S.c.one_over_t && !S.oot[w] && (double)k.lnf_u <= QSCALE / (double)t) S.oot[w] = 1;
                 k.lnf_u = S.oot[w] ? (int64_t)(((uint64_t)1 << QBITS) + t / 2) / (int64_t)t : (k.lnf_u >> 1);
+                if (k.lnf_u < 1) k.lnf_u = 1;           // smallest increment of the 2^-40 grid
                 k.lnf = (double)k.lnf_u / QSCALE;
             }
         }
@@ -1008,7 +1009,7 @@ void orc_walker_set_dofs(void* p, size_t slot, const double* dofs, int which)
 }
 void orc_walker_set_lnf(void* p, size_t slot, double lnf)
 {
-    DISPATCH(static_cast<OrcHandle*>(p), { S.wk[slot].lnf = lnf; S.wk[slot].lnf_u = (int64_t)std::llround(lnf * QSCALE); });
+    DISPATCH(static_cast<OrcHandle*>(p), { S.wk[slot].lnf = lnf; S.wk[slot].lnf_u = std::max<int64_t>(1, (int64_t)std::llround(lnf * QSCALE)); });
 }
 void orc_walker_set_logdos(void* p, size_t slot, const double* g)
 {

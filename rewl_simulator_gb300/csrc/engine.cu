@@ -32,6 +32,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -285,8 +286,9 @@ struct SweepParams {
     int nbcap;               // table capacity per warp (Ising, shared memory)
 };
 
-// Per-warp staging of one chunk: energy change without / with the left
-// neighbour flipped, wrap correction (x = L-1 sees the row start), threshold.
+// Per-warp staging of one chunk for the lane-0 resolver: energy change without /
+// with the left neighbour flipped, wrap correction (x = L-1 sees the row start),
+// acceptance threshold.
 struct Stage {
     long long T[32];
     int d0[32];
@@ -294,7 +296,65 @@ struct Stage {
     int wc[32];
 };
 
-template <bool REPLAY>
+// Accept chain of one chunk of C sites, executed identically by all 32 lanes
+// (every lane holds the same E, b, gc, acc).  Lane j owns site j's precomputed
+// values; they reach every lane by shuffles that depend on nothing in the chain,
+// so the unrolled loop issues them early.  The proposal of step j+1 depends on
+// step j's outcome only through (E, left-neighbour flip, wrap flip): both
+// candidates are formed and their logDoS entries loaded before step j resolves,
+// which takes the shared-memory latency off the chain.  The only store that can
+// land between such a prefetch and its use is step j's own, to the bin step j
+// ends in: that case takes the freshly stored value.
+template <int C>
+__device__ __forceinline__ void resolve_chunk_all_lanes(int& E, int& b, long long& gc, unsigned& acc,
+                                                        long long* gs, const int Ewlo, const int sh, const int nb,
+                                                        const long long lnf, const int my_d0, const int my_d1,
+                                                        const int my_wc, const long long my_T)
+{
+    int En = E + __shfl_sync(kFull, my_d0, 0);
+    int bn = (En - Ewlo) >> sh;
+    bool inr = (unsigned)bn < (unsigned)nb;
+    long long gn = gs[inr ? bn : b];
+#pragma unroll
+    for (int j = 0; j < C; ++j) {
+        const long long Tj = __shfl_sync(kFull, my_T, j);
+        int E0 = 0, E1 = 0, b0 = 0, b1 = 0;
+        bool i0 = false, i1 = false;
+        long long g0 = 0, g1 = 0;
+        if (j + 1 < C) {
+            const int d0n = __shfl_sync(kFull, my_d0, j + 1);
+            const int d1n = __shfl_sync(kFull, my_d1, j + 1);
+            const int wcn = __shfl_sync(kFull, my_wc, j + 1);
+            const int w0 = (acc & 1u) ? wcn : 0;
+            const int w1 = (j == 0 || (acc & 1u)) ? wcn : 0;
+            E0 = E + d0n + w0;
+            E1 = En + d1n + w1;
+            b0 = (E0 - Ewlo) >> sh;
+            b1 = (E1 - Ewlo) >> sh;
+            i0 = (unsigned)b0 < (unsigned)nb;
+            i1 = (unsigned)b1 < (unsigned)nb;
+            g0 = gs[i0 ? b0 : 0];
+            g1 = gs[i1 ? b1 : 0];
+        }
+        const bool a = inr && (gn - gc < Tj);
+        if (a) { E = En; b = bn; gc = gn; acc |= 1u << j; }
+        gc += lnf;
+        gs[b] = gc;
+        if (j + 1 < C) {
+            En = a ? E1 : E0;
+            bn = a ? b1 : b0;
+            inr = a ? i1 : i0;
+            gn = a ? g1 : g0;
+            if (bn == b) gn = gc;
+        }
+    }
+}
+
+// Ising sweeps.  One warp per walker; lattice and logDoS staged in shared memory
+// for the whole launch.  Per-stage counts are not kept in the loop: within a
+// launch every visit adds the same ln f, so the counts added to bin k are
+// (g_end[k] - g_start[k]) / ln f exactly (ln f >= one 2^-40 unit always).
+template <bool REPLAY, int VARIANT>
 __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -309,16 +369,14 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
     const int L = I.L, N = I.N, C = I.chunk, nb = W.nb;
     unsigned char* base = smem + (size_t)wib * p.smem_per_warp;
     long long* gs = reinterpret_cast<long long*>(base);
-    uint32_t* Hs = reinterpret_cast<uint32_t*>(gs + p.nbcap);
-    Stage* st = reinterpret_cast<Stage*>(Hs + p.nbcap);
+    Stage* st = reinterpret_cast<Stage*>(gs + p.nbcap);
     int8_t* lat = reinterpret_cast<int8_t*>(st + 1);
 
     const int cfg = P.slot_cfg[s];
     int8_t* gl = P.spins + P.cfg_off[cfg];
     for (int i = lane; i < N; i += 32) lat[i] = gl[i];
     long long* gg = reinterpret_cast<long long*>(P.g + P.slot_tab[s]);
-    uint32_t* gH = P.H + P.slot_tab[s];
-    for (int b = lane; b < nb; b += 32) { gs[b] = gg[b]; Hs[b] = gH[b]; }
+    for (int k = lane; k < nb; k += 32) gs[k] = gg[k];
     __syncwarp();
 
     const int J = (int)I.J_u;
@@ -328,84 +386,118 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
     const uint64_t sweeps0 = P.slot_sweeps[s];
     const uint32_t uid = (uint32_t)(s - I.first_slot);
     const uint64_t seed = I.seed;
+    const bool all_lanes = (!REPLAY) && VARIANT == 3 && (C == 32 || C == 16 || C == 24 || C == 8 || C == 4);
 
-    int E = 0, M = 0, b = 0;
-    long long gc = 0;
-    long long draws = 0, thr_off = 0, thr_n = 0;
-    int err = 0;
-    if (lane == 0) {
-        E = (int)P.cfg_E[cfg];
-        M = P.cfg_M[3 * cfg];
-        b = (E - Ewlo) >> sh;
-        if (b < 0 || b >= nb) { err = ERR_BOUNDS; b = 0; }
-        gc = gs[b];
-        if (REPLAY) { draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
-    }
-    err = __shfl_sync(kFull, err, 0);
-    if (err) {
-        if (lane == 0) atomicOr(&P.counters[0], err);
+    int E = (int)P.cfg_E[cfg];
+    int M = P.cfg_M[3 * cfg];
+    int b = (E - Ewlo) >> sh;
+    if (b < 0 || b >= nb) {
+        if (lane == 0) atomicOr(&P.counters[0], ERR_BOUNDS);
         return;
     }
+    long long gc = gs[b];
+    long long draws = 0, thr_off = 0, thr_n = 0;
+    int err = 0;
+    if (REPLAY) { draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
 
     for (int sw = 0; sw < p.nsweeps; ++sw) {
         const uint64_t A0 = (sweeps0 + (uint64_t)sw) * (uint64_t)N;
         for (int c0 = 0; c0 < N; c0 += C) {
-            int si = 0;
+            // chunk = sites c0 .. c0+C-1 of one row (C divides L)
+            const int y = c0 / L, x = c0 - y * L + lane;
+            const int row = y * L;
+            const int up = (y == 0 ? L - 1 : y - 1) * L, down = (y == L - 1 ? 0 : y + 1) * L;
+            int si = 0, d0 = 0, d1 = 0, wc = 0;
+            long long T = 0;
             if (lane < C) {
-                const int i = c0 + lane;
-                si = lat[i];
-                const int left = lat[nb_left(i, L)], right = lat[nb_right(i, L)];
-                const int sum = lat[nb_up(i, L)] + left + right + lat[nb_down(i, L)];
-                const int d0 = 2 * J * si * sum;
-                st->d0[lane] = d0;
-                st->d1[lane] = lane > 0 ? d0 - 4 * J * si * left : d0;
-                st->wc[lane] = (C == L && lane == L - 1) ? -4 * J * si * right : 0;
+                si = lat[row + x];
+                const int left = lat[row + (x == 0 ? L - 1 : x - 1)];
+                const int right = lat[row + (x == L - 1 ? 0 : x + 1)];
+                const int sum = lat[up + x] + left + right + lat[down + x];
+                d0 = 2 * J * si * sum;
+                d1 = lane > 0 ? d0 - 4 * J * si * left : d0;
+                wc = (C == L && lane == L - 1) ? -4 * J * si * right : 0;
                 if (!REPLAY) {
-                    const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)i, kStreamWL);
-                    st->T[lane] = accept_threshold(neglog_u32(word));
+                    const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)(c0 + lane), kStreamWL);
+                    T = accept_threshold(neglog_u32(word));
                 }
             }
-            __syncwarp();
             unsigned acc = 0;
-            if (lane == 0) {
-                for (int j = 0; j < C; ++j) {
-                    int dE = (j > 0 && ((acc >> (j - 1)) & 1u)) ? st->d1[j] : st->d0[j];
-                    dE += (acc & 1u) ? st->wc[j] : 0;
-                    const int En = E + dE;
-                    const int bn = (En - Ewlo) >> sh;
-                    const bool inr = (unsigned)bn < (unsigned)nb;
-                    const long long gn = gs[inr ? bn : b];
-                    const long long d = gn - gc;
-                    bool a;
-                    if (!REPLAY) {
-                        a = inr && (d < st->T[j]);
-                    } else {
-                        if (inr && d > 0) {
+            if (all_lanes) {
+                switch (C) {
+                case 32: resolve_chunk_all_lanes<32>(E, b, gc, acc, gs, Ewlo, sh, nb, lnf, d0, d1, wc, T); break;
+                case 24: resolve_chunk_all_lanes<24>(E, b, gc, acc, gs, Ewlo, sh, nb, lnf, d0, d1, wc, T); break;
+                case 16: resolve_chunk_all_lanes<16>(E, b, gc, acc, gs, Ewlo, sh, nb, lnf, d0, d1, wc, T); break;
+                case 8: resolve_chunk_all_lanes<8>(E, b, gc, acc, gs, Ewlo, sh, nb, lnf, d0, d1, wc, T); break;
+                default: resolve_chunk_all_lanes<4>(E, b, gc, acc, gs, Ewlo, sh, nb, lnf, d0, d1, wc, T); break;
+                }
+            } else {
+                if (lane < C) { st->d0[lane] = d0; st->d1[lane] = d1; st->wc[lane] = wc; st->T[lane] = T; }
+                __syncwarp();
+                if (lane == 0) {
+                    int En = E + st->d0[0];
+                    int bn = (En - Ewlo) >> sh;
+                    bool inr = (unsigned)bn < (unsigned)nb;
+                    long long gn = gs[inr ? bn : b];
+                    for (int j = 0; j < C; ++j) {
+                        int E0 = 0, E1 = 0, b0 = 0, b1 = 0;
+                        bool i0 = false, i1 = false;
+                        long long g0 = 0, g1 = 0;
+                        if (j + 1 < C) {
+                            const int w0 = (acc & 1u) ? st->wc[j + 1] : 0;
+                            const int w1 = (j == 0 || (acc & 1u)) ? st->wc[j + 1] : 0;
+                            E0 = E + st->d0[j + 1] + w0;
+                            E1 = En + st->d1[j + 1] + w1;
+                            b0 = (E0 - Ewlo) >> sh;
+                            b1 = (E1 - Ewlo) >> sh;
+                            i0 = (unsigned)b0 < (unsigned)nb;
+                            i1 = (unsigned)b1 < (unsigned)nb;
+                            g0 = gs[i0 ? b0 : 0];
+                            g1 = gs[i1 ? b1 : 0];
+                        }
+                        const long long d = gn - gc;
+                        bool a;
+                        if (!REPLAY) {
+                            a = inr && (d < st->T[j]);
+                        } else if (inr && d > 0) {
                             if (draws >= thr_n) { err = ERR_REPLAY_EXHAUSTED; a = false; }
                             else { a = d < P.thr[thr_off + draws]; ++draws; }
-                        } else a = inr;
+                        } else {
+                            a = inr;
+                        }
+                        if (a) { E = En; b = bn; gc = gn; acc |= 1u << j; }
+                        gc += lnf;
+                        gs[b] = gc;
+                        En = a ? E1 : E0;
+                        bn = a ? b1 : b0;
+                        inr = a ? i1 : i0;
+                        gn = a ? g1 : g0;
+                        if (bn == b) gn = gc;
                     }
-                    if (a) { E = En; b = bn; gc = gn; acc |= 1u << j; }
-                    gc += lnf;
-                    gs[b] = gc;
-                    Hs[b] += 1u;
                 }
+                // lane 0 holds the chain state; every lane needs it
+                acc = __shfl_sync(kFull, acc, 0);
+                E = __shfl_sync(kFull, E, 0);
+                b = __shfl_sync(kFull, b, 0);
+                gc = __shfl_sync(kFull, gc, 0);
+                if (REPLAY) { draws = __shfl_sync(kFull, draws, 0); err = __shfl_sync(kFull, err, 0); }
             }
-            acc = __shfl_sync(kFull, acc, 0);
             const unsigned plus = __ballot_sync(kFull, lane < C && si > 0);
-            if (lane < C && ((acc >> lane) & 1u)) lat[c0 + lane] = (int8_t)(-si);
-            if (lane == 0) M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus));
+            if (lane < C && ((acc >> lane) & 1u)) lat[row + x] = (int8_t)(-si);
+            M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus));
             __syncwarp();
         }
     }
-    // write back
+    // write back: lattice, logDoS, counts and visits derived from the logDoS change
     for (int i = lane; i < N; i += 32) gl[i] = lat[i];
+    uint32_t* gH = P.H + P.slot_tab[s];
     uint64_t* gv = P.visits + P.slot_tab[s];
     for (int k = lane; k < nb; k += 32) {
-        const uint32_t hn = Hs[k], ho = gH[k];
-        gv[k] += (uint64_t)(hn - ho);
-        gH[k] = hn;
-        gg[k] = gs[k];
+        const long long gnew = gs[k];
+        const long long dv = (gnew - gg[k]) / lnf;
+        gH[k] += (uint32_t)dv;
+        gv[k] += (uint64_t)dv;
+        gg[k] = gnew;
     }
     if (lane == 0) {
         P.cfg_E[cfg] = E;
@@ -753,6 +845,7 @@ __global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
         if (fp.one_over_t && !oot && t > 0 && __ll2double_rn(lnf) <= __ddiv_rn(kLogdosScale, __ull2double_rn(t))) oot = 1;
         if (oot && t > 0) lnf = (long long)((((unsigned long long)1 << kLogdosBits) + t / 2) / t);
         else lnf = lnf >> 1;
+        if (lnf < 1) lnf = 1;                  // the 2^-40 grid's smallest increment
         P.win_lnf[w] = lnf;
         P.win_oot[w] = oot;
         P.win_done[w] = (__ll2double_rn(lnf) / kLogdosScale) < fp.lnf_final ? 1 : 0;
@@ -838,6 +931,7 @@ struct rewl_engine {
     size_t ev_used = 0;
     int64_t kernel_launches = 0;        // sweep-kernel launches since the last timing read
     int64_t launches_total = 0;         // every engine kernel since creation
+    int sweep_variant = 3;              // Ising resolver: 3 all-lane (default), 2 lane-0 (REWL_SWEEP_VARIANT=2)
 
     DBuf<InstDev> d_inst;
     DBuf<WinDev> d_win;
@@ -1120,7 +1214,7 @@ int upload_all(rewl_engine* e)
         CUDA_TRY(cudaMemsetAsync(e->H.p, 0, tab * sizeof(uint32_t), s));
         CUDA_TRY(cudaMemsetAsync(e->visits.p, 0, tab * sizeof(uint64_t), s));
     }
-    std::vector<int64_t> lnf(win, (int64_t)std::llround(D.lnf_initial * kLogdosScale));
+    std::vector<int64_t> lnf(win, std::max<int64_t>(1, (int64_t)std::llround(D.lnf_initial * kLogdosScale)));
     CUDA_TRY(cudaMemcpyAsync(e->win_lnf.p, lnf.data(), win * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     CUDA_TRY(cudaMemsetAsync(e->win_done.p, 0, win * sizeof(int32_t), s));
     CUDA_TRY(cudaMemsetAsync(e->win_oot.p, 0, win * sizeof(int32_t), s));
@@ -1150,7 +1244,7 @@ int plan_launches(rewl_engine* e)
         if (l.slots.empty()) continue;
         if (model == REWL_MODEL_ISING2D) {
             l.nbcap = (maxnb + 1) & ~1;
-            l.smem_per_warp = (int)(l.nbcap * 12 + sizeof(Stage) + ((maxN + 15) & ~15));
+            l.smem_per_warp = (int)(l.nbcap * 8 + sizeof(Stage) + ((maxN + 15) & ~15));
         } else {
             l.nbcap = 0;
             l.smem_per_warp = (int)(sizeof(StageAT) + ((2 * maxN + 15) & ~15));
@@ -1170,8 +1264,9 @@ int plan_launches(rewl_engine* e)
         if (rc) return rc;
         e->launches.push_back(std::move(l));
     }
-    CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-    CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_at<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_at<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     return REWL_OK;
@@ -1210,8 +1305,9 @@ int launch_sweeps(rewl_engine* e, int nsweeps)
         const int blocks = (sp.nslots + l.wpb - 1) / l.wpb;
         const size_t smem = (size_t)l.wpb * l.smem_per_warp;
         if (l.model == REWL_MODEL_ISING2D) {
-            if (replay) k_sweep_ising<true><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
-            else k_sweep_ising<false><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+            if (replay) k_sweep_ising<true, 2><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+            else if (e->sweep_variant == 2) k_sweep_ising<false, 2><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+            else k_sweep_ising<false, 3><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
         } else {
             if (replay) k_sweep_at<true><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
             else k_sweep_at<false><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
@@ -1331,6 +1427,7 @@ int rewl_create(const rewl_batch_desc* desc, rewl_engine** out)
     *out = nullptr;
     rewl_engine* e = new rewl_engine();
     e->desc = *desc;
+    if (const char* v = std::getenv("REWL_SWEEP_VARIANT")) e->sweep_variant = std::atoi(v) == 2 ? 2 : 3;
     int rc = build_host(e);               // descriptor validation and layout: host only
     if (rc) { delete e; return rc; }
     int ndev = 0;
@@ -1474,7 +1571,7 @@ int rewl_set_lnf(rewl_engine* e, int32_t ii, int32_t w, double lnf)
 {
     const int wi = window_index(e, ii, w);
     if (wi < 0 || !(lnf > 0) || lnf > 64) return fail(REWL_EINVAL, "bad window or ln f");
-    const int64_t q = (int64_t)std::llround(lnf * kLogdosScale);
+    const int64_t q = std::max<int64_t>(1, (int64_t)std::llround(lnf * kLogdosScale));
     cudaSetDevice(e->desc.device);
     CUDA_TRY(cudaMemcpyAsync(e->win_lnf.p + wi, &q, 8, cudaMemcpyHostToDevice, e->stream));
     const int32_t done = (lnf < e->desc.lnf_final) ? 1 : 0;
