@@ -131,14 +131,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_batch(rg, seed: int, device: int):
+def make_batch(rg, seed: int, device: int, schedule: str = "halving"):
     w = WORKLOAD
     ins = rg.Instance(model=rg.MODEL_ISING2D, L=w["L"], energy_min=w["energy_min"], energy_max=w["energy_max"],
                       bin_width=w["bin_width"], num_windows=w["num_windows"],
                       replicas_per_window=w["replicas_per_window"], window_overlap=w["window_overlap"], seed=seed)
+    one_over_t = schedule == "1/t"
     return rg.Batch(instances=[ins], sweeps_per_exchange=w["sweeps_per_exchange"],
                     sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
-                    lnf_final=w["lnf_final"], device=device)
+                    lnf_final=w["lnf_final"], device=device, one_over_t=int(one_over_t),
+                    flatness_mode=rg.FLAT_ALL_VISITED if one_over_t else rg.FLAT_MIN_OVER_MEAN)
 
 
 # --------------------------------------------------------------------------- CPU leg
@@ -195,10 +197,10 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------------------- GPU leg
-def time_to_accuracy(rg, device: int, tol: float = 1e-2, max_seconds: float = 1800.0):
+def time_to_accuracy(rg, device: int, tol: float = 1e-2, max_seconds: float = 1800.0, schedule: str = "halving"):
     z = np.load(ROOT / "tests" / "golden" / "exact_ising_L32.npz")
     exact = z["lng"]
-    batch = make_batch(rg, seed=777, device=device)
+    batch = make_batch(rg, seed=777, device=device, schedule=schedule)
     t0 = time.perf_counter()
     with rg.Engine(batch) as eng:
         while True:
@@ -209,7 +211,7 @@ def time_to_accuracy(rg, device: int, tol: float = 1e-2, max_seconds: float = 18
             if err <= tol or st.all_done or el > max_seconds:
                 lnf, _ = eng.window_state(0, 0)
                 return {"seconds": el, "max_abs_dlng": err, "reached": err <= tol, "sweeps": st.sweeps,
-                        "flips": st.attempted_flips, "lnf_window0": lnf, "tolerance": tol}
+                        "flips": st.attempted_flips, "lnf_window0": lnf, "tolerance": tol, "schedule": schedule}
 
 
 def run_gpu(args):
@@ -317,7 +319,8 @@ def run_gpu(args):
         line["cpu_baseline"] = {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
                                 "sample": f"{n} check intervals of the same workload ({total:.1f} s)"}
     if args.tta:
-        line["time_to_accuracy"] = time_to_accuracy(rg, device, max_seconds=args.tta_seconds)
+        line["time_to_accuracy"] = time_to_accuracy(rg, device, max_seconds=args.tta_seconds,
+                                                    schedule=args.tta_schedule)
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -333,6 +336,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--tta", action="store_true", help="also measure GPU time to max|d ln g| <= 1e-2")
     ap.add_argument("--tta-seconds", type=float, default=1800.0, help="give up the time-to-accuracy run after this")
+    ap.add_argument("--tta-schedule", choices=["halving", "1/t"], default="halving",
+                    help="ln f schedule of the time-to-accuracy run (1/t: the reference's default build)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -86,7 +86,9 @@ typedef struct rewl_batch_desc {
     int32_t reduce_logdos;        /* REDUCE_LOGDOS: subtract logdos[0] at each histogram reset */
     int32_t rng_mode;             /* REWL_RNG_* */
     int32_t device;               /* CUDA device ordinal */
-    int32_t walkers_per_block;    /* 0: automatic (autotuned); else 1, 2, 4 or 8 */
+    int32_t warps_per_block;      /* 0: automatic; else 1, 2, 4 or 8 */
+    int32_t walkers_per_warp;     /* 0: automatic; else 1, 2 or 4 (Ising bin-tracking kernel) */
+    int32_t reserved;
     const rewl_instance_desc* instances;
 } rewl_batch_desc;
 
@@ -221,6 +223,36 @@ int rewl_restore(rewl_engine* eng, const void* buffer, size_t bytes);
 
 /* The CUDA stream the engine launches on (cudaStream_t as void*). */
 int rewl_get_stream(rewl_engine* eng, void** stream);
+
+/* ------------------------------------------------------------------------
+ * Learned warm start (no reference counterpart: the reference always starts
+ * ln g at 0, src/REWL/rewl_histograms.hpp:42-50).  An MLP maps
+ * [E/N, 1/L, J, K, sigma_h, window lo/N, window hi/N] to ln g(E)/N; training
+ * and inference run on the GPU with BF16 tensor-core GEMMs (FP32 accumulate).
+ * ------------------------------------------------------------------------ */
+typedef struct rewl_mlp rewl_mlp;
+
+/* `layers` hidden layers of width `hidden` (multiple of 64), GELU; seeded init. */
+int rewl_mlp_create(int32_t device, int32_t hidden, int32_t layers, uint64_t seed, rewl_mlp** out);
+int rewl_mlp_destroy(rewl_mlp* mlp);
+const char* rewl_mlp_last_error_string(void);
+/* number of floats in the (padded) parameter vector */
+int rewl_mlp_num_params(const rewl_mlp* mlp, int64_t* count);
+/* per layer: input width, output width, weight offset, bias offset (padded layout) */
+int rewl_mlp_layout(const rewl_mlp* mlp, int64_t* rows_of_4, int32_t capacity_rows);
+/* fp32 master parameters (which = 0) or the last gradient (which = 1) */
+int rewl_mlp_get_params(rewl_mlp* mlp, int32_t which, float* out, int64_t count);
+int rewl_mlp_set_params(rewl_mlp* mlp, const float* in, int64_t count);
+/* y[i] = f(X[i, :in_dim]) for n rows */
+int rewl_mlp_predict(rewl_mlp* mlp, const float* X, int32_t n, int32_t in_dim, float* y);
+/* one forward + backward of the mean squared error on n rows (n a multiple of 64); no update */
+int rewl_mlp_gradient(rewl_mlp* mlp, const float* X, const float* y, int32_t n, int32_t in_dim, float* loss);
+/* load a training set into device memory */
+int rewl_mlp_set_data(rewl_mlp* mlp, const float* X, const float* y, int32_t n, int32_t in_dim);
+/* `steps` Adam steps on random batches of `batch` rows; per-step losses into `losses` (may be NULL) */
+int rewl_mlp_train(rewl_mlp* mlp, int32_t steps, int32_t batch, float lr, float* losses);
+/* kernels launched by this network so far */
+int rewl_mlp_launches(const rewl_mlp* mlp, int64_t* count);
 
 #ifdef __cplusplus
 }

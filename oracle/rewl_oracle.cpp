@@ -527,13 +527,24 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
                 start = (size_t)(((uint64_t)philox_word(c.seed, k.uid, 0, STREAM_ADJ) * k.sys.N) >> 32);
             else { start = (size_t)(k.U(k.gen) * (double)k.sys.N); ++k.draws; }
             const size_t cap = 4000 * nd;
-            if (!adjust(*S, k, start, cap))
-            {   // stuck in a local extremum: restart from the all +1 state and walk up
-                std::fill(k.sys.spin.begin(), k.sys.spin.end(), 1.0);
+            bool ok = adjust(*S, k, start, cap);
+            // stuck in a local extremum: restart from all +1 (walk up), then from
+            // the checkerboard (walk down)
+            for (int attempt = 1; attempt <= 2 && !ok; ++attempt)
+            {
+                const size_t N = k.sys.N, L = (size_t)c.L;
+                for (size_t i = 0; i < nd; ++i)
+                {
+                    const size_t site = (M::num_obs == 13) ? i / 2 : i;   // AT layout is interleaved
+                    const size_t x = site % L, y = site / L;
+                    k.sys.spin[i] = (attempt == 1 || ((x + y) & 1) == 0) ? 1.0 : -1.0;
+                }
+                (void)N;
                 k.sys.recalculate();
                 set_flavour(k.sys, 0);
-                if (!adjust(*S, k, start, cap)) { delete S; return nullptr; }
+                ok = adjust(*S, k, start, cap);
             }
+            if (!ok) { delete S; return nullptr; }
         }
     return S;
 }

@@ -16,7 +16,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 LIB = PKG / "librewl_gb300.so"
-SOURCES = [CSRC / "engine.cu"]
+SOURCES = [CSRC / "engine.cu", CSRC / "mlp.cu"]
 DEPS = SOURCES + [CSRC / "rng.cuh", INCLUDE / "rewl.h"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -29,17 +29,31 @@ def nvcc() -> str:
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile the engine into rewl_simulator_gb300/librewl_gb300.so."""
+    """Compile the engine into rewl_simulator_gb300/librewl_gb300.so.
+
+    Each translation unit is compiled concurrently, then linked.
+    """
     if LIB.exists() and not force:
         newest = max(p.stat().st_mtime for p in DEPS)
         if LIB.stat().st_mtime >= newest:
             return LIB
-    tmp = LIB.with_name(f".librewl_gb300.{os.getpid()}.so")
-    cmd = [nvcc(), *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-shared",
-           "-I", str(INCLUDE), *map(str, SOURCES), "-o", str(tmp)]
+    objdir = PKG / "_build"
+    objdir.mkdir(exist_ok=True)
+    common = [nvcc(), *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", str(INCLUDE)]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    subprocess.run(cmd, check=True)
+        common.append("-Xptxas=-v")
+    procs, objs = [], []
+    for src in SOURCES:
+        obj = objdir / f"{src.stem}.{os.getpid()}.o"
+        objs.append(obj)
+        procs.append(subprocess.Popen(common + ["-c", str(src), "-o", str(obj)]))
+    rcs = [p.wait() for p in procs]
+    if any(rcs):
+        raise RuntimeError(f"nvcc failed for {[str(s) for s, r in zip(SOURCES, rcs) if r]}")
+    tmp = LIB.with_name(f".librewl_gb300.{os.getpid()}.so")
+    subprocess.run([nvcc(), *ARCH_FLAGS, "-shared", *map(str, objs), "-o", str(tmp)], check=True)
+    for o in objs:
+        o.unlink()
     os.replace(tmp, LIB)
     return LIB
 
@@ -64,6 +78,7 @@ def load() -> C.CDLL:
 def _declare(L: C.CDLL) -> None:
     vp, i32, i64, u64, sz, dp = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_size_t, C.c_void_p
     L.rewl_last_error_string.restype = C.c_char_p
+    L.rewl_mlp_last_error_string.restype = C.c_char_p
     sigs = {
         "rewl_create": [vp, vp],
         "rewl_destroy": [vp],
@@ -91,6 +106,17 @@ def _declare(L: C.CDLL) -> None:
         "rewl_snapshot_size": [vp, vp],
         "rewl_snapshot": [vp, vp, sz],
         "rewl_restore": [vp, vp, sz],
+        "rewl_mlp_create": [i32, i32, i32, u64, vp],
+        "rewl_mlp_destroy": [vp],
+        "rewl_mlp_num_params": [vp, vp],
+        "rewl_mlp_layout": [vp, vp, i32],
+        "rewl_mlp_get_params": [vp, i32, vp, i64],
+        "rewl_mlp_set_params": [vp, vp, i64],
+        "rewl_mlp_predict": [vp, vp, i32, i32, vp],
+        "rewl_mlp_gradient": [vp, vp, vp, i32, i32, vp],
+        "rewl_mlp_set_data": [vp, vp, vp, i32, i32],
+        "rewl_mlp_train": [vp, i32, i32, C.c_float, vp],
+        "rewl_mlp_launches": [vp, vp],
     }
     for name, args in sigs.items():
         f = getattr(L, name)

@@ -245,14 +245,19 @@ __global__ void k_init(DevPtrs P, int nslots, int init_mode_mask_unused)
     const uint32_t start = mulhi32(philox_word(I.seed, uid, 0, kStreamAdjust), (uint32_t)I.N);
     const int64_t cap = 4000LL * I.ndof;
     bool ok = adjust_walk(I, W, sp, E, M, flavour, h, start, cap);
-    if (!ok) {
-        for (int i = 0; i < I.ndof; ++i) sp[i] = 1;
+    // a greedy walk can stick in a local extremum: retry from all +1 (walks up
+    // from the ground state) and then from the checkerboard (walks down from the top)
+    for (int attempt = 1; attempt <= 2 && !ok; ++attempt) {
+        for (int i = 0; i < I.ndof; ++i) {
+            const int site = i % I.N, x = site % I.L, y = site / I.L;
+            sp[i] = (attempt == 1 || ((x + y) & 1) == 0) ? 1 : -1;
+        }
         if (I.model == REWL_MODEL_ISING2D) ising_recalc(sp, I.L, I.J_u, E, M[0]);
         else at_recalc(sp, sp + I.N, I.L, I.J_u, I.K_u, h, E, M);
         flavour = 0;
         ok = adjust_walk(I, W, sp, E, M, flavour, h, start, cap);
-        if (!ok) atomicOr(&P.counters[0], ERR_ADJUST);
     }
+    if (!ok) atomicOr(&P.counters[0], ERR_ADJUST);
     P.cfg_E[c] = E;
     P.cfg_M[3 * c] = M[0]; P.cfg_M[3 * c + 1] = M[1]; P.cfg_M[3 * c + 2] = M[2];
     P.slot_flavour[s] = flavour;
@@ -506,6 +511,224 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
         if (REPLAY) P.slot_draws[s] = draws;
         if (err) atomicOr(&P.counters[0], err);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Bin-tracking Ising sweeps (used when every energy change is a whole number of
+// bins: 4|J| divisible by the bin width, as for J = 1 and width 4).  The chain
+// then carries only the bin index b and the logDoS value g[b].
+//
+// G walkers share a warp (P = 32/G lanes each); all lanes of a walker hold the
+// same chain state, so the warp's instructions advance G chains at once.  For
+// each chunk the walker's lanes first write one 16-byte record per site:
+// integer acceptance threshold, packed bin changes (without / with the left
+// neighbour flipped, wrap term for x = L-1) and the spin.  The accept chain then
+// runs "two worlds" ahead: while step j resolves, the proposal of step j+1 is
+// formed for both outcomes of step j, its logDoS entry loaded and its acceptance
+// evaluated, so the loop-carried dependency per step is one select; the shared
+// memory loads of consecutive steps overlap.  The only store that can land
+// between such a load and its use is step j's commit to the bin step j ends in,
+// which is exactly the world's own current bin: that case uses the value being
+// committed.
+// ---------------------------------------------------------------------------
+struct __align__(16) SiteRec {
+    long long T;    // accept iff d < T
+    int pk;         // bytes: bin change, same with left neighbour flipped, wrap term
+    int s;          // spin
+};
+
+__device__ __forceinline__ int sx8(int v) { return (int)(signed char)(v & 0xFF); }
+
+struct World {
+    int B;          // bin before the step
+    int BN;         // proposed bin
+    long long GC;   // logDoS at B (committed value)
+    long long GN;   // logDoS at BN
+    bool C;         // acceptance of the step in this world
+};
+
+template <int G, int C>
+__global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
+{
+    constexpr int P = 32 / G;
+    constexpr int SPL = (C + P - 1) / P;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int grp = lane / P, q = lane - grp * P;
+    const int li = (blockIdx.x * (blockDim.x >> 5) + wib) * G + grp;
+    const bool valid = li < p.nslots;
+    if (__ballot_sync(kFull, valid) == 0) return;             // whole warp without walkers
+    const DevPtrs& P_ = p.P;
+    const int s = p.slots[valid ? li : 0];                     // idle groups shadow a walker, never write
+    const InstDev I = P_.inst[P_.slot_inst[s]];
+    const int w = P_.slot_win[s];
+    const WinDev W = P_.win[w];
+    const int L = I.L, N = I.N, nb = W.nb;
+    unsigned char* base = smem + (size_t)(wib * G + grp) * p.smem_per_warp;
+    long long* gs = reinterpret_cast<long long*>(base);
+    SiteRec* rec = reinterpret_cast<SiteRec*>(gs + p.nbcap);
+    int8_t* lat = reinterpret_cast<int8_t*>(rec + 32);
+
+    const int cfg = P_.slot_cfg[s];
+    int8_t* gl = P_.spins + P_.cfg_off[cfg];
+    long long* gg = reinterpret_cast<long long*>(P_.g + P_.slot_tab[s]);
+    for (int i = q; i < N; i += P) lat[i] = gl[i];
+    for (int k = q; k < nb; k += P) gs[k] = gg[k];
+    __syncwarp();
+
+    const int J = (int)I.J_u;
+    const int sh = I.bin_shift;
+    const int Ewlo = (int)W.elo_u;
+    const long long lnf = P_.win_lnf[w];
+    const uint64_t sweeps0 = P_.slot_sweeps[s];
+    const uint32_t uid = (uint32_t)(s - I.first_slot);
+    const uint64_t seed = I.seed;
+
+    const int E0 = (int)P_.cfg_E[cfg];
+    int b = (E0 - Ewlo) >> sh;
+    const bool bad = ((E0 - Ewlo) & ((1 << sh) - 1)) != 0 || b < 0 || b >= nb;
+    if (__ballot_sync(kFull, valid && bad)) {
+        if (lane == 0) atomicOr(&P_.counters[0], ERR_BOUNDS);
+        return;
+    }
+    int M = P_.cfg_M[3 * cfg];
+    long long gc = gs[b];
+
+    for (int sw = 0; sw < p.nsweeps; ++sw) {
+        const uint64_t A0 = (sweeps0 + (uint64_t)sw) * (uint64_t)N;
+        for (int c0 = 0; c0 < N; c0 += C) {
+            const int y = c0 / L, x0 = c0 - y * L;
+            const int row = y * L;
+            const int up = (y == 0 ? L - 1 : y - 1) * L, down = (y == L - 1 ? 0 : y + 1) * L;
+            int my_s[SPL];
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int jj = q + k * P;
+                my_s[k] = 0;
+                if (jj < C) {
+                    const int x = x0 + jj;
+                    const int si = lat[row + x];
+                    const int left = lat[row + (x == 0 ? L - 1 : x - 1)];
+                    const int right = lat[row + (x == L - 1 ? 0 : x + 1)];
+                    const int sum = lat[up + x] + left + right + lat[down + x];
+                    const int d0 = 2 * J * si * sum;
+                    const int d1 = jj > 0 ? d0 - 4 * J * si * left : d0;
+                    const int wc = (C == L && jj == L - 1) ? -4 * J * si * right : 0;
+                    SiteRec r;
+                    r.pk = ((d0 >> sh) & 0xFF) | (((d1 >> sh) & 0xFF) << 8) | (((wc >> sh) & 0xFF) << 16);
+                    r.T = accept_threshold(neglog_u32(philox_word(seed, uid, A0 + (uint64_t)(c0 + jj), kStreamWL)));
+                    r.s = si;
+                    rec[jj] = r;
+                    my_s[k] = si;
+                }
+            }
+            __syncwarp();
+
+            // step 0 of the chunk: no earlier flip in the chunk can affect it
+            unsigned acc = 0;
+            World X;
+            {
+                const SiteRec r = rec[0];
+                X.B = b;
+                X.GC = gc;
+                X.BN = b + sx8(r.pk);
+                const bool in = (unsigned)X.BN < (unsigned)nb;
+                X.GN = gs[in ? X.BN : b];
+                X.C = in && (X.GN - X.GC < r.T);
+            }
+            World X1 = X;                        // both worlds coincide at step 0
+            bool pa = false;
+#pragma unroll
+            for (int j = 0; j < C; ++j) {
+                const bool a = pa ? X1.C : X.C;                 // outcome of step j
+                const World R = pa ? X1 : X;                     // real state of step j
+                World Y0, Y1;
+                if (j + 1 < C) {
+                    const SiteRec r = rec[j + 1];
+                    const int wrapb = sx8(r.pk >> 16);
+                    const int w0 = (j == 0) ? 0 : ((acc & 1u) ? wrapb : 0);
+                    const int w1 = (j == 0) ? wrapb : ((acc & 1u) ? wrapb : 0);
+                    // world a_j = 0: stays in R.B, left neighbour not flipped
+                    Y0.B = R.B;
+                    Y0.GC = R.GC + lnf;
+                    Y0.BN = R.B + sx8(r.pk) + w0;
+                    // world a_j = 1: moved to R.BN, left neighbour flipped
+                    Y1.B = R.BN;
+                    Y1.GC = R.GN + lnf;
+                    Y1.BN = R.BN + sx8(r.pk >> 8) + w1;
+                    const bool in0 = (unsigned)Y0.BN < (unsigned)nb;
+                    const bool in1 = (unsigned)Y1.BN < (unsigned)nb;
+                    const long long l0 = gs[in0 ? Y0.BN : 0];
+                    const long long l1 = gs[in1 ? Y1.BN : 0];
+                    Y0.GN = (Y0.BN == Y0.B) ? Y0.GC : l0;
+                    Y1.GN = (Y1.BN == Y1.B) ? Y1.GC : l1;
+                    Y0.C = in0 && (Y0.GN - Y0.GC < r.T);
+                    Y1.C = in1 && (Y1.GN - Y1.GC < r.T);
+                }
+                // commit step j
+                const int bj = a ? R.BN : R.B;
+                const long long gj = (a ? R.GN : R.GC) + lnf;
+                gs[bj] = gj;
+                if (a) acc |= 1u << j;
+                if (j + 1 < C) { X = Y0; X1 = Y1; pa = a; }
+                else { b = bj; gc = gj; }
+            }
+            // apply the chunk's flips and the magnetisation change
+            unsigned plus = 0;
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+                const int jj = q + k * P;
+                const unsigned bal = __ballot_sync(kFull, jj < C && my_s[k] > 0);
+                const unsigned mine = P == 32 ? bal : ((bal >> (grp * P)) & ((1u << P) - 1u));
+                plus |= (k * P < 32) ? (mine << (k * P)) : 0u;
+                if (jj < C && ((acc >> jj) & 1u)) lat[row + x0 + jj] = (int8_t)(-my_s[k]);
+            }
+            const unsigned full = C == 32 ? 0xFFFFFFFFu : ((1u << C) - 1u);
+            M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus & full));
+            __syncwarp();
+        }
+    }
+    if (valid) {
+        for (int i = q; i < N; i += P) gl[i] = lat[i];
+        uint32_t* gH = P_.H + P_.slot_tab[s];
+        uint64_t* gv = P_.visits + P_.slot_tab[s];
+        for (int k = q; k < nb; k += P) {
+            const long long gnew = gs[k];
+            const long long dv = (gnew - gg[k]) / lnf;
+            gH[k] += (uint32_t)dv;
+            gv[k] += (uint64_t)dv;
+            gg[k] = gnew;
+        }
+        if (q == 0) {
+            P_.cfg_E[cfg] = (long long)Ewlo + ((long long)b << sh);
+            P_.cfg_M[3 * cfg] = M;
+            P_.slot_sweeps[s] = sweeps0 + (uint64_t)p.nsweeps;
+        }
+    }
+}
+
+template <int G>
+void launch_bins(int C, dim3 grid, dim3 block, size_t smem, cudaStream_t st, const SweepParams& sp)
+{
+    switch (C) {
+    case 32: k_sweep_ising_bins<G, 32><<<grid, block, smem, st>>>(sp); break;
+    case 24: k_sweep_ising_bins<G, 24><<<grid, block, smem, st>>>(sp); break;
+    case 16: k_sweep_ising_bins<G, 16><<<grid, block, smem, st>>>(sp); break;
+    case 8: k_sweep_ising_bins<G, 8><<<grid, block, smem, st>>>(sp); break;
+    default: k_sweep_ising_bins<G, 4><<<grid, block, smem, st>>>(sp); break;
+    }
+}
+
+template <int G>
+cudaError_t allow_bins_smem()
+{
+    cudaError_t e = cudaSuccess;
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    return e;
 }
 
 // Ashkin-Teller: sweep = sigma pass then tau pass (wang_landau.hpp:109-119); the
@@ -902,9 +1125,12 @@ struct HostInst {
 struct Launch {
     int model;
     std::vector<int32_t> slots;
-    int smem_per_warp;
+    int smem_per_warp;      // per walker for the bin-tracking kernel, per warp otherwise
     int nbcap;
-    int wpb;
+    int wpb;                // warps per block
+    int bins = 0;           // Ising bin-tracking kernel with `walkers_per_warp` walkers per warp and chunk `chunk`
+    int walkers_per_warp = 1;
+    int chunk = 32;
     DBuf<int32_t> d_slots;
 };
 
@@ -1071,8 +1297,10 @@ int build_host(rewl_engine* e)
     if (D.flatness_mode < 0 || D.flatness_mode > 2) return fail(REWL_EINVAL, "bad flatness mode");
     if (D.mask_mode < 0 || D.mask_mode > 1) return fail(REWL_EINVAL, "bad mask mode");
     if (D.rng_mode != REWL_RNG_PHILOX && D.rng_mode != REWL_RNG_REPLAY) return fail(REWL_EINVAL, "bad rng mode");
-    if (D.walkers_per_block != 0 && D.walkers_per_block != 1 && D.walkers_per_block != 2 && D.walkers_per_block != 4 && D.walkers_per_block != 8)
-        return fail(REWL_EINVAL, "walkers_per_block must be 0, 1, 2, 4 or 8");
+    if (D.warps_per_block != 0 && D.warps_per_block != 1 && D.warps_per_block != 2 && D.warps_per_block != 4 && D.warps_per_block != 8)
+        return fail(REWL_EINVAL, "warps_per_block must be 0, 1, 2, 4 or 8");
+    if (D.walkers_per_warp != 0 && D.walkers_per_warp != 1 && D.walkers_per_warp != 2 && D.walkers_per_warp != 4)
+        return fail(REWL_EINVAL, "walkers_per_warp must be 0, 1, 2 or 4");
     int slot = 0, win = 0;
     int64_t tab = 0, spin = 0, maskoff = 0, fieldoff = 0;
     std::vector<int64_t> h_fields;
@@ -1226,40 +1454,76 @@ int upload_all(rewl_engine* e)
     return REWL_OK;
 }
 
+bool bins_eligible(const InstDev& I, const rewl_batch_desc& D)
+{
+    if (I.model != REWL_MODEL_ISING2D || D.rng_mode != REWL_RNG_PHILOX) return false;
+    const int C = I.chunk;
+    if (!(C == 32 || C == 24 || C == 16 || C == 8 || C == 4)) return false;
+    const long long step = 4 * std::llabs(I.J_u);            // every energy change is a multiple of 4|J|
+    if (step % (1LL << I.bin_shift) != 0) return false;
+    if (8 * std::llabs(I.J_u) >> I.bin_shift > 60) return false;   // bin changes fit a signed byte (with margin)
+    return true;
+}
+
 int plan_launches(rewl_engine* e)
 {
-    // one launch per model; shared memory sized for the largest walker of the launch
-    const int nsm_guess = 152;
-    for (int model = 0; model < 2; ++model) {
-        Launch l;
-        l.model = model;
+    const int nsm = 152;
+    // group walkers by (model, bin-tracking kernel, chunk) so each launch has one kernel shape
+    struct Key { int model, bins, chunk; };
+    std::vector<Key> keys;
+    std::vector<Launch> plans;
+    for (int s = 0; s < e->nslots; ++s) {
+        const HostInst& H = e->inst[e->h_slot_inst[s]];
+        const int bins = bins_eligible(H.dev, e->desc) && getenv("REWL_SWEEP_VARIANT") == nullptr ? 1 : 0;
+        Key k{H.d.model, bins, bins ? H.dev.chunk : 0};
+        size_t idx = 0;
+        for (; idx < keys.size(); ++idx)
+            if (keys[idx].model == k.model && keys[idx].bins == k.bins && keys[idx].chunk == k.chunk) break;
+        if (idx == keys.size()) {
+            keys.push_back(k);
+            Launch l;
+            l.model = k.model; l.bins = k.bins; l.chunk = k.chunk ? k.chunk : 32;
+            plans.push_back(std::move(l));
+        }
+        plans[idx].slots.push_back(s);
+    }
+    for (auto& l : plans) {
         int maxN = 0, maxnb = 0;
-        for (int s = 0; s < e->nslots; ++s) {
-            const HostInst& H = e->inst[e->h_slot_inst[s]];
-            if (H.d.model != model) continue;
-            l.slots.push_back(s);
-            maxN = std::max(maxN, H.dev.N);
+        for (int s : l.slots) {
+            maxN = std::max(maxN, e->inst[e->h_slot_inst[s]].dev.N);
             maxnb = std::max(maxnb, e->h_slot_nb[s]);
         }
-        if (l.slots.empty()) continue;
-        if (model == REWL_MODEL_ISING2D) {
+        const int n = (int)l.slots.size();
+        if (l.bins) {
+            int G = e->desc.walkers_per_warp;
+            if (G == 0) G = 4;                                     // shares the warp's issue slots among 4 chains
+            l.walkers_per_warp = G;
+            l.nbcap = (maxnb + 1) & ~1;
+            int raw = l.nbcap * 8 + 32 * (int)sizeof(SiteRec) + ((maxN + 15) & ~15);
+            l.smem_per_warp = ((raw + 127) & ~127) + 16;           // per walker; +16 skews the walkers' banks
+            if ((size_t)l.smem_per_warp * G > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory", l.smem_per_warp);
+            int wpb = e->desc.warps_per_block;
+            if (wpb == 0) {
+                const int warps = (n + G - 1) / G;
+                wpb = warps <= nsm * 2 ? 1 : warps <= nsm * 8 ? 2 : 4;
+            }
+            while (wpb > 1 && (size_t)wpb * G * l.smem_per_warp > 200 * 1024) wpb >>= 1;
+            l.wpb = wpb;
+        } else if (l.model == REWL_MODEL_ISING2D) {
             l.nbcap = (maxnb + 1) & ~1;
             l.smem_per_warp = (int)(l.nbcap * 8 + sizeof(Stage) + ((maxN + 15) & ~15));
         } else {
             l.nbcap = 0;
             l.smem_per_warp = (int)(sizeof(StageAT) + ((2 * maxN + 15) & ~15));
         }
-        l.smem_per_warp = (l.smem_per_warp + 15) & ~15;
-        int wpb = e->desc.walkers_per_block;
-        if (wpb == 0) {
-            // few walkers: one warp per block spreads them over the SMs;
-            // many walkers: pack warps to amortise the block's resources
-            const int n = (int)l.slots.size();
-            wpb = n <= nsm_guess * 2 ? 1 : n <= nsm_guess * 8 ? 2 : 4;
+        if (!l.bins) {
+            l.smem_per_warp = (l.smem_per_warp + 15) & ~15;
+            int wpb = e->desc.warps_per_block;
+            if (wpb == 0) wpb = n <= nsm * 2 ? 1 : n <= nsm * 8 ? 2 : 4;
+            while (wpb > 1 && (size_t)wpb * l.smem_per_warp > 200 * 1024) wpb >>= 1;
+            if ((size_t)l.smem_per_warp > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory (limit 220 KiB)", l.smem_per_warp);
+            l.wpb = wpb;
         }
-        while (wpb > 1 && (size_t)wpb * l.smem_per_warp > 200 * 1024) wpb >>= 1;
-        if ((size_t)l.smem_per_warp > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory (limit 220 KiB)", l.smem_per_warp);
-        l.wpb = wpb;
         int rc = upload(l.d_slots, l.slots, e->stream);
         if (rc) return rc;
         e->launches.push_back(std::move(l));
@@ -1269,6 +1533,9 @@ int plan_launches(rewl_engine* e)
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_at<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_at<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUDA_TRY(allow_bins_smem<1>());
+    CUDA_TRY(allow_bins_smem<2>());
+    CUDA_TRY(allow_bins_smem<4>());
     return REWL_OK;
 }
 
@@ -1302,6 +1569,19 @@ int launch_sweeps(rewl_engine* e, int nsweeps)
         SweepParams sp;
         sp.P = P; sp.slots = l.d_slots.p; sp.nslots = (int)l.slots.size(); sp.nsweeps = nsweeps;
         sp.smem_per_warp = l.smem_per_warp; sp.nbcap = l.nbcap;
+        if (l.bins) {
+            const int G = l.walkers_per_warp;
+            const int warps = (sp.nslots + G - 1) / G;
+            const int blocks = (warps + l.wpb - 1) / l.wpb;
+            const size_t smem = (size_t)l.wpb * G * l.smem_per_warp;
+            if (G == 1) launch_bins<1>(l.chunk, blocks, 32 * l.wpb, smem, e->stream, sp);
+            else if (G == 2) launch_bins<2>(l.chunk, blocks, 32 * l.wpb, smem, e->stream, sp);
+            else launch_bins<4>(l.chunk, blocks, 32 * l.wpb, smem, e->stream, sp);
+            CUDA_TRY(cudaGetLastError());
+            e->kernel_launches++;
+            e->launches_total++;
+            continue;
+        }
         const int blocks = (sp.nslots + l.wpb - 1) / l.wpb;
         const size_t smem = (size_t)l.wpb * l.smem_per_warp;
         if (l.model == REWL_MODEL_ISING2D) {

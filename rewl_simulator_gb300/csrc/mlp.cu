@@ -1,0 +1,607 @@
+// Learned warm start: an MLP surrogate ln g(E)/N = f(E/N, 1/L, J, K, sigma_h,
+// window lo/N, window hi/N), trained and evaluated on the GPU with hand-written
+// BF16 tensor-core GEMMs (mma.sync m16n8k16, FP32 accumulation), a fused
+// bias + GELU epilogue, split-K weight gradients, and Adam on FP32 master weights.
+//
+// Shapes: 7 inputs (padded to 64) -> 4 x 256 (GELU) -> 1 output (padded to 64).
+// A batch of 4096 is 4096 x 256 x 256 per hidden GEMM, i.e. latency-bound work.
+// The tiles are therefore small (64 x 64 x 32, four warps) so that a layer spans
+// ~256 blocks, and every GEMM of a step runs on one stream.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rewl.h"
+#include "rng.cuh"
+
+namespace {
+
+thread_local std::string g_mlp_error;
+
+int mfail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_mlp_error = buf;
+    return code;
+}
+
+#define MCUDA(expr)                                                                     \
+    do {                                                                                \
+        cudaError_t _e = (expr);                                                        \
+        if (_e != cudaSuccess)                                                          \
+            return mfail(REWL_EDEVICE, "%s: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                         __FILE__, __LINE__);                                           \
+    } while (0)
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int kBM = 64, kBN = 64, kBK = 32, kPad = 8;
+constexpr int kIn = 64;        // padded input width (a multiple of the 64-wide tile)
+constexpr int kOut = 64;       // padded output width
+
+// ---------------------------------------------------------------------------
+// GEMM: C[M x N] = op(A) * op(B) with bf16 operands, fp32 accumulation.
+//   A_KM = false: A stored [M][K] (lda = K);  true: A stored [K][M] (lda = M)
+//   B_NK = true:  B stored [N][K] (ldb = K);  false: B stored [K][N] (ldb = N)
+// M, N multiples of 64, K (per split) a multiple of 32.
+// Epilogues:
+//   EPI_F32:       C fp32 (atomicAdd when split over K)
+//   EPI_BIAS_GELU: Z = acc + bias -> Zout (fp32), Y = gelu(Z) -> Yout (bf16)
+//   EPI_BIAS_F32:  acc + bias -> fp32
+//   EPI_BF16:      acc -> bf16
+// ---------------------------------------------------------------------------
+enum { EPI_F32 = 0, EPI_BIAS_GELU = 1, EPI_BIAS_F32 = 2, EPI_BF16 = 3 };
+
+struct GemmArgs {
+    const bf16* A;
+    const bf16* B;
+    int M, N, K, lda, ldb;
+    int k_per_split;
+    float* Cf;
+    bf16* Cb;
+    int ldc;
+    const float* bias;
+};
+
+__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(a));
+}
+
+__device__ __forceinline__ void ldsm_x4_t(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(a));
+}
+
+__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                 "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+template <bool A_KM, bool B_NK, int EPI>
+__global__ void __launch_bounds__(128) k_gemm(const GemmArgs g)
+{
+    // shared tiles, rows padded by 8 bf16 (16 B) so ldmatrix rows hit distinct banks
+    constexpr int A_ROWS = A_KM ? kBK : kBM, A_COLS = A_KM ? kBM : kBK;
+    constexpr int B_ROWS = B_NK ? kBN : kBK, B_COLS = B_NK ? kBK : kBN;
+    __shared__ __align__(16) bf16 As[A_ROWS][A_COLS + kPad];
+    __shared__ __align__(16) bf16 Bs[B_ROWS][B_COLS + kPad];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;   // warp's 32 x 32 sub-tile
+    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+    const int kb = blockIdx.z * g.k_per_split, ke = kb + g.k_per_split;
+
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+
+    for (int k0 = kb; k0 < ke; k0 += kBK) {
+        // global -> shared, 16-byte chunks: each tile is 64 x 32 bf16 = 256 chunks
+        for (int c = tid; c < 256; c += 128) {
+            if (!A_KM) {
+                const int r = c >> 2, q = (c & 3) * 8;      // [64 m][32 k]
+                *reinterpret_cast<uint4*>(&As[r][q]) = *reinterpret_cast<const uint4*>(g.A + (size_t)(m0 + r) * g.lda + k0 + q);
+            } else {
+                const int r = c >> 3, q = (c & 7) * 8;      // [32 k][64 m]
+                *reinterpret_cast<uint4*>(&As[r][q]) = *reinterpret_cast<const uint4*>(g.A + (size_t)(k0 + r) * g.lda + m0 + q);
+            }
+            if (B_NK) {
+                const int r = c >> 2, q = (c & 3) * 8;      // [64 n][32 k]
+                *reinterpret_cast<uint4*>(&Bs[r][q]) = *reinterpret_cast<const uint4*>(g.B + (size_t)(n0 + r) * g.ldb + k0 + q);
+            } else {
+                const int r = c >> 3, q = (c & 7) * 8;      // [32 k][64 n]
+                *reinterpret_cast<uint4*>(&Bs[r][q]) = *reinterpret_cast<const uint4*>(g.B + (size_t)(k0 + r) * g.ldb + n0 + q);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kBK; kk += 16) {
+            uint32_t a[2][4], b[4][2];
+            const int mat = lane >> 3, rin = lane & 7;
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int mb = wm + i * 16;
+                if (!A_KM) ldsm_x4(a[i][0], a[i][1], a[i][2], a[i][3], &As[mb + (mat & 1) * 8 + rin][kk + (mat >> 1) * 8]);
+                else ldsm_x4_t(a[i][0], a[i][1], a[i][2], a[i][3], &As[kk + (mat >> 1) * 8 + rin][mb + (mat & 1) * 8]);
+            }
+#pragma unroll
+            for (int jp = 0; jp < 2; ++jp) {
+                const int nb = wn + jp * 16;
+                if (B_NK) ldsm_x4(b[2 * jp][0], b[2 * jp][1], b[2 * jp + 1][0], b[2 * jp + 1][1],
+                                  &Bs[nb + (mat >> 1) * 8 + rin][kk + (mat & 1) * 8]);
+                else ldsm_x4_t(b[2 * jp][0], b[2 * jp][1], b[2 * jp + 1][0], b[2 * jp + 1][1],
+                               &Bs[kk + (mat & 1) * 8 + rin][nb + (mat >> 1) * 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], a[i][0], a[i][1], a[i][2], a[i][3], b[j][0], b[j][1]);
+        }
+        __syncthreads();
+    }
+    // epilogue: thread owns rows (lane>>2) and +8, columns 2*(lane&3) + {0,1} of each 16 x 8 tile
+    const int gr = lane >> 2, tc = (lane & 3) * 2;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int row = m0 + wm + i * 16 + gr + h * 8;
+                const int col = n0 + wn + j * 8 + tc;
+                float v0 = acc[i][j][2 * h], v1 = acc[i][j][2 * h + 1];
+                const size_t o = (size_t)row * g.ldc + col;
+                if (EPI == EPI_F32) {
+                    if (gridDim.z > 1) { atomicAdd(g.Cf + o, v0); atomicAdd(g.Cf + o + 1, v1); }
+                    else { g.Cf[o] = v0; g.Cf[o + 1] = v1; }
+                } else if (EPI == EPI_BIAS_GELU) {
+                    v0 += g.bias[col]; v1 += g.bias[col + 1];
+                    g.Cf[o] = v0; g.Cf[o + 1] = v1;
+                    *reinterpret_cast<__nv_bfloat162*>(g.Cb + o) = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
+                } else if (EPI == EPI_BIAS_F32) {
+                    g.Cf[o] = v0 + g.bias[col]; g.Cf[o + 1] = v1 + g.bias[col + 1];
+                } else {
+                    *reinterpret_cast<__nv_bfloat162*>(g.Cb + o) = __floats2bfloat162_rn(v0, v1);
+                }
+            }
+}
+
+// G = dY * gelu'(Z) (bf16), dY given in bf16
+__global__ void k_gelu_back(const bf16* dY, const float* Z, bf16* G, size_t n)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float z = Z[i];
+    const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
+    const float pdf = 0.3989422804014327f * __expf(-0.5f * z * z);
+    G[i] = __float2bfloat16_rn(__bfloat162float(dY[i]) * (cdf + z * pdf));
+}
+
+// column sums over the batch: db[n] += sum_b G[b][n]
+__global__ void k_colsum(const bf16* G, int B, int N, float* db)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b0 = blockIdx.y * 256;
+    if (n >= N) return;
+    float s = 0.f;
+    for (int b = b0; b < b0 + 256 && b < B; ++b) s += __bfloat162float(G[(size_t)b * N + n]);
+    atomicAdd(db + n, s);
+}
+
+// loss gradient of 0.5 * mean((out[:,0] - y)^2) * 2 = mean squared error
+__global__ void k_loss_grad(const float* out, const float* y, int B, bf16* dOut, float* loss)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const float e = out[(size_t)b * kOut] - y[b];
+    for (int c = 0; c < kOut; ++c) dOut[(size_t)b * kOut + c] = __float2bfloat16_rn(c == 0 ? 2.0f * e / (float)B : 0.f);
+    atomicAdd(loss, e * e / (float)B);
+}
+
+// Adam on fp32 masters; refresh the bf16 copy.  mask zeroes the padded entries.
+__global__ void k_adam(float* p, float* m, float* v, const float* grad, const float* mask, bf16* pb, size_t n,
+                       float lr, float b1, float b2, float eps, float c1, float c2)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = grad[i] * mask[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi; v[i] = vi;
+    const float pi = (p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps)) * mask[i];
+    p[i] = pi;
+    if (pb) pb[i] = __float2bfloat16_rn(pi);
+}
+
+// batch gather with Philox indices: Xb = X[idx], yb = y[idx]
+__global__ void k_gather(const bf16* X, const float* y, int n, bf16* Xb, float* yb, int B, uint64_t seed, uint64_t step)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const uint32_t w = rewl::philox_word(seed, 0x4D4C5000u, step * (uint64_t)B + (uint64_t)b, 0x4D4C5001u);
+    const int i = (int)rewl::mulhi32(w, (uint32_t)n);
+    for (int c = 0; c < kIn; c += 8)
+        *reinterpret_cast<uint4*>(Xb + (size_t)b * kIn + c) = *reinterpret_cast<const uint4*>(X + (size_t)i * kIn + c);
+    yb[b] = y[i];
+}
+
+template <typename T>
+struct Buf {
+    T* p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        n = count;
+        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) return mfail(REWL_ENOMEM, "cudaMalloc failed");
+        return cudaMemset(p, 0, count * sizeof(T)) == cudaSuccess ? REWL_OK : mfail(REWL_EDEVICE, "cudaMemset failed");
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+};
+
+} // namespace
+
+struct rewl_mlp {
+    int device = 0;
+    int hidden = 256, layers = 4;
+    int batch_cap = 0;
+    cudaStream_t stream = nullptr;
+    // layer l: weight [out_l x in_l] row-major, bias [out_l]; in_0 = 32, out_last = 64
+    std::vector<int> din, dout;
+    std::vector<size_t> woff, boff;
+    size_t nparams = 0;
+    Buf<float> P, Mm, Vm, Gr, Mask;   // fp32 master params, Adam moments, grads, pad mask
+    Buf<bf16> Pb;                     // bf16 params (weights used by the GEMMs)
+    // activations for the current batch
+    std::vector<Buf<bf16>> H;         // H[0] = input (B x 32), H[l+1] = gelu(Z_l)
+    std::vector<Buf<float>> Z;        // pre-activations (hidden layers)
+    Buf<float> out, yb, loss;
+    Buf<bf16> dOut, dH, G;
+    Buf<bf16> Xall;
+    Buf<float> yall;
+    int nall = 0;
+    int64_t step = 0;
+    uint64_t seed = 1;
+    int64_t launches = 0;
+
+    void release()
+    {
+        P.release(); Mm.release(); Vm.release(); Gr.release(); Mask.release(); Pb.release();
+        for (auto& h : H) h.release();
+        for (auto& z : Z) z.release();
+        out.release(); yb.release(); loss.release(); dOut.release(); dH.release(); G.release();
+        Xall.release(); yall.release();
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+namespace {
+
+int ensure_batch(rewl_mlp* m, int B)
+{
+    if (B <= m->batch_cap) return REWL_OK;
+    for (auto& h : m->H) h.release();
+    for (auto& z : m->Z) z.release();
+    m->out.release(); m->yb.release(); m->dOut.release(); m->dH.release(); m->G.release();
+    m->H.assign(m->layers + 1, Buf<bf16>());
+    m->Z.assign(m->layers, Buf<float>());
+    int rc;
+    if ((rc = m->H[0].alloc((size_t)B * kIn))) return rc;
+    for (int l = 0; l < m->layers; ++l) {
+        if ((rc = m->H[l + 1].alloc((size_t)B * m->hidden))) return rc;
+        if ((rc = m->Z[l].alloc((size_t)B * m->hidden))) return rc;
+    }
+    if ((rc = m->out.alloc((size_t)B * kOut)) || (rc = m->yb.alloc(B)) || (rc = m->dOut.alloc((size_t)B * kOut)) ||
+        (rc = m->dH.alloc((size_t)B * m->hidden)) || (rc = m->G.alloc((size_t)B * m->hidden)))
+        return rc;
+    m->batch_cap = B;
+    return REWL_OK;
+}
+
+template <bool A_KM, bool B_NK, int EPI>
+int gemm(rewl_mlp* m, const bf16* A, const bf16* B, int M, int N, int K, int lda, int ldb, int splits, float* Cf,
+         bf16* Cb, int ldc, const float* bias)
+{
+    if (M % kBM || N % kBN || K % (kBK * splits)) return mfail(REWL_EINVAL, "gemm shape %d x %d x %d (split %d)", M, N, K, splits);
+    GemmArgs g{A, B, M, N, K, lda, ldb, K / splits, Cf, Cb, ldc, bias};
+    dim3 grid(N / kBN, M / kBM, splits);
+    k_gemm<A_KM, B_NK, EPI><<<grid, 128, 0, m->stream>>>(g);
+    m->launches++;
+    MCUDA(cudaGetLastError());
+    return REWL_OK;
+}
+
+// forward for B rows already in H[0]; leaves outputs in m->out
+int forward(rewl_mlp* m, int B)
+{
+    int rc;
+    for (int l = 0; l < m->layers; ++l) {
+        const bf16* W = m->Pb.p + m->woff[l];
+        const float* bias = m->P.p + m->boff[l];
+        if ((rc = gemm<false, true, EPI_BIAS_GELU>(m, m->H[l].p, W, B, m->dout[l], m->din[l], m->din[l], m->din[l], 1,
+                                                   m->Z[l].p, m->H[l + 1].p, m->dout[l], bias)))
+            return rc;
+    }
+    const int L = m->layers;
+    return gemm<false, true, EPI_BIAS_F32>(m, m->H[L].p, m->Pb.p + m->woff[L], B, kOut, m->hidden, m->hidden, m->hidden,
+                                           1, m->out.p, nullptr, kOut, m->P.p + m->boff[L]);
+}
+
+// backward of the mean squared error on m->yb; gradients accumulate into Gr (zeroed here)
+int backward(rewl_mlp* m, int B)
+{
+    MCUDA(cudaMemsetAsync(m->Gr.p, 0, m->nparams * sizeof(float), m->stream));
+    MCUDA(cudaMemsetAsync(m->loss.p, 0, sizeof(float), m->stream));
+    k_loss_grad<<<(B + 127) / 128, 128, 0, m->stream>>>(m->out.p, m->yb.p, B, m->dOut.p, m->loss.p);
+    m->launches++;
+    const int L = m->layers;
+    const int splits = B >= 4096 ? 16 : (B >= 1024 ? 4 : 1);
+    int rc;
+    // output layer: dW = dOut^T H_L, db = colsum(dOut), dH = dOut W
+    if ((rc = gemm<true, false, EPI_F32>(m, m->dOut.p, m->H[L].p, kOut, m->hidden, B, kOut, m->hidden, splits,
+                                         m->Gr.p + m->woff[L], nullptr, m->hidden, nullptr)))
+        return rc;
+    k_colsum<<<dim3((kOut + 127) / 128, (B + 255) / 256), 128, 0, m->stream>>>(m->dOut.p, B, kOut, m->Gr.p + m->boff[L]);
+    m->launches++;
+    if ((rc = gemm<false, false, EPI_BF16>(m, m->dOut.p, m->Pb.p + m->woff[L], B, m->hidden, kOut, kOut, m->hidden, 1,
+                                           nullptr, m->dH.p, m->hidden, nullptr)))
+        return rc;
+    for (int l = L - 1; l >= 0; --l) {
+        const size_t n = (size_t)B * m->hidden;
+        k_gelu_back<<<(unsigned)((n + 255) / 256), 256, 0, m->stream>>>(m->dH.p, m->Z[l].p, m->G.p, n);
+        m->launches++;
+        if ((rc = gemm<true, false, EPI_F32>(m, m->G.p, m->H[l].p, m->dout[l], m->din[l], B, m->dout[l], m->din[l],
+                                             splits, m->Gr.p + m->woff[l], nullptr, m->din[l], nullptr)))
+            return rc;
+        k_colsum<<<dim3((m->dout[l] + 127) / 128, (B + 255) / 256), 128, 0, m->stream>>>(m->G.p, B, m->dout[l],
+                                                                                          m->Gr.p + m->boff[l]);
+        m->launches++;
+        if (l > 0)
+            if ((rc = gemm<false, false, EPI_BF16>(m, m->G.p, m->Pb.p + m->woff[l], B, m->din[l], m->dout[l], m->dout[l],
+                                                   m->din[l], 1, nullptr, m->dH.p, m->din[l], nullptr)))
+                return rc;
+    }
+    return REWL_OK;
+}
+
+uint64_t splitmix(uint64_t& s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+int upload_features(rewl_mlp* m, const float* X, int n, int in_dim, bf16* dst)
+{
+    std::vector<bf16> h((size_t)n * kIn, __float2bfloat16(0.f));
+    for (int i = 0; i < n; ++i)
+        for (int c = 0; c < in_dim; ++c) h[(size_t)i * kIn + c] = __float2bfloat16(X[(size_t)i * in_dim + c]);
+    MCUDA(cudaMemcpyAsync(dst, h.data(), h.size() * sizeof(bf16), cudaMemcpyHostToDevice, m->stream));
+    MCUDA(cudaStreamSynchronize(m->stream));
+    return REWL_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char* rewl_mlp_last_error_string(void) { return g_mlp_error.c_str(); }
+
+int rewl_mlp_create(int32_t device, int32_t hidden, int32_t layers, uint64_t seed, rewl_mlp** out)
+{
+    if (!out || hidden <= 0 || hidden % 64 || layers < 1 || layers > 16) return mfail(REWL_EINVAL, "hidden must be a positive multiple of 64, layers in 1..16");
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return mfail(REWL_EDEVICE, "cannot open device %d", device);
+    rewl_mlp* m = new rewl_mlp();
+    m->device = device; m->hidden = hidden; m->layers = layers; m->seed = seed;
+    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) { delete m; return mfail(REWL_EDEVICE, "stream"); }
+    for (int l = 0; l <= layers; ++l) {
+        m->din.push_back(l == 0 ? kIn : hidden);
+        m->dout.push_back(l == layers ? kOut : hidden);
+    }
+    size_t off = 0;
+    for (int l = 0; l <= layers; ++l) {
+        m->woff.push_back(off); off += (size_t)m->dout[l] * m->din[l];
+        m->boff.push_back(off); off += (size_t)m->dout[l];
+        off = (off + 7) & ~size_t(7);               // keep every weight block 16-byte aligned in bf16
+    }
+    m->nparams = off;
+    int rc;
+    if ((rc = m->P.alloc(off)) || (rc = m->Mm.alloc(off)) || (rc = m->Vm.alloc(off)) || (rc = m->Gr.alloc(off)) ||
+        (rc = m->Mask.alloc(off)) || (rc = m->Pb.alloc(off)) || (rc = m->loss.alloc(1))) {
+        m->release(); delete m; return rc;
+    }
+    // PyTorch-style uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) init over the real (unpadded) entries
+    std::vector<float> p(off, 0.f), mask(off, 0.f);
+    uint64_t s = seed;
+    for (int l = 0; l <= layers; ++l) {
+        const int fan_in = l == 0 ? 7 : hidden;
+        const int real_in = l == 0 ? 7 : hidden;
+        const int real_out = l == layers ? 1 : hidden;
+        const float bound = 1.0f / std::sqrt((float)fan_in);
+        for (int o = 0; o < m->dout[l]; ++o)
+            for (int i = 0; i < m->din[l]; ++i) {
+                const bool real = o < real_out && i < real_in;
+                const size_t k = m->woff[l] + (size_t)o * m->din[l] + i;
+                mask[k] = real ? 1.f : 0.f;
+                p[k] = real ? bound * (2.0f * (float)((splitmix(s) >> 11) * (1.0 / 9007199254740992.0)) - 1.0f) : 0.f;
+            }
+        for (int o = 0; o < m->dout[l]; ++o) {
+            const size_t k = m->boff[l] + o;
+            const bool real = o < real_out;
+            mask[k] = real ? 1.f : 0.f;
+            p[k] = real ? bound * (2.0f * (float)((splitmix(s) >> 11) * (1.0 / 9007199254740992.0)) - 1.0f) : 0.f;
+        }
+    }
+    std::vector<bf16> pb(off);
+    for (size_t k = 0; k < off; ++k) pb[k] = __float2bfloat16(p[k]);
+    if (cudaMemcpy(m->P.p, p.data(), off * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(m->Mask.p, mask.data(), off * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(m->Pb.p, pb.data(), off * 2, cudaMemcpyHostToDevice) != cudaSuccess) {
+        m->release(); delete m; return mfail(REWL_EDEVICE, "parameter upload failed");
+    }
+    *out = m;
+    return REWL_OK;
+}
+
+int rewl_mlp_destroy(rewl_mlp* m)
+{
+    if (!m) return REWL_OK;
+    cudaSetDevice(m->device);
+    m->release();
+    delete m;
+    return REWL_OK;
+}
+
+int rewl_mlp_num_params(const rewl_mlp* m, int64_t* n)
+{
+    if (!m || !n) return mfail(REWL_EINVAL, "null argument");
+    *n = (int64_t)m->nparams;
+    return REWL_OK;
+}
+
+// parameter vector in the engine's padded layout (fp32 masters); `which` 0 = params, 1 = grads
+int rewl_mlp_get_params(rewl_mlp* m, int32_t which, float* out, int64_t n)
+{
+    if (!m || !out || n < (int64_t)m->nparams) return mfail(REWL_EINVAL, "bad arguments");
+    cudaSetDevice(m->device);
+    MCUDA(cudaStreamSynchronize(m->stream));
+    MCUDA(cudaMemcpy(out, which ? m->Gr.p : m->P.p, m->nparams * 4, cudaMemcpyDeviceToHost));
+    return REWL_OK;
+}
+
+int rewl_mlp_set_params(rewl_mlp* m, const float* in, int64_t n)
+{
+    if (!m || !in || n < (int64_t)m->nparams) return mfail(REWL_EINVAL, "bad arguments");
+    cudaSetDevice(m->device);
+    std::vector<bf16> pb(m->nparams);
+    for (size_t k = 0; k < m->nparams; ++k) pb[k] = __float2bfloat16(in[k]);
+    MCUDA(cudaMemcpy(m->P.p, in, m->nparams * 4, cudaMemcpyHostToDevice));
+    MCUDA(cudaMemcpy(m->Pb.p, pb.data(), m->nparams * 2, cudaMemcpyHostToDevice));
+    return REWL_OK;
+}
+
+// layer geometry: din, dout, weight offset, bias offset per layer (layers + 1 rows of 4)
+int rewl_mlp_layout(const rewl_mlp* m, int64_t* out, int32_t cap_rows)
+{
+    if (!m || !out || cap_rows < m->layers + 1) return mfail(REWL_EINVAL, "bad arguments");
+    for (int l = 0; l <= m->layers; ++l) {
+        out[4 * l] = m->din[l]; out[4 * l + 1] = m->dout[l];
+        out[4 * l + 2] = (int64_t)m->woff[l]; out[4 * l + 3] = (int64_t)m->boff[l];
+    }
+    return REWL_OK;
+}
+
+int rewl_mlp_predict(rewl_mlp* m, const float* X, int32_t n, int32_t in_dim, float* y)
+{
+    if (!m || !X || !y || n < 1 || in_dim < 1 || in_dim > kIn) return mfail(REWL_EINVAL, "bad arguments");
+    cudaSetDevice(m->device);
+    const int Bp = (n + kBM - 1) / kBM * kBM;
+    int rc = ensure_batch(m, Bp);
+    if (rc) return rc;
+    MCUDA(cudaMemsetAsync(m->H[0].p, 0, (size_t)Bp * kIn * sizeof(bf16), m->stream));
+    if ((rc = upload_features(m, X, n, in_dim, m->H[0].p))) return rc;
+    if ((rc = forward(m, Bp))) return rc;
+    std::vector<float> o((size_t)Bp * kOut);
+    MCUDA(cudaMemcpyAsync(o.data(), m->out.p, o.size() * 4, cudaMemcpyDeviceToHost, m->stream));
+    MCUDA(cudaStreamSynchronize(m->stream));
+    for (int i = 0; i < n; ++i) y[i] = o[(size_t)i * kOut];
+    return REWL_OK;
+}
+
+// One forward + backward on the given rows (no update); gradients readable with
+// rewl_mlp_get_params(which = 1); returns the loss.
+int rewl_mlp_gradient(rewl_mlp* m, const float* X, const float* y, int32_t n, int32_t in_dim, float* loss)
+{
+    if (!m || !X || !y || n < 1 || n % kBM || in_dim < 1 || in_dim > kIn) return mfail(REWL_EINVAL, "n must be a multiple of 64");
+    cudaSetDevice(m->device);
+    int rc = ensure_batch(m, n);
+    if (rc) return rc;
+    if ((rc = upload_features(m, X, n, in_dim, m->H[0].p))) return rc;
+    MCUDA(cudaMemcpyAsync(m->yb.p, y, (size_t)n * 4, cudaMemcpyHostToDevice, m->stream));
+    if ((rc = forward(m, n)) || (rc = backward(m, n))) return rc;
+    MCUDA(cudaMemcpyAsync(loss, m->loss.p, 4, cudaMemcpyDeviceToHost, m->stream));
+    MCUDA(cudaStreamSynchronize(m->stream));
+    return REWL_OK;
+}
+
+// Load a training set (features n x in_dim, targets n) into device memory.
+int rewl_mlp_set_data(rewl_mlp* m, const float* X, const float* y, int32_t n, int32_t in_dim)
+{
+    if (!m || !X || !y || n < 1 || in_dim < 1 || in_dim > kIn) return mfail(REWL_EINVAL, "bad arguments");
+    cudaSetDevice(m->device);
+    m->Xall.release(); m->yall.release();
+    int rc;
+    if ((rc = m->Xall.alloc((size_t)n * kIn)) || (rc = m->yall.alloc(n))) return rc;
+    if ((rc = upload_features(m, X, n, in_dim, m->Xall.p))) return rc;
+    MCUDA(cudaMemcpy(m->yall.p, y, (size_t)n * 4, cudaMemcpyHostToDevice));
+    m->nall = n;
+    return REWL_OK;
+}
+
+// `steps` Adam steps on batches of `batch` rows drawn (Philox) from the loaded set.
+// losses (may be NULL) receives the loss of every step.
+int rewl_mlp_train(rewl_mlp* m, int32_t steps, int32_t batch, float lr, float* losses)
+{
+    if (!m || steps < 0 || batch < 64 || batch % kBM || !(lr > 0)) return mfail(REWL_EINVAL, "bad arguments");
+    if (m->nall < 1) return mfail(REWL_ESTATE, "no training data (rewl_mlp_set_data)");
+    cudaSetDevice(m->device);
+    int rc = ensure_batch(m, batch);
+    if (rc) return rc;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    std::vector<float> lh(steps);
+    for (int s = 0; s < steps; ++s) {
+        k_gather<<<(batch + 127) / 128, 128, 0, m->stream>>>(m->Xall.p, m->yall.p, m->nall, m->H[0].p, m->yb.p, batch,
+                                                             m->seed, (uint64_t)m->step);
+        m->launches++;
+        if ((rc = forward(m, batch)) || (rc = backward(m, batch))) return rc;
+        m->step++;
+        const float c1 = 1.f - std::pow(b1, (float)m->step), c2 = 1.f - std::pow(b2, (float)m->step);
+        k_adam<<<(unsigned)((m->nparams + 255) / 256), 256, 0, m->stream>>>(m->P.p, m->Mm.p, m->Vm.p, m->Gr.p, m->Mask.p,
+                                                                            m->Pb.p, m->nparams, lr, b1, b2, eps, c1, c2);
+        m->launches++;
+        MCUDA(cudaGetLastError());
+        if (losses) MCUDA(cudaMemcpyAsync(&lh[s], m->loss.p, 4, cudaMemcpyDeviceToHost, m->stream));
+    }
+    MCUDA(cudaStreamSynchronize(m->stream));
+    if (losses) std::memcpy(losses, lh.data(), lh.size() * 4);
+    return REWL_OK;
+}
+
+int rewl_mlp_launches(const rewl_mlp* m, int64_t* n)
+{
+    if (!m || !n) return mfail(REWL_EINVAL, "null argument");
+    *n = m->launches;
+    return REWL_OK;
+}
+
+} // extern "C"

@@ -53,7 +53,8 @@ class _BatchDesc(C.Structure):
                 ("sweeps_per_check", C.c_int32), ("flatness_mode", C.c_int32), ("flatness_param", C.c_double),
                 ("lnf_initial", C.c_double), ("lnf_final", C.c_double), ("mask_mode", C.c_int32),
                 ("one_over_t", C.c_int32), ("reduce_logdos", C.c_int32), ("rng_mode", C.c_int32),
-                ("device", C.c_int32), ("walkers_per_block", C.c_int32), ("instances", C.c_void_p)]
+                ("device", C.c_int32), ("warps_per_block", C.c_int32), ("walkers_per_warp", C.c_int32),
+                ("reserved", C.c_int32), ("instances", C.c_void_p)]
 
 
 class _Status(C.Structure):
@@ -104,7 +105,8 @@ class Batch:
     reduce_logdos: int = 1
     rng_mode: int = RNG_PHILOX
     device: int = 0
-    walkers_per_block: int = 0
+    warps_per_block: int = 0
+    walkers_per_warp: int = 0
 
 
 @dataclass
@@ -153,7 +155,7 @@ class Engine:
         b.num_instances = n
         for name in ("sweeps_per_exchange", "sweeps_per_check", "flatness_mode", "flatness_param", "lnf_initial",
                      "lnf_final", "mask_mode", "one_over_t", "reduce_logdos", "rng_mode", "device",
-                     "walkers_per_block"):
+                     "warps_per_block", "walkers_per_warp"):
             setattr(b, name, getattr(batch, name))
         b.instances = C.cast(self._inst, C.c_void_p)
         self._desc = b

@@ -32,7 +32,7 @@ def _create(engine_lib, **overrides):
                num_windows=2, replicas_per_window=2, window_overlap=0.75, init_mode=0, seed=1)
     bat = dict(sweeps_per_exchange=10, sweeps_per_check=20, flatness_mode=0, flatness_param=0.8,
                lnf_initial=1.0, lnf_final=1e-6, mask_mode=0, one_over_t=0, reduce_logdos=1, rng_mode=0,
-               device=0, walkers_per_block=0)
+               device=0, warps_per_block=0, walkers_per_warp=0)
     for k, v in overrides.items():
         (ins if k in ins else bat)[k] = v
     lib = engine_lib.load_library()
@@ -58,7 +58,7 @@ BAD = [
     dict(L=1), dict(L=200), dict(model=7), dict(num_windows=0), dict(replicas_per_window=33),
     dict(window_overlap=1.0), dict(bin_width=3.0), dict(J=0.5), dict(energy_max=-200.0),
     dict(sweeps_per_check=15), dict(sweeps_per_exchange=0), dict(lnf_initial=0.0), dict(flatness_mode=5),
-    dict(mask_mode=3), dict(rng_mode=9), dict(walkers_per_block=3), dict(init_mode=2),
+    dict(mask_mode=3), dict(rng_mode=9), dict(warps_per_block=3), dict(walkers_per_warp=3), dict(init_mode=2),
     dict(num_windows=40, window_overlap=0.0, energy_min=-128.0, energy_max=-120.0),
 ]
 

@@ -55,12 +55,13 @@ def test_replay_matches_reference(engine_lib, oracle_lib, name):
 
 
 def _pair(rg, po, model, L, emin, emax, bw, nwin, R, se, sc, seed, K=0.5, fields=None, flat=0.8,
-          mask=0, lnf0=1.0, overlap=0.75, flat_mode=0):
+          mask=0, lnf0=1.0, overlap=0.75, flat_mode=0, walkers_per_warp=0):
     ins = rg.Instance(model=model, L=L, J=1.0, K=K if model else 0.0, fields=fields, energy_min=emin,
                       energy_max=emax, bin_width=bw, num_windows=nwin, replicas_per_window=R,
                       window_overlap=overlap, init_mode=0, seed=seed)
     b = rg.Batch(instances=[ins], sweeps_per_exchange=se, sweeps_per_check=sc, flatness_mode=flat_mode,
-                 flatness_param=flat, lnf_initial=lnf0, lnf_final=1e-7, mask_mode=mask)
+                 flatness_param=flat, lnf_initial=lnf0, lnf_final=1e-7, mask_mode=mask,
+                 walkers_per_warp=walkers_per_warp)
     eng = rg.Engine(b)
     cfg = po.Config(model=model, L=L, K=K, escale_bits=0 if model == 0 else 20, nwin=nwin, R=R,
                     sweeps_per_exchange=se, sweeps_per_check=sc, emin=emin, emax=emax, bw=bw, overlap=overlap,
@@ -88,6 +89,8 @@ def _compare(eng, orc, tag):
 CASES = [
     # model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles
     ("ising_L8_3x2", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 6),
+    ("ising_L16_4x3", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 5),
+    ("ising_L32_64w_top", 0, 32, -2048.0, 2052.0, 4.0, 64, 1, 4, 8, 23, 2),
     ("ising_L6_2x3", 0, 6, -72.0, 76.0, 4.0, 2, 3, 20, 40, 5, 8),
     ("ising_L12_4x2_bw8", 0, 12, -288.0, 296.0, 8.0, 4, 2, 10, 20, 3, 5),
     ("ising_L40_3x2", 0, 40, -3200.0, -2000.0, 4.0, 3, 2, 4, 8, 9, 3),
@@ -96,10 +99,12 @@ CASES = [
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("walkers_per_warp", [0, 1, 2, 4])
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
-def test_engine_matches_oracle_ising(engine_lib, oracle_lib, case):
+def test_engine_matches_oracle_ising(engine_lib, oracle_lib, case, walkers_per_warp):
     _, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles = case
-    eng, orc = _pair(engine_lib, oracle_lib, model, L, emin, emax, bw, nwin, R, se, sc, seed)
+    eng, orc = _pair(engine_lib, oracle_lib, model, L, emin, emax, bw, nwin, R, se, sc, seed,
+                     walkers_per_warp=walkers_per_warp)
     try:
         _compare(eng, orc, "init")
         for k in range(cycles):
