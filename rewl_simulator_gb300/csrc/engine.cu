@@ -518,18 +518,10 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
 // bins: 4|J| divisible by the bin width, as for J = 1 and width 4).  The chain
 // then carries only the bin index b and the logDoS value g[b].
 //
-// G walkers share a warp (P = 32/G lanes each); all lanes of a walker hold the
-// same chain state, so the warp's instructions advance G chains at once.  For
-// each chunk the walker's lanes first write one 16-byte record per site:
-// integer acceptance threshold, packed bin changes (without / with the left
-// neighbour flipped, wrap term for x = L-1) and the spin.  The accept chain then
-// runs "two worlds" ahead: while step j resolves, the proposal of step j+1 is
-// formed for both outcomes of step j, its logDoS entry loaded and its acceptance
-// evaluated, so the loop-carried dependency per step is one select; the shared
-// memory loads of consecutive steps overlap.  The only store that can land
-// between such a load and its use is step j's commit to the bin step j ends in,
-// which is exactly the world's own current bin: that case uses the value being
-// committed.
+// G walkers share a warp (P = 32/G lanes each).  For each chunk the walker's
+// lanes first write one 16-byte record per site: integer acceptance threshold,
+// packed bin changes (without / with the left neighbour flipped, wrap term for
+// x = L-1) and the spin.
 // ---------------------------------------------------------------------------
 struct __align__(16) SiteRec {
     long long T;    // accept iff d < T
@@ -539,18 +531,20 @@ struct __align__(16) SiteRec {
 
 __device__ __forceinline__ int sx8(int v) { return (int)(signed char)(v & 0xFF); }
 
-struct World {
-    int B;          // bin before the step
-    int BN;         // proposed bin
-    long long GC;   // logDoS at B (committed value)
-    long long GN;   // logDoS at BN
-    bool C;         // acceptance of the step in this world
-};
-
+// Speculative resolution of D = log2(P) consecutive sites per round: each of a
+// walker's P lanes assumes one accept/reject pattern (its lane index), follows
+// that path through the bins -- the logDoS value of a bin at a step is its value
+// before the round plus ln f times the path's earlier visits to it -- and checks
+// that every decision it computes agrees with its assumption.  Exactly one lane
+// (the true path) is consistent; a ballot finds it, it commits the round's logDoS
+// updates, and its final (bin, value) becomes the walker's state.  All loads of a
+// round are independent, so a round costs about one shared-memory latency plus a
+// ballot and a shuffle instead of D dependent load-compare-select steps.
 template <int G, int C>
 __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
 {
-    constexpr int P = 32 / G;
+    constexpr int P = 32 / G;                 // lanes (paths) per walker
+    constexpr int D = P == 32 ? 5 : (P == 16 ? 4 : 3);
     constexpr int SPL = (C + P - 1) / P;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -593,6 +587,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     }
     int M = P_.cfg_M[3 * cfg];
     long long gc = gs[b];
+    const unsigned gmask = P == 32 ? 0xFFFFFFFFu : (((1u << P) - 1u) << (grp * P));
 
     for (int sw = 0; sw < p.nsweeps; ++sw) {
         const uint64_t A0 = (sweeps0 + (uint64_t)sw) * (uint64_t)N;
@@ -624,54 +619,67 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             }
             __syncwarp();
 
-            // step 0 of the chunk: no earlier flip in the chunk can affect it
             unsigned acc = 0;
-            World X;
-            {
-                const SiteRec r = rec[0];
-                X.B = b;
-                X.GC = gc;
-                X.BN = b + sx8(r.pk);
-                const bool in = (unsigned)X.BN < (unsigned)nb;
-                X.GN = gs[in ? X.BN : b];
-                X.C = in && (X.GN - X.GC < r.T);
-            }
-            World X1 = X;                        // both worlds coincide at step 0
-            bool pa = false;
 #pragma unroll
-            for (int j = 0; j < C; ++j) {
-                const bool a = pa ? X1.C : X.C;                 // outcome of step j
-                const World R = pa ? X1 : X;                     // real state of step j
-                World Y0, Y1;
-                if (j + 1 < C) {
-                    const SiteRec r = rec[j + 1];
-                    const int wrapb = sx8(r.pk >> 16);
-                    const int w0 = (j == 0) ? 0 : ((acc & 1u) ? wrapb : 0);
-                    const int w1 = (j == 0) ? wrapb : ((acc & 1u) ? wrapb : 0);
-                    // world a_j = 0: stays in R.B, left neighbour not flipped
-                    Y0.B = R.B;
-                    Y0.GC = R.GC + lnf;
-                    Y0.BN = R.B + sx8(r.pk) + w0;
-                    // world a_j = 1: moved to R.BN, left neighbour flipped
-                    Y1.B = R.BN;
-                    Y1.GC = R.GN + lnf;
-                    Y1.BN = R.BN + sx8(r.pk >> 8) + w1;
-                    const bool in0 = (unsigned)Y0.BN < (unsigned)nb;
-                    const bool in1 = (unsigned)Y1.BN < (unsigned)nb;
-                    const long long l0 = gs[in0 ? Y0.BN : 0];
-                    const long long l1 = gs[in1 ? Y1.BN : 0];
-                    Y0.GN = (Y0.BN == Y0.B) ? Y0.GC : l0;
-                    Y1.GN = (Y1.BN == Y1.B) ? Y1.GC : l1;
-                    Y0.C = in0 && (Y0.GN - Y0.GC < r.T);
-                    Y1.C = in1 && (Y1.GN - Y1.GC < r.T);
+            for (int j0 = 0; j0 < C; j0 += D) {
+                constexpr int DD = D;                       // steps in a full round
+                const int nd = (C - j0) < DD ? (C - j0) : DD;   // steps in this round (compile-time after unrolling)
+                const unsigned path = (unsigned)q;
+                int cur = b;
+                long long curBase = gc;
+                int prop[DD], aft[DD];
+                long long propBase[DD], aftBase[DD];
+                bool ok = q < (1 << nd);
+                // follow the assumed path: bins first (no loads depend on loads)
+#pragma unroll
+                for (int k = 0; k < DD; ++k) {
+                    if (k < nd) {
+                        const SiteRec r = rec[j0 + k];
+                        const bool prevflip = (k == 0) ? (j0 > 0 && ((acc >> (j0 - 1)) & 1u)) : ((path >> (k - 1)) & 1u);
+                        const bool site0flip = (j0 == 0) ? (k > 0 && (path & 1u)) : (acc & 1u);
+                        const int db = sx8(prevflip ? (r.pk >> 8) : r.pk) + (site0flip ? sx8(r.pk >> 16) : 0);
+                        prop[k] = cur + db;
+                        const bool in = (unsigned)prop[k] < (unsigned)nb;
+                        propBase[k] = gs[in ? prop[k] : 0];
+                        const bool ak = (path >> k) & 1u;
+                        // decisions need the visit counts of earlier steps on this path
+                        int cp = 0, cc = 0;
+#pragma unroll
+                        for (int kk = 0; kk < k; ++kk) { cp += aft[kk] == prop[k]; cc += aft[kk] == cur; }
+                        const long long gP = propBase[k] + (long long)cp * lnf;
+                        const long long gC = curBase + (long long)cc * lnf;
+                        const bool dec = in && (gP - gC < r.T);
+                        ok = ok && (dec == ak);
+                        aft[k] = ak ? prop[k] : cur;
+                        aftBase[k] = ak ? propBase[k] : curBase;
+                        cur = aft[k];
+                        curBase = aftBase[k];
+                    }
                 }
-                // commit step j
-                const int bj = a ? R.BN : R.B;
-                const long long gj = (a ? R.GN : R.GC) + lnf;
-                gs[bj] = gj;
-                if (a) acc |= 1u << j;
-                if (j + 1 < C) { X = Y0; X1 = Y1; pa = a; }
-                else { b = bj; gc = gj; }
+                const unsigned bal = __ballot_sync(kFull, ok) & gmask;
+                const int winner = __ffs(bal) - 1;           // the consistent lane of this walker
+                const int wq = winner - grp * P;             // its path bits
+                if (lane == winner) {
+                    // commit: each visited bin ends at base + (its visits in the round) * ln f
+#pragma unroll
+                    for (int k = 0; k < DD; ++k) {
+                        if (k < nd) {
+                            int cnt = 0;
+#pragma unroll
+                            for (int kk = 0; kk < DD; ++kk) cnt += (kk < nd) && aft[kk] == aft[k];
+                            gs[aft[k]] = aftBase[k] + (long long)cnt * lnf;
+                        }
+                    }
+                }
+                // new walker state from the winner
+                int cnt_end = 0;
+#pragma unroll
+                for (int kk = 0; kk < DD; ++kk) cnt_end += (kk < nd) && aft[kk] == cur;
+                const long long gend = curBase + (long long)cnt_end * lnf;
+                b = __shfl_sync(kFull, cur, winner);
+                gc = __shfl_sync(kFull, gend, winner);
+                acc |= (unsigned)wq << j0;
+                __syncwarp();
             }
             // apply the chunk's flips and the magnetisation change
             unsigned plus = 0;
@@ -1496,7 +1504,7 @@ int plan_launches(rewl_engine* e)
         const int n = (int)l.slots.size();
         if (l.bins) {
             int G = e->desc.walkers_per_warp;
-            if (G == 0) G = 4;                                     // shares the warp's issue slots among 4 chains
+            if (G == 0) G = 1;                                     // 32 speculative paths per walker
             l.walkers_per_warp = G;
             l.nbcap = (maxnb + 1) & ~1;
             int raw = l.nbcap * 8 + 32 * (int)sizeof(SiteRec) + ((maxN + 15) & ~15);
