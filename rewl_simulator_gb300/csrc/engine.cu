@@ -519,9 +519,9 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
 // then carries only the bin index b and the logDoS value g[b].
 //
 // G walkers share a warp (P = 32/G lanes each).  For each chunk the walker's
-// lanes first write one 16-byte record per site: integer acceptance threshold,
-// packed bin changes (without / with the left neighbour flipped, wrap term for
-// x = L-1) and the spin.
+// lanes first form, per site: the integer acceptance threshold, the packed bin
+// changes (without / with the left neighbour flipped, wrap term for x = L-1)
+// and the spin.
 // ---------------------------------------------------------------------------
 struct __align__(16) SiteRec {
     long long T;    // accept iff d < T
@@ -531,24 +531,22 @@ struct __align__(16) SiteRec {
 
 __device__ __forceinline__ int sx8(int v) { return (int)(signed char)(v & 0xFF); }
 
-// Speculative resolution of D = log2(P) consecutive sites per round: each of a
-// walker's P lanes assumes one accept/reject pattern (its lane index), follows
-// that path through the bins -- the logDoS value of a bin at a step is its value
-// before the round plus ln f times the path's earlier visits to it -- and checks
-// that every decision it computes agrees with its assumption.  Exactly one lane
-// (the true path) is consistent; a ballot finds it, it commits the round's logDoS
-// updates, and its final (bin, value) becomes the walker's state.  All loads of a
-// round are independent, so a round costs about one shared-memory latency plus a
-// ballot and a shuffle instead of D dependent load-compare-select steps.
+// The accept chain, all lanes of a walker in lockstep.  Per step the only
+// dependent work is: load g at the proposed bin, one 64-bit compare against
+// (g at the current bin + threshold) -- formed while the load is in flight --
+// and a select of the next proposal, whose two candidates (previous site
+// accepted or not) are already formed.  The commit store of a step is issued
+// before the next step's load, so shared memory always hands the load the
+// latest value.  Per-site data (threshold, bin changes) reaches every lane by
+// register shuffles, which the unrolled loop issues ahead of the chain.
 template <int G, int C>
 __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
 {
-    constexpr int P = 32 / G;                 // lanes (paths) per walker
-    constexpr int D = P == 32 ? 5 : (P == 16 ? 4 : 3);
+    constexpr int P = 32 / G;
     constexpr int SPL = (C + P - 1) / P;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int grp = lane / P, q = lane - grp * P;
+    const int grp = lane / P, q = lane - grp * P, gbase = grp * P;
     const int li = (blockIdx.x * (blockDim.x >> 5) + wib) * G + grp;
     const bool valid = li < p.nslots;
     if (__ballot_sync(kFull, valid) == 0) return;             // whole warp without walkers
@@ -560,8 +558,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     const int L = I.L, N = I.N, nb = W.nb;
     unsigned char* base = smem + (size_t)(wib * G + grp) * p.smem_per_warp;
     long long* gs = reinterpret_cast<long long*>(base);
-    SiteRec* rec = reinterpret_cast<SiteRec*>(gs + p.nbcap);
-    int8_t* lat = reinterpret_cast<int8_t*>(rec + 32);
+    int8_t* lat = reinterpret_cast<int8_t*>(gs + p.nbcap);
 
     const int cfg = P_.slot_cfg[s];
     int8_t* gl = P_.spins + P_.cfg_off[cfg];
@@ -587,7 +584,6 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     }
     int M = P_.cfg_M[3 * cfg];
     long long gc = gs[b];
-    const unsigned gmask = P == 32 ? 0xFFFFFFFFu : (((1u << P) - 1u) << (grp * P));
 
     for (int sw = 0; sw < p.nsweeps; ++sw) {
         const uint64_t A0 = (sweeps0 + (uint64_t)sw) * (uint64_t)N;
@@ -595,11 +591,12 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             const int y = c0 / L, x0 = c0 - y * L;
             const int row = y * L;
             const int up = (y == 0 ? L - 1 : y - 1) * L, down = (y == L - 1 ? 0 : y + 1) * L;
-            int my_s[SPL];
+            int my_s[SPL], my_pk[SPL];
+            long long my_T[SPL];
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 const int jj = q + k * P;
-                my_s[k] = 0;
+                my_s[k] = 0; my_pk[k] = 0; my_T[k] = 0;
                 if (jj < C) {
                     const int x = x0 + jj;
                     const int si = lat[row + x];
@@ -609,77 +606,52 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                     const int d0 = 2 * J * si * sum;
                     const int d1 = jj > 0 ? d0 - 4 * J * si * left : d0;
                     const int wc = (C == L && jj == L - 1) ? -4 * J * si * right : 0;
-                    SiteRec r;
-                    r.pk = ((d0 >> sh) & 0xFF) | (((d1 >> sh) & 0xFF) << 8) | (((wc >> sh) & 0xFF) << 16);
-                    r.T = accept_threshold(neglog_u32(philox_word(seed, uid, A0 + (uint64_t)(c0 + jj), kStreamWL)));
-                    r.s = si;
-                    rec[jj] = r;
+                    my_pk[k] = ((d0 >> sh) & 0xFF) | (((d1 >> sh) & 0xFF) << 8) | (((wc >> sh) & 0xFF) << 16);
+                    my_T[k] = accept_threshold(neglog_u32(philox_word(seed, uid, A0 + (uint64_t)(c0 + jj), kStreamWL)));
                     my_s[k] = si;
                 }
             }
-            __syncwarp();
 
             unsigned acc = 0;
+            int pk = __shfl_sync(kFull, my_pk[0], gbase);
+            long long T = __shfl_sync(kFull, my_T[0], gbase);
+            int bn = b + sx8(pk);
+            bool in = (unsigned)bn < (unsigned)nb;
+            int an = in ? bn : b;
+            long long gcT = gc + T, gcL = gc + lnf;
 #pragma unroll
-            for (int j0 = 0; j0 < C; j0 += D) {
-                constexpr int DD = D;                       // steps in a full round
-                const int nd = (C - j0) < DD ? (C - j0) : DD;   // steps in this round (compile-time after unrolling)
-                const unsigned path = (unsigned)q;
-                int cur = b;
-                long long curBase = gc;
-                int prop[DD], aft[DD];
-                long long propBase[DD], aftBase[DD];
-                bool ok = q < (1 << nd);
-                // follow the assumed path: bins first (no loads depend on loads)
-#pragma unroll
-                for (int k = 0; k < DD; ++k) {
-                    if (k < nd) {
-                        const SiteRec r = rec[j0 + k];
-                        const bool prevflip = (k == 0) ? (j0 > 0 && ((acc >> (j0 - 1)) & 1u)) : ((path >> (k - 1)) & 1u);
-                        const bool site0flip = (j0 == 0) ? (k > 0 && (path & 1u)) : (acc & 1u);
-                        const int db = sx8(prevflip ? (r.pk >> 8) : r.pk) + (site0flip ? sx8(r.pk >> 16) : 0);
-                        prop[k] = cur + db;
-                        const bool in = (unsigned)prop[k] < (unsigned)nb;
-                        propBase[k] = gs[in ? prop[k] : 0];
-                        const bool ak = (path >> k) & 1u;
-                        // decisions need the visit counts of earlier steps on this path
-                        int cp = 0, cc = 0;
-#pragma unroll
-                        for (int kk = 0; kk < k; ++kk) { cp += aft[kk] == prop[k]; cc += aft[kk] == cur; }
-                        const long long gP = propBase[k] + (long long)cp * lnf;
-                        const long long gC = curBase + (long long)cc * lnf;
-                        const bool dec = in && (gP - gC < r.T);
-                        ok = ok && (dec == ak);
-                        aft[k] = ak ? prop[k] : cur;
-                        aftBase[k] = ak ? propBase[k] : curBase;
-                        cur = aft[k];
-                        curBase = aftBase[k];
-                    }
+            for (int j = 0; j < C; ++j) {
+                const long long gn = gs[an];
+                int c0n = 0, c1n = 0, a0 = 0, a1 = 0;
+                bool i0 = false, i1 = false;
+                long long T1 = 0;
+                if (j + 1 < C) {
+                    const int pk1 = __shfl_sync(kFull, my_pk[(j + 1) / P], gbase + (j + 1) % P);
+                    T1 = __shfl_sync(kFull, my_T[(j + 1) / P], gbase + (j + 1) % P);
+                    const int wrapb = sx8(pk1 >> 16);
+                    const int w0 = (j == 0) ? 0 : ((acc & 1u) ? wrapb : 0);
+                    const int w1 = (j == 0) ? wrapb : ((acc & 1u) ? wrapb : 0);
+                    c0n = b + sx8(pk1) + w0;                  // step j rejected: stay, left not flipped
+                    c1n = bn + sx8(pk1 >> 8) + w1;            // step j accepted: move, left flipped
+                    i0 = (unsigned)c0n < (unsigned)nb;
+                    i1 = (unsigned)c1n < (unsigned)nb;
+                    a0 = i0 ? c0n : 0;
+                    a1 = i1 ? c1n : 0;
                 }
-                const unsigned bal = __ballot_sync(kFull, ok) & gmask;
-                const int winner = __ffs(bal) - 1;           // the consistent lane of this walker
-                const int wq = winner - grp * P;             // its path bits
-                if (lane == winner) {
-                    // commit: each visited bin ends at base + (its visits in the round) * ln f
-#pragma unroll
-                    for (int k = 0; k < DD; ++k) {
-                        if (k < nd) {
-                            int cnt = 0;
-#pragma unroll
-                            for (int kk = 0; kk < DD; ++kk) cnt += (kk < nd) && aft[kk] == aft[k];
-                            gs[aft[k]] = aftBase[k] + (long long)cnt * lnf;
-                        }
-                    }
+                const bool a = in && (gn < gcT);
+                const long long gnew = a ? gn + lnf : gcL;
+                const int bnew = a ? bn : b;
+                gs[bnew] = gnew;
+                if (a) acc |= 1u << j;
+                b = bnew;
+                gc = gnew;
+                if (j + 1 < C) {
+                    bn = a ? c1n : c0n;
+                    in = a ? i1 : i0;
+                    an = a ? a1 : a0;
+                    gcT = gnew + T1;
+                    gcL = gnew + lnf;
                 }
-                // new walker state from the winner
-                int cnt_end = 0;
-#pragma unroll
-                for (int kk = 0; kk < DD; ++kk) cnt_end += (kk < nd) && aft[kk] == cur;
-                const long long gend = curBase + (long long)cnt_end * lnf;
-                b = __shfl_sync(kFull, cur, winner);
-                gc = __shfl_sync(kFull, gend, winner);
-                acc |= (unsigned)wq << j0;
-                __syncwarp();
             }
             // apply the chunk's flips and the magnetisation change
             unsigned plus = 0;
@@ -687,7 +659,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             for (int k = 0; k < SPL; ++k) {
                 const int jj = q + k * P;
                 const unsigned bal = __ballot_sync(kFull, jj < C && my_s[k] > 0);
-                const unsigned mine = P == 32 ? bal : ((bal >> (grp * P)) & ((1u << P) - 1u));
+                const unsigned mine = P == 32 ? bal : ((bal >> gbase) & ((1u << P) - 1u));
                 plus |= (k * P < 32) ? (mine << (k * P)) : 0u;
                 if (jj < C && ((acc >> jj) & 1u)) lat[row + x0 + jj] = (int8_t)(-my_s[k]);
             }
@@ -1504,10 +1476,14 @@ int plan_launches(rewl_engine* e)
         const int n = (int)l.slots.size();
         if (l.bins) {
             int G = e->desc.walkers_per_warp;
-            if (G == 0) G = 1;                                     // 32 speculative paths per walker
+            if (G == 0) {
+                // one walker per warp while the SM sub-partitions outnumber the walkers
+                // (the chain is latency-bound); pack walkers into warps beyond that
+                G = n <= 4 * nsm ? 1 : (n <= 16 * nsm ? 2 : 4);
+            }
             l.walkers_per_warp = G;
             l.nbcap = (maxnb + 1) & ~1;
-            int raw = l.nbcap * 8 + 32 * (int)sizeof(SiteRec) + ((maxN + 15) & ~15);
+            int raw = l.nbcap * 8 + ((maxN + 15) & ~15);
             l.smem_per_warp = ((raw + 127) & ~127) + 16;           // per walker; +16 skews the walkers' banks
             if ((size_t)l.smem_per_warp * G > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory", l.smem_per_warp);
             int wpb = e->desc.warps_per_block;
