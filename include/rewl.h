@@ -253,6 +253,18 @@ int rewl_mlp_set_data(rewl_mlp* mlp, const float* X, const float* y, int32_t n, 
 int rewl_mlp_train(rewl_mlp* mlp, int32_t steps, int32_t batch, float lr, float* losses);
 /* kernels launched by this network so far */
 int rewl_mlp_launches(const rewl_mlp* mlp, int64_t* count);
+/* Allocation-free prediction (no counterpart in the reference).  Same result as
+ * rewl_mlp_predict, but X (n x in_dim floats) and y (n floats) are DEVICE
+ * pointers and the work is enqueued on `stream` (a cudaStream_t; NULL = legacy
+ * default stream) without waiting for it.  Activations live in a static 9.5 MiB
+ * device array, so no call allocates device memory; for callers that cannot
+ * allocate (while a stream is being captured, or at a device-memory limit).
+ * At most 4096 rows per call and hidden width at most 256, else REWL_EINVAL.
+ * The first call on a device looks up the array's address: make it before any
+ * stream capture.  The array is shared by all networks on a device: calls that
+ * may overlap (other streams, other threads) race and must be ordered by the
+ * caller.  Parameters must not change while a call is in flight. */
+int rewl_mlp_predict_noalloc(rewl_mlp* mlp, const float* X, int32_t n, int32_t in_dim, float* y, void* stream);
 
 #ifdef __cplusplus
 }

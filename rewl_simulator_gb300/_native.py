@@ -117,6 +117,7 @@ def _declare(L: C.CDLL) -> None:
         "rewl_mlp_set_data": [vp, vp, vp, i32, i32],
         "rewl_mlp_train": [vp, i32, i32, C.c_float, vp],
         "rewl_mlp_launches": [vp, vp],
+        "rewl_mlp_predict_noalloc": [vp, vp, i32, i32, vp, vp],
     }
     for name, args in sigs.items():
         f = getattr(L, name)

@@ -14,6 +14,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -605,3 +606,124 @@ int rewl_mlp_launches(const rewl_mlp* m, int64_t* n)
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free prediction (rewl_mlp_predict_noalloc).
+//
+// rewl_mlp_predict grows its activation buffers with cudaMalloc when a larger
+// batch arrives and stages inputs through host memory.  Callers that must not
+// allocate -- code enqueuing work while a CUDA stream is being captured, or a
+// loop holding device memory at its limit -- use this variant instead: inputs
+// and outputs are device pointers owned by the caller, and the activations live
+// in one file-scope static device array.  Its address is looked up once per
+// device (cudaGetSymbolAddress with that device current) on the first call.
+//
+// Limits: at most kNoAllocMaxRows rows per call and hidden width at most
+// kNoAllocMaxHidden (9.5 MiB of scratch); larger requests fail with REWL_EINVAL.
+// Nothing in the scratch has to start at zero: every call writes each element
+// it later reads (the staging kernel writes the zero padding too).  The scratch
+// is shared by every network on a device, so calls that may overlap -- on
+// different streams, or from different host threads -- race on it and must be
+// ordered by the caller (for example, issue them on one stream).
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxRows = 4096;
+constexpr int kNoAllocMaxHidden = 256;
+constexpr int kNoAllocMaxDevices = 64;
+constexpr size_t kNaIn = (size_t)kNoAllocMaxRows * kIn * sizeof(bf16);                   // padded inputs
+constexpr size_t kNaH = (size_t)kNoAllocMaxRows * kNoAllocMaxHidden * sizeof(bf16);      // activations (x2)
+constexpr size_t kNaZ = (size_t)kNoAllocMaxRows * kNoAllocMaxHidden * sizeof(float);     // pre-activations
+constexpr size_t kNaOut = (size_t)kNoAllocMaxRows * kOut * sizeof(float);                // padded outputs
+constexpr size_t kNoAllocBytes = kNaIn + 2 * kNaH + kNaZ + kNaOut;
+static_assert(kNaIn % 256 == 0 && kNaH % 256 == 0 && kNaZ % 256 == 0, "sub-buffers stay 256-byte aligned");
+
+} // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Address of the static scratch on `device` (which must be current).
+int noalloc_scratch(int device, unsigned char** out)
+{
+    if (device < 0 || device >= kNoAllocMaxDevices) return mfail(REWL_EINVAL, "device %d out of range", device);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return mfail(REWL_EDEVICE, "cudaGetSymbolAddress(scratch) on device %d: %s", device, cudaGetErrorString(e));
+        g_noalloc_ptr[device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_ptr[device];
+    return REWL_OK;
+}
+
+// rows x kIn bf16 inputs, zero beyond n rows and in_dim columns
+__global__ void k_noalloc_stage(const float* X, int n, int in_dim, int rows, bf16* H0)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)rows * kIn) return;
+    const int r = (int)(i / kIn), c = (int)(i % kIn);
+    H0[i] = __float2bfloat16(r < n && c < in_dim ? X[(size_t)r * in_dim + c] : 0.f);
+}
+
+__global__ void k_noalloc_take(const float* out, int n, float* y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = out[(size_t)i * kOut];
+}
+
+template <int EPI>
+cudaError_t noalloc_layer(cudaStream_t st, const bf16* A, const bf16* W, int M, int N, int K, float* Cf, bf16* Cb,
+                          const float* bias)
+{
+    const GemmArgs g{A, W, M, N, K, K, K, K, Cf, Cb, N, bias};
+    k_gemm<false, true, EPI><<<dim3(N / kBN, M / kBM, 1), 128, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+extern "C" int rewl_mlp_predict_noalloc(rewl_mlp* m, const float* X, int32_t n, int32_t in_dim, float* y, void* stream)
+{
+    if (!m || !X || !y || n < 1 || in_dim < 1 || in_dim > kIn) return mfail(REWL_EINVAL, "bad arguments");
+    if (n > kNoAllocMaxRows)
+        return mfail(REWL_EINVAL, "rewl_mlp_predict_noalloc: %d rows exceed the static scratch limit of %d rows per call",
+                     n, kNoAllocMaxRows);
+    if (m->hidden > kNoAllocMaxHidden)
+        return mfail(REWL_EINVAL, "rewl_mlp_predict_noalloc: hidden width %d exceeds the static scratch limit of %d",
+                     m->hidden, kNoAllocMaxHidden);
+    MCUDA(cudaSetDevice(m->device));
+    unsigned char* s = nullptr;
+    int rc = noalloc_scratch(m->device, &s);
+    if (rc) return rc;
+    bf16* H0 = reinterpret_cast<bf16*>(s);
+    bf16* Ha = reinterpret_cast<bf16*>(s + kNaIn);
+    bf16* Hb = reinterpret_cast<bf16*>(s + kNaIn + kNaH);
+    float* Z = reinterpret_cast<float*>(s + kNaIn + 2 * kNaH);
+    float* out = reinterpret_cast<float*>(s + kNaIn + 2 * kNaH + kNaZ);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int rows = (n + kBM - 1) / kBM * kBM;
+
+    k_noalloc_stage<<<(unsigned)(((size_t)rows * kIn + 255) / 256), 256, 0, st>>>(X, n, in_dim, rows, H0);
+    MCUDA(cudaGetLastError());
+    const bf16* cur = H0;
+    for (int l = 0; l < m->layers; ++l) {
+        bf16* nxt = (l & 1) ? Hb : Ha;
+        MCUDA(noalloc_layer<EPI_BIAS_GELU>(st, cur, m->Pb.p + m->woff[l], rows, m->dout[l], m->din[l], Z, nxt,
+                                           m->P.p + m->boff[l]));
+        cur = nxt;
+    }
+    const int L = m->layers;
+    MCUDA(noalloc_layer<EPI_BIAS_F32>(st, cur, m->Pb.p + m->woff[L], rows, kOut, m->hidden, out, nullptr,
+                                      m->P.p + m->boff[L]));
+    k_noalloc_take<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, y);
+    MCUDA(cudaGetLastError());
+    m->launches += L + 3;
+    return REWL_OK;
+}

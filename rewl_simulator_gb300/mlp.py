@@ -86,6 +86,12 @@ class MLP:
         self._check(self.lib.rewl_mlp_predict(self.h, _p(X), X.shape[0], X.shape[1], _p(y)))
         return y
 
+    def predict_noalloc(self, X_ptr: int, n: int, in_dim: int, y_ptr: int, stream: int = 0) -> None:
+        """rewl_mlp_predict_noalloc: device pointers in and out, enqueued on `stream`
+        (a cudaStream_t handle) with no device allocation and no wait."""
+        self._check(self.lib.rewl_mlp_predict_noalloc(self.h, C.c_void_p(X_ptr), n, in_dim, C.c_void_p(y_ptr),
+                                                      C.c_void_p(stream)))
+
     def gradient(self, X: np.ndarray, y: np.ndarray) -> float:
         X = np.ascontiguousarray(X, dtype=np.float32)
         y = np.ascontiguousarray(y, dtype=np.float32)
