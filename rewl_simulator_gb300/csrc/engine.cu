@@ -529,21 +529,49 @@ struct __align__(16) SiteRec {
     int s;          // spin
 };
 
-__device__ __forceinline__ int sx8(int v) { return (int)(signed char)(v & 0xFF); }
 
-// The accept chain, all lanes of a walker in lockstep.  Per step the only
-// dependent work is: load g at the proposed bin, one 64-bit compare against
-// (g at the current bin + threshold) -- formed while the load is in flight --
-// and a select of the next proposal, whose two candidates (previous site
-// accepted or not) are already formed.  The commit store of a step is issued
-// before the next step's load, so shared memory always hands the load the
-// latest value.  Per-site data (threshold, bin changes) reaches every lane by
-// register shuffles, which the unrolled loop issues ahead of the chain.
+// The accept chain, all lanes of a walker in lockstep, with the table reads one
+// site ahead.  While site j is being decided, the two bins site j+1 may propose
+// (one if site j is rejected, one if it is accepted -- which moves the walker
+// and flips the left neighbour of site j+1) are already being loaded, so the
+// load latency overlaps the decision.  Per site the dependent work is then:
+// one 64-bit compare of g(proposal) against g(current) + threshold, a select of
+// the taken branch and one add.
+//
+// A prefetched load follows the commit store of the site before it, so it is
+// stale only when it reads the bin the next commit writes, i.e. exactly when
+// its proposal keeps the bin (offset change 0); the value is then the one just
+// committed.
+//
+// The table carries kGuard sentinel bins on each side holding 2^62, so a
+// proposal outside the window fails the compare by itself (no range checks),
+// and prefetches issued from such a proposal stay inside the table.  Bin
+// positions are byte offsets into the table.
+//
+// The chain runs without a break from chunk to chunk: the first offsets of the
+// next chunk are formed from the lattice before the current chunk's flips, then
+// corrected for the neighbours the current chunk flips as soon as those are
+// decided, and handed to all lanes by shuffle; thresholds come from one Philox
+// block per four sites, 4C sites at a time, one batch ahead.
+constexpr int kGuard = 8;
+constexpr long long kGuardValue = 1LL << 62;
+
+__device__ __forceinline__ long long lds64(const char* base, int off)
+{
+    return *reinterpret_cast<const long long*>(base + off);
+}
+__device__ __forceinline__ int pack_e(int e0, int e1) { return (e0 & 0xFFFF) | (e1 << 16); }
+__device__ __forceinline__ int e_lo(int v) { return (int)(short)(v & 0xFFFF); }
+__device__ __forceinline__ int e_hi(int v) { return v >> 16; }
+
 template <int G, int C>
 __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
 {
     constexpr int P = 32 / G;
-    constexpr int SPL = (C + P - 1) / P;
+    constexpr int SPL = (C + P - 1) / P;          // sites per lane in a chunk
+    constexpr int BPL = (C + P - 1) / P;          // Philox blocks per lane in a batch of 4C sites
+    constexpr int kAhead = 4;                     // per-site inputs are read this many sites early
+    static_assert(C % 4 == 0 && C >= 4 && C <= 32 && P >= 4, "chunk");
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int grp = lane / P, q = lane - grp * P, gbase = grp * P;
@@ -557,117 +585,227 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     const WinDev W = P_.win[w];
     const int L = I.L, N = I.N, nb = W.nb;
     unsigned char* base = smem + (size_t)(wib * G + grp) * p.smem_per_warp;
-    long long* gs = reinterpret_cast<long long*>(base);
-    int8_t* lat = reinterpret_cast<int8_t*>(gs + p.nbcap);
+    const int gs_bytes = ((p.nbcap + 2 * kGuard) * 8 + 15) & ~15;
+    long long* gs = reinterpret_cast<long long*>(base) + kGuard;     // gs[-kGuard .. nb+kGuard)
+    int8_t* lat = reinterpret_cast<int8_t*>(base + gs_bytes);
+    long long* Tb = reinterpret_cast<long long*>(base + gs_bytes + ((N + 15) & ~15));   // 2 x 4C thresholds
+    int* Db = reinterpret_cast<int*>(Tb + 8 * C);                                     // 2 x C packed offsets
+    char* const gsb = reinterpret_cast<char*>(gs);
 
     const int cfg = P_.slot_cfg[s];
     int8_t* gl = P_.spins + P_.cfg_off[cfg];
     long long* gg = reinterpret_cast<long long*>(P_.g + P_.slot_tab[s]);
     for (int i = q; i < N; i += P) lat[i] = gl[i];
     for (int k = q; k < nb; k += P) gs[k] = gg[k];
+    for (int k = q; k < kGuard; k += P) { gs[-1 - k] = kGuardValue; gs[nb + k] = kGuardValue; }
     __syncwarp();
 
     const int J = (int)I.J_u;
-    const int sh = I.bin_shift;
+    const int sh = I.bin_shift;                        // energy change -> bin change (x8: byte offset)
     const int Ewlo = (int)W.elo_u;
     const long long lnf = P_.win_lnf[w];
     const uint64_t sweeps0 = P_.slot_sweeps[s];
     const uint32_t uid = (uint32_t)(s - I.first_slot);
-    const uint64_t seed = I.seed;
+    const uint32_t k0 = (uint32_t)I.seed ^ uid, k1 = (uint32_t)(I.seed >> 32);
+    const bool wraps = C == L;                         // a row is one chunk: its last site sees the row start
 
     const int E0 = (int)P_.cfg_E[cfg];
-    int b = (E0 - Ewlo) >> sh;
-    const bool bad = ((E0 - Ewlo) & ((1 << sh) - 1)) != 0 || b < 0 || b >= nb;
+    const int b0 = (E0 - Ewlo) >> sh;
+    const bool bad = ((E0 - Ewlo) & ((1 << sh) - 1)) != 0 || b0 < 0 || b0 >= nb;
     if (__ballot_sync(kFull, valid && bad)) {
         if (lane == 0) atomicOr(&P_.counters[0], ERR_BOUNDS);
         return;
     }
     int M = P_.cfg_M[3 * cfg];
-    long long gc = gs[b];
 
-    for (int sw = 0; sw < p.nsweeps; ++sw) {
-        const uint64_t A0 = (sweeps0 + (uint64_t)sw) * (uint64_t)N;
-        for (int c0 = 0; c0 < N; c0 += C) {
-            const int y = c0 / L, x0 = c0 - y * L;
-            const int row = y * L;
-            const int up = (y == 0 ? L - 1 : y - 1) * L, down = (y == L - 1 ? 0 : y + 1) * L;
-            int my_s[SPL], my_pk[SPL];
-            long long my_T[SPL];
+    // thresholds (+ ln f) of the 4C sites from attempt A0 on into Tb[buf]
+    auto draw = [&](uint64_t A0, int buf) {
+        longlong2* dst = reinterpret_cast<longlong2*>(Tb + buf * 4 * C);
 #pragma unroll
-            for (int k = 0; k < SPL; ++k) {
-                const int jj = q + k * P;
-                my_s[k] = 0; my_pk[k] = 0; my_T[k] = 0;
-                if (jj < C) {
-                    const int x = x0 + jj;
-                    const int si = lat[row + x];
-                    const int left = lat[row + (x == 0 ? L - 1 : x - 1)];
-                    const int right = lat[row + (x == L - 1 ? 0 : x + 1)];
-                    const int sum = lat[up + x] + left + right + lat[down + x];
-                    const int d0 = 2 * J * si * sum;
-                    const int d1 = jj > 0 ? d0 - 4 * J * si * left : d0;
-                    const int wc = (C == L && jj == L - 1) ? -4 * J * si * right : 0;
-                    my_pk[k] = ((d0 >> sh) & 0xFF) | (((d1 >> sh) & 0xFF) << 8) | (((wc >> sh) & 0xFF) << 16);
-                    my_T[k] = accept_threshold(neglog_u32(philox_word(seed, uid, A0 + (uint64_t)(c0 + jj), kStreamWL)));
-                    my_s[k] = si;
-                }
+        for (int k = 0; k < BPL; ++k) {
+            const int bi = q + k * P;
+            if (bi < C) {
+                const uint64_t a = A0 + (uint64_t)(4 * bi);
+                const Philox4 r = philox4x32_10(Philox4{(uint32_t)(a >> 2), (uint32_t)(a >> 34), kStreamWL, 0u}, k0, k1);
+                longlong2 t01, t23;
+                t01.x = accept_threshold(neglog_u32(r.x)) + lnf;
+                t01.y = accept_threshold(neglog_u32(r.y)) + lnf;
+                t23.x = accept_threshold(neglog_u32(r.z)) + lnf;
+                t23.y = accept_threshold(neglog_u32(r.w)) + lnf;
+                dst[2 * bi] = t01;
+                dst[2 * bi + 1] = t23;
             }
+        }
+    };
 
-            unsigned acc = 0;
-            int pk = __shfl_sync(kFull, my_pk[0], gbase);
-            long long T = __shfl_sync(kFull, my_T[0], gbase);
-            int bn = b + sx8(pk);
-            bool in = (unsigned)bn < (unsigned)nb;
-            int an = in ? bn : b;
-            long long gcT = gc + T, gcL = gc + lnf;
+    // Inputs of a chunk formed from the lattice as it stands, before the flips of the
+    // chunk processed meanwhile (which starts at site c0prev, or -1): per site the
+    // spin, the energy change without / with the previous site of the sequence
+    // flipped, and for the neighbours lying in the chunk at c0prev (other than the
+    // previous site) their bit there and the correction 4 J s s_nbr if it flips.
+    int ns[SPL], nd0[SPL], nd1[SPL], nbit[SPL][2], ncoef[SPL][2], nwrap = 0;
+    auto prepare = [&](int y, int x0, int c0prev) {
+        const int row = y * L;
+        const int up = (y == 0 ? L - 1 : y - 1) * L, down = (y == L - 1 ? 0 : y + 1) * L;
+        nwrap = 0;
 #pragma unroll
-            for (int j = 0; j < C; ++j) {
-                const long long gn = gs[an];
-                int c0n = 0, c1n = 0, a0 = 0, a1 = 0;
-                bool i0 = false, i1 = false;
-                long long T1 = 0;
-                if (j + 1 < C) {
-                    const int pk1 = __shfl_sync(kFull, my_pk[(j + 1) / P], gbase + (j + 1) % P);
-                    T1 = __shfl_sync(kFull, my_T[(j + 1) / P], gbase + (j + 1) % P);
-                    const int wrapb = sx8(pk1 >> 16);
-                    const int w0 = (j == 0) ? 0 : ((acc & 1u) ? wrapb : 0);
-                    const int w1 = (j == 0) ? wrapb : ((acc & 1u) ? wrapb : 0);
-                    c0n = b + sx8(pk1) + w0;                  // step j rejected: stay, left not flipped
-                    c1n = bn + sx8(pk1 >> 8) + w1;            // step j accepted: move, left flipped
-                    i0 = (unsigned)c0n < (unsigned)nb;
-                    i1 = (unsigned)c1n < (unsigned)nb;
-                    a0 = i0 ? c0n : 0;
-                    a1 = i1 ? c1n : 0;
-                }
-                const bool a = in && (gn < gcT);
-                const long long gnew = a ? gn + lnf : gcL;
-                const int bnew = a ? bn : b;
-                gs[bnew] = gnew;
-                if (a) acc |= 1u << j;
-                b = bnew;
-                gc = gnew;
-                if (j + 1 < C) {
-                    bn = a ? c1n : c0n;
-                    in = a ? i1 : i0;
-                    an = a ? a1 : a0;
-                    gcT = gnew + T1;
-                    gcL = gnew + lnf;
-                }
+        for (int k = 0; k < SPL; ++k) {
+            const int jj = q + k * P;
+            ns[k] = 0; nd0[k] = 0; nd1[k] = 0;
+            nbit[k][0] = nbit[k][1] = -1; ncoef[k][0] = ncoef[k][1] = 0;
+            if (jj < C) {
+                const int x = x0 + jj;
+                const int xl = x == 0 ? L - 1 : x - 1, xr = x == L - 1 ? 0 : x + 1;
+                const int si = lat[row + x];
+                const int su = lat[up + x], sl = lat[row + xl], sr = lat[row + xr];
+                const int d0 = 2 * J * si * (su + sl + sr + lat[down + x]);
+                ns[k] = si;
+                nd0[k] = d0;
+                nd1[k] = x > 0 ? d0 - 4 * J * si * sl : d0;        // x > 0: the left site comes just before
+                if (jj == C - 1 && wraps) nwrap = -4 * J * si * sr;
+                const int ou = up + x - c0prev, orr = row + xr - c0prev;
+                if (c0prev >= 0 && (unsigned)ou < (unsigned)C) { nbit[k][0] = ou; ncoef[k][0] = 4 * J * si * su; }
+                if (c0prev >= 0 && xr == 0 && (unsigned)orr < (unsigned)C) { nbit[k][1] = orr; ncoef[k][1] = 4 * J * si * sr; }
             }
-            // apply the chunk's flips and the magnetisation change
+        }
+    };
+    // packed offsets of prepared site slot k once the bits of `acc` it depends on are known
+    auto finish = [&](int k, unsigned acc) {
+        int corr = 0;
+#pragma unroll
+        for (int n = 0; n < 2; ++n)
+            if (nbit[k][n] >= 0 && ((acc >> nbit[k][n]) & 1u)) corr += ncoef[k][n];
+        return pack_e(((nd0[k] - corr) >> sh) * 8, ((nd1[k] - corr) >> sh) * 8);
+    };
+
+    // ---- chunk 0 ----
+    int cs[SPL];                                        // spins of the current chunk
+    int E_[4];                                          // packed offsets of the first 4 sites of the chunk
+    long long T_[4];                                    // thresholds of the first 4 sites of the chunk
+    int cwrap;
+    draw(sweeps0 * (uint64_t)N, 0);
+    prepare(0, 0, -1);
+    {
+#pragma unroll
+        for (int k = 0; k < SPL; ++k) {
+            const int jj = q + k * P;
+            cs[k] = ns[k];
+            if (jj < C) Db[jj] = finish(k, 0u);
+        }
+        cwrap = __shfl_sync(kFull, (nwrap >> sh) * 8, gbase + (C - 1) % P);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { E_[i] = Db[i]; T_[i] = Tb[i]; }
+
+    int bc = b0 * 8;                                    // byte offset of the current bin
+    long long gcv = gs[b0];                             // g at the current bin
+    int bp = bc + e_lo(E_[0]);                          // site 0: proposal (left neighbour unprocessed)
+    long long LD = lds64(gsb, bp);                      // g at the proposed bin
+    int q0 = bc + e_lo(E_[1]), q1 = bp + e_hi(E_[1]);   // site 1 if site 0 is rejected / accepted
+    bool z0 = e_lo(E_[1]) == 0, z1 = e_hi(E_[1]) == 0;
+    long long l0 = lds64(gsb, q0), l1 = lds64(gsb, q1);
+    long long gcT = gcv - lnf + T_[0];                  // g at the current bin + threshold
+
+    const int nch = N / C;
+    const int total = p.nsweeps * nch;
+    int y = 0, x0 = 0;                                  // position of the current chunk
+    for (int t = 0; t < total; ++t) {
+        const int tn = t + 1;                           // the next chunk (wraps into the next sweep)
+        int yn = y, xn = x0 + C;
+        if (xn == L) { xn = 0; yn = y + 1 == L ? 0 : y + 1; }
+        const int c0 = y * L + x0;
+        const long long* Tc = Tb + ((t >> 2) & 1) * 4 * C + (t & 3) * C;
+        const long long* Tn = Tb + ((tn >> 2) & 1) * 4 * C + (tn & 3) * C;
+        const int* Dc = Db + (t & 1) * C;
+        int* Dn = Db + (tn & 1) * C;
+        if ((tn & 3) == 0 && tn < total) {
+            // the next chunk opens a batch: draw it now (its buffer is not in use)
+            const int swn = tn / nch;
+            draw((sweeps0 + (uint64_t)swn) * (uint64_t)N + (uint64_t)((tn - swn * nch) * C), (tn >> 2) & 1);
+            __syncwarp();
+        }
+        prepare(yn, xn, c0);
+        long long Tnext0 = Tn[0];
+
+        long long Tr[C + 1];
+        int Er[C];
+        Tr[0] = T_[0];
+#pragma unroll
+        for (int i = 1; i < 4; ++i) Tr[i] = T_[i];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Er[i] = E_[i];
+        unsigned acc = 0;
+#pragma unroll
+        for (int j = 0; j < C; ++j) {
+            if ((j & 1) == 0 && j + kAhead + 2 <= C) {
+                const int jn = j + kAhead;
+                const longlong2 tv = reinterpret_cast<const longlong2*>(Tc)[jn >> 1];
+                Tr[jn] = tv.x; Tr[jn + 1] = tv.y;
+                const int2 d = reinterpret_cast<const int2*>(Dc)[jn >> 1];
+                Er[jn] = d.x; Er[jn + 1] = d.y;
+            }
+            if (j == C - 1) Tr[C] = Tnext0;
+            const bool a = LD < gcT;
+            const long long sel = a ? LD : gcv;
+            const long long gnew = sel + lnf;
+            const int bnew = a ? bp : bc;
+            *reinterpret_cast<long long*>(gsb + bnew) = gnew;
+            if (a) acc |= 1u << j;
+            if (j == 1 || j == 3) {
+                // next chunk's sites j-1, j: the neighbours they have in this chunk are decided
+#pragma unroll
+                for (int i = j - 1; i <= j; ++i)
+                    E_[i] = __shfl_sync(kFull, finish(i / P, acc), gbase + i % P);
+            }
+            gcT = sel + Tr[j + 1];                     // gnew + threshold of site j+1
+            const bool zs = a ? z1 : z0;               // the prefetch read the bin just committed
+            const long long lt = a ? l1 : l0;
+            LD = zs ? gnew : lt;
+            bp = a ? q1 : q0;
+            int ev = (j + 2 < C) ? Er[j + 2] : E_[j + 2 - C];
+            int e0 = e_lo(ev), e1 = e_hi(ev);
+            if (j + 2 == C - 1) {                      // a row's last site sees the row start
+                const int wv = (wraps && (acc & 1u)) ? cwrap : 0;
+                e0 += wv; e1 += wv;
+            }
+            q0 = bnew + e0;
+            q1 = bp + e1;
+            z0 = e0 == 0;
+            z1 = e1 == 0;
+            l0 = lds64(gsb, q0);
+            l1 = lds64(gsb, q1);
+            bc = bnew;
+            gcv = gnew;
+        }
+        // apply the chunk's flips and the magnetisation change
+        {
             unsigned plus = 0;
 #pragma unroll
             for (int k = 0; k < SPL; ++k) {
                 const int jj = q + k * P;
-                const unsigned bal = __ballot_sync(kFull, jj < C && my_s[k] > 0);
+                const unsigned bal = __ballot_sync(kFull, jj < C && cs[k] > 0);
                 const unsigned mine = P == 32 ? bal : ((bal >> gbase) & ((1u << P) - 1u));
                 plus |= (k * P < 32) ? (mine << (k * P)) : 0u;
-                if (jj < C && ((acc >> jj) & 1u)) lat[row + x0 + jj] = (int8_t)(-my_s[k]);
+                if (jj < C && ((acc >> jj) & 1u)) lat[c0 + jj] = (int8_t)(-cs[k]);
             }
             const unsigned full = C == 32 ? 0xFFFFFFFFu : ((1u << C) - 1u);
             M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus & full));
-            __syncwarp();
         }
+        // publish the next chunk: spins, offsets, wrap term, first thresholds
+#pragma unroll
+        for (int k = 0; k < SPL; ++k) {
+            const int jj = q + k * P;
+            cs[k] = ns[k];
+            if (jj < C) Dn[jj] = finish(k, acc);
+        }
+        cwrap = __shfl_sync(kFull, (nwrap >> sh) * 8, gbase + (C - 1) % P);
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < 4; ++i) T_[i] = Tn[i];
+        y = yn; x0 = xn;
     }
+    __syncwarp();
     if (valid) {
         for (int i = q; i < N; i += P) gl[i] = lat[i];
         uint32_t* gH = P_.H + P_.slot_tab[s];
@@ -680,7 +818,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             gg[k] = gnew;
         }
         if (q == 0) {
-            P_.cfg_E[cfg] = (long long)Ewlo + ((long long)b << sh);
+            P_.cfg_E[cfg] = (long long)Ewlo + ((long long)(bc >> 3) << sh);
             P_.cfg_M[3 * cfg] = M;
             P_.slot_sweeps[s] = sweeps0 + (uint64_t)p.nsweeps;
         }
@@ -1441,24 +1579,32 @@ bool bins_eligible(const InstDev& I, const rewl_batch_desc& D)
     if (!(C == 32 || C == 24 || C == 16 || C == 8 || C == 4)) return false;
     const long long step = 4 * std::llabs(I.J_u);            // every energy change is a multiple of 4|J|
     if (step % (1LL << I.bin_shift) != 0) return false;
-    if (8 * std::llabs(I.J_u) >> I.bin_shift > 60) return false;   // bin changes fit a signed byte (with margin)
+    // the thresholds are drawn four sites per Philox block, 4C sites at a time
+    if (I.N % (4 * C) != 0) return false;
+    // a proposal lands at most 8|J| / width bins away, and a prefetch issued from an
+    // out-of-window proposal twice that: the guard bins cover both
+    const long long maxbins = (8 * std::llabs(I.J_u)) >> I.bin_shift;
+    if (2 * maxbins > kGuard) return false;
     return true;
 }
 
 int plan_launches(rewl_engine* e)
 {
     const int nsm = 152;
-    // group walkers by (model, bin-tracking kernel, chunk) so each launch has one kernel shape
-    struct Key { int model, bins, chunk; };
+    // group walkers by (model, bin-tracking kernel, chunk, sites) so each launch has one
+    // kernel shape and the walkers sharing a warp run the same number of chunks
+    struct Key { int model, bins, chunk, sites; };
     std::vector<Key> keys;
     std::vector<Launch> plans;
     for (int s = 0; s < e->nslots; ++s) {
         const HostInst& H = e->inst[e->h_slot_inst[s]];
         const int bins = bins_eligible(H.dev, e->desc) && getenv("REWL_SWEEP_VARIANT") == nullptr ? 1 : 0;
-        Key k{H.d.model, bins, bins ? H.dev.chunk : 0};
+        Key k{H.d.model, bins, bins ? H.dev.chunk : 0, bins ? H.dev.N : 0};
         size_t idx = 0;
         for (; idx < keys.size(); ++idx)
-            if (keys[idx].model == k.model && keys[idx].bins == k.bins && keys[idx].chunk == k.chunk) break;
+            if (keys[idx].model == k.model && keys[idx].bins == k.bins && keys[idx].chunk == k.chunk &&
+                keys[idx].sites == k.sites)
+                break;
         if (idx == keys.size()) {
             keys.push_back(k);
             Launch l;
@@ -1483,7 +1629,7 @@ int plan_launches(rewl_engine* e)
             }
             l.walkers_per_warp = G;
             l.nbcap = (maxnb + 1) & ~1;
-            int raw = l.nbcap * 8 + ((maxN + 15) & ~15);
+            int raw = (((l.nbcap + 2 * kGuard) * 8 + 15) & ~15) + ((maxN + 15) & ~15) + 8 * l.chunk * 8 + 2 * l.chunk * 4;
             l.smem_per_warp = ((raw + 127) & ~127) + 16;           // per walker; +16 skews the walkers' banks
             if ((size_t)l.smem_per_warp * G > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory", l.smem_per_warp);
             int wpb = e->desc.warps_per_block;
