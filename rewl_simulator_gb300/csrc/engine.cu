@@ -560,9 +560,7 @@ __device__ __forceinline__ long long lds64(const char* base, int off)
 {
     return *reinterpret_cast<const long long*>(base + off);
 }
-__device__ __forceinline__ int pack_e(int e0, int e1) { return (e0 & 0xFFFF) | (e1 << 16); }
-__device__ __forceinline__ int e_lo(int v) { return (int)(short)(v & 0xFFFF); }
-__device__ __forceinline__ int e_hi(int v) { return v >> 16; }
+__device__ __forceinline__ void sts64(char* base, int off, long long v) { *reinterpret_cast<long long*>(base + off) = v; }
 
 template <int G, int C>
 __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
@@ -589,8 +587,11 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     long long* gs = reinterpret_cast<long long*>(base) + kGuard;     // gs[-kGuard .. nb+kGuard)
     int8_t* lat = reinterpret_cast<int8_t*>(base + gs_bytes);
     long long* Tb = reinterpret_cast<long long*>(base + gs_bytes + ((N + 15) & ~15));   // 2 x 4C thresholds
-    int* Db = reinterpret_cast<int*>(Tb + 8 * C);                                     // 2 x C packed offsets
-    char* const gsb = reinterpret_cast<char*>(gs);
+    int2* Db = reinterpret_cast<int2*>(Tb + 8 * C);                                   // 2 x C offset pairs
+    // table positions are byte offsets from the start of shared memory, so that the
+    // accesses need no address arithmetic
+    char* const sm = reinterpret_cast<char*>(smem);
+    const int gsoff = (int)(reinterpret_cast<char*>(gs) - sm);
 
     const int cfg = P_.slot_cfg[s];
     int8_t* gl = P_.spins + P_.cfg_off[cfg];
@@ -669,18 +670,18 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             }
         }
     };
-    // packed offsets of prepared site slot k once the bits of `acc` it depends on are known
+    // offsets of prepared site slot k once the bits of `acc` it depends on are known
     auto finish = [&](int k, unsigned acc) {
         int corr = 0;
 #pragma unroll
         for (int n = 0; n < 2; ++n)
             if (nbit[k][n] >= 0 && ((acc >> nbit[k][n]) & 1u)) corr += ncoef[k][n];
-        return pack_e(((nd0[k] - corr) >> sh) * 8, ((nd1[k] - corr) >> sh) * 8);
+        return make_int2(((nd0[k] - corr) >> sh) * 8, ((nd1[k] - corr) >> sh) * 8);
     };
 
     // ---- chunk 0 ----
     int cs[SPL];                                        // spins of the current chunk
-    int E_[4];                                          // packed offsets of the first 4 sites of the chunk
+    int2 E_[4];                                         // offsets of the first 4 sites of the chunk
     long long T_[4];                                    // thresholds of the first 4 sites of the chunk
     int cwrap;
     draw(sweeps0 * (uint64_t)N, 0);
@@ -698,13 +699,12 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
 #pragma unroll
     for (int i = 0; i < 4; ++i) { E_[i] = Db[i]; T_[i] = Tb[i]; }
 
-    int bc = b0 * 8;                                    // byte offset of the current bin
+    int bc = gsoff + b0 * 8;                            // shared offset of the current bin
     long long gcv = gs[b0];                             // g at the current bin
-    int bp = bc + e_lo(E_[0]);                          // site 0: proposal (left neighbour unprocessed)
-    long long LD = lds64(gsb, bp);                      // g at the proposed bin
-    int q0 = bc + e_lo(E_[1]), q1 = bp + e_hi(E_[1]);   // site 1 if site 0 is rejected / accepted
-    bool z0 = e_lo(E_[1]) == 0, z1 = e_hi(E_[1]) == 0;
-    long long l0 = lds64(gsb, q0), l1 = lds64(gsb, q1);
+    int bp = bc + E_[0].x;                              // site 0: proposal (left neighbour unprocessed)
+    long long LD = lds64(sm, bp);                       // g at the proposed bin
+    int q0 = bc + E_[1].x, q1 = bp + E_[1].y;           // site 1 if site 0 is rejected / accepted
+    long long l0 = lds64(sm, q0), l1 = lds64(sm, q1);
     long long gcT = gcv - lnf + T_[0];                  // g at the current bin + threshold
 
     const int nch = N / C;
@@ -717,8 +717,8 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
         const int c0 = y * L + x0;
         const long long* Tc = Tb + ((t >> 2) & 1) * 4 * C + (t & 3) * C;
         const long long* Tn = Tb + ((tn >> 2) & 1) * 4 * C + (tn & 3) * C;
-        const int* Dc = Db + (t & 1) * C;
-        int* Dn = Db + (tn & 1) * C;
+        const int2* Dc = Db + (t & 1) * C;
+        int2* Dn = Db + (tn & 1) * C;
         if ((tn & 3) == 0 && tn < total) {
             // the next chunk opens a batch: draw it now (its buffer is not in use)
             const int swn = tn / nch;
@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
         long long Tnext0 = Tn[0];
 
         long long Tr[C + 1];
-        int Er[C];
+        int2 Er[C];
         Tr[0] = T_[0];
 #pragma unroll
         for (int i = 1; i < 4; ++i) Tr[i] = T_[i];
@@ -742,39 +742,38 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                 const int jn = j + kAhead;
                 const longlong2 tv = reinterpret_cast<const longlong2*>(Tc)[jn >> 1];
                 Tr[jn] = tv.x; Tr[jn + 1] = tv.y;
-                const int2 d = reinterpret_cast<const int2*>(Dc)[jn >> 1];
-                Er[jn] = d.x; Er[jn + 1] = d.y;
+                const int4 d = reinterpret_cast<const int4*>(Dc)[jn >> 1];
+                Er[jn] = make_int2(d.x, d.y); Er[jn + 1] = make_int2(d.z, d.w);
             }
             if (j == C - 1) Tr[C] = Tnext0;
             const bool a = LD < gcT;
             const long long sel = a ? LD : gcv;
             const long long gnew = sel + lnf;
             const int bnew = a ? bp : bc;
-            *reinterpret_cast<long long*>(gsb + bnew) = gnew;
+            sts64(sm, bnew, gnew);
             if (a) acc |= 1u << j;
             if (j == 1 || j == 3) {
                 // next chunk's sites j-1, j: the neighbours they have in this chunk are decided
 #pragma unroll
-                for (int i = j - 1; i <= j; ++i)
-                    E_[i] = __shfl_sync(kFull, finish(i / P, acc), gbase + i % P);
+                for (int i = j - 1; i <= j; ++i) {
+                    const int2 v = finish(i / P, acc);
+                    E_[i] = make_int2(__shfl_sync(kFull, v.x, gbase + i % P), __shfl_sync(kFull, v.y, gbase + i % P));
+                }
             }
             gcT = sel + Tr[j + 1];                     // gnew + threshold of site j+1
-            const bool zs = a ? z1 : z0;               // the prefetch read the bin just committed
-            const long long lt = a ? l1 : l0;
-            LD = zs ? gnew : lt;
             bp = a ? q1 : q0;
-            int ev = (j + 2 < C) ? Er[j + 2] : E_[j + 2 - C];
-            int e0 = e_lo(ev), e1 = e_hi(ev);
+            const long long lt = a ? l1 : l0;
+            LD = bp == bnew ? gnew : lt;               // the prefetch read the bin just committed
+            const int2 ev = (j + 2 < C) ? Er[j + 2] : E_[j + 2 - C];
+            int e0 = ev.x, e1 = ev.y;
             if (j + 2 == C - 1) {                      // a row's last site sees the row start
                 const int wv = (wraps && (acc & 1u)) ? cwrap : 0;
                 e0 += wv; e1 += wv;
             }
             q0 = bnew + e0;
             q1 = bp + e1;
-            z0 = e0 == 0;
-            z1 = e1 == 0;
-            l0 = lds64(gsb, q0);
-            l1 = lds64(gsb, q1);
+            l0 = lds64(sm, q0);
+            l1 = lds64(sm, q1);
             bc = bnew;
             gcv = gnew;
         }
@@ -818,7 +817,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             gg[k] = gnew;
         }
         if (q == 0) {
-            P_.cfg_E[cfg] = (long long)Ewlo + ((long long)(bc >> 3) << sh);
+            P_.cfg_E[cfg] = (long long)Ewlo + ((long long)((bc - gsoff) >> 3) << sh);
             P_.cfg_M[3 * cfg] = M;
             P_.slot_sweeps[s] = sweeps0 + (uint64_t)p.nsweeps;
         }
@@ -1629,7 +1628,7 @@ int plan_launches(rewl_engine* e)
             }
             l.walkers_per_warp = G;
             l.nbcap = (maxnb + 1) & ~1;
-            int raw = (((l.nbcap + 2 * kGuard) * 8 + 15) & ~15) + ((maxN + 15) & ~15) + 8 * l.chunk * 8 + 2 * l.chunk * 4;
+            int raw = (((l.nbcap + 2 * kGuard) * 8 + 15) & ~15) + ((maxN + 15) & ~15) + 8 * l.chunk * 8 + 2 * l.chunk * 8;
             l.smem_per_warp = ((raw + 127) & ~127) + 16;           // per walker; +16 skews the walkers' banks
             if ((size_t)l.smem_per_warp * G > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory", l.smem_per_warp);
             int wpb = e->desc.warps_per_block;
