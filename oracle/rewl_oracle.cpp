@@ -430,16 +430,19 @@ static inline void set_flavour(Ising&, int) {}
 static inline void set_flavour(AshkinTeller& m, int f) { m.st.which = f; }
 
 // adjust_state_to_range (src/REWL/rewl_walker.hpp:79-115); returns false when
-// the deterministic walk did not reach the window within max_steps.
+// the deterministic walk did not reach the window within max_steps.  Without a
+// flip the walk's next decisions depend only on (site, flavour), which repeat
+// within 2N steps, so 2N steps without a flip mean it can never move again: it
+// stops there with the same outcome it would reach at max_steps.
 template <class M> static bool adjust(Sim<M>& S, Walker<M>& w, size_t start_site, size_t max_steps)
 {
     const size_t N = w.sys.N;
     size_t site = start_site;
     bool in = S.in_range(w, w.sys.st.energy);
-    size_t steps = 0;
+    size_t steps = 0, idle = 0;
     while (!in)
     {
-        if (++steps > max_steps) return false;
+        if (++steps > max_steps || ++idle > 2 * N) return false;
         ++site;
         if (site == N) { site = 0; w.sys.switch_flavor(); }
         typename std::conditional<std::is_same<M, Ising>::value, IsingState, ATState>::type t;
@@ -447,8 +450,7 @@ template <class M> static bool adjust(Sim<M>& S, Walker<M>& w, size_t start_site
         const double e = w.sys.st.energy;
         const int64_t g = S.gbin(e);
         const bool too_low = g < w.gb_lo, too_high = g >= w.gb_lo + (int64_t)w.nb;
-        if (too_low && t.energy > e) w.sys.set_state(site, t);
-        else if (too_high && t.energy <= e) w.sys.set_state(site, t);
+        if ((too_low && t.energy > e) || (too_high && t.energy <= e)) { w.sys.set_state(site, t); idle = 0; }
         in = S.in_range(w, w.sys.st.energy);
     }
     return true;

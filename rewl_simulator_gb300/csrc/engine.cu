@@ -69,7 +69,11 @@ int fail(int code, const char* fmt, ...)
 constexpr int kMaxReplicas = 32;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 
-enum : int { ERR_BOUNDS = 1, ERR_ADJUST = 2, ERR_REPLAY_EXHAUSTED = 4 };
+enum : int { ERR_BOUNDS = 1, ERR_ADJUST = 2, ERR_REPLAY_EXHAUSTED = 4, ERR_RANGE = 8 };
+// |logDoS| beyond which a window is reported instead of risking int64 overflow: 2^62 units
+// (4.2e6 nats) leaves 4.2e6 nats of headroom, more than one check interval can add to a bin
+// at ln f = 1 in the configured workloads (sweeps_per_check x N visits per walker)
+constexpr long long kLogdosLimit = 1LL << 62;
 
 struct InstDev {
     int32_t model, L, N, ndof;
@@ -187,9 +191,10 @@ __device__ bool adjust_walk(const InstDev& I, const WinDev& W, int8_t* sp, int64
     auto in_range = [&](int64_t e) { const int64_t b = global_bin(I, e) - W.gblo; return b >= 0 && b < W.nb; };
     bool in = in_range(E);
     int site = (int)start;
-    int64_t steps = 0;
+    int64_t steps = 0, idle = 0;
     while (!in) {
-        if (++steps > max_steps) return false;
+        // without a flip the decisions repeat within 2N steps: the walk is stuck for good
+        if (++steps > max_steps || ++idle > 2 * (int64_t)N) return false;
         ++site;
         if (site == N) { site = 0; flavour ^= 1; }
         int64_t dE;
@@ -210,6 +215,7 @@ __device__ bool adjust_walk(const InstDev& I, const WinDev& W, int8_t* sp, int64
         const int64_t En = E + dE;
         if ((too_low && En > E) || (too_high && En <= E)) {
             E = En;
+            idle = 0;
             if (I.model == REWL_MODEL_ISING2D) { M[0] -= 2 * a[site]; a[site] = (int8_t)-a[site]; }
             else {
                 // flavour was possibly toggled above; the flipped plane is the one chosen before the toggle
@@ -543,9 +549,10 @@ struct __align__(16) SiteRec {
 // its proposal keeps the bin (offset change 0); the value is then the one just
 // committed.
 //
-// The table carries kGuard sentinel bins on each side holding 2^62, so a
-// proposal outside the window fails the compare by itself (no range checks),
-// and prefetches issued from such a proposal stay inside the table.  Bin
+// The table carries kGuard sentinel bins on each side holding INT64_MAX, so a
+// proposal outside the window fails the compare by itself whatever g holds (no
+// range checks): the current bin never leaves the window, and prefetches issued
+// from an out-of-window proposal stay inside the table.  Bin
 // positions are byte offsets into the table.
 //
 // The chain runs without a break from chunk to chunk: the first offsets of the
@@ -554,7 +561,7 @@ struct __align__(16) SiteRec {
 // decided, and handed to all lanes by shuffle; thresholds come from one Philox
 // block per four sites, 4C sites at a time, one batch ahead.
 constexpr int kGuard = 8;
-constexpr long long kGuardValue = 1LL << 62;
+constexpr long long kGuardValue = 0x7FFFFFFFFFFFFFFFLL;   // never below g + threshold
 
 __device__ __forceinline__ long long lds64(const char* base, int off)
 {
@@ -817,6 +824,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             gg[k] = gnew;
         }
         if (q == 0) {
+            if ((unsigned)(bc - gsoff) >= (unsigned)(nb * 8)) atomicOr(&P_.counters[0], ERR_BOUNDS);
             P_.cfg_E[cfg] = (long long)Ewlo + ((long long)((bc - gsoff) >> 3) << sh);
             P_.cfg_M[3 * cfg] = M;
             P_.slot_sweeps[s] = sweeps0 + (uint64_t)p.nsweeps;
@@ -1123,8 +1131,12 @@ __global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
 
     for (int r = 0; r < R; ++r) {
         const uint32_t* H = P.H + P.slot_tab[first + r];
-        unsigned long long mn = ~0ull, mx = 0, sum = 0, n = 0, zero = 0;
+        const int64_t* g = P.g + P.slot_tab[first + r];
+        unsigned long long mn = ~0ull, mx = 0, sum = 0, n = 0, zero = 0, big = 0;
         for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            // a window that never goes flat (a replica trapped away from part of its
+            // range) lets ln g grow without bound: report it before int64 overflows
+            big |= (unsigned long long)(g[b] > kLogdosLimit || g[b] < -kLogdosLimit);
             if (!bin_valid(P, W, first, R, b, fp.mask_mode)) continue;
             const unsigned long long h = H[b];
             mn = h < mn ? h : mn; mx = h > mx ? h : mx; sum += h; ++n; zero += (h == 0);
@@ -1134,7 +1146,9 @@ __global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
         sum = block_reduce(sum, OpAdd(), red_u, 0ull);
         n = block_reduce(n, OpAdd(), red_u, 0ull);
         zero = block_reduce(zero, OpAdd(), red_u, 0ull);
+        big = block_reduce(big, OpMax(), red_u, 0ull);
         if (threadIdx.x == 0) {
+            if (big) atomicOr(&P.counters[0], ERR_RANGE);
             bool f;
             if (fp.flat_mode == REWL_FLAT_ALL_VISITED) f = P.win_oot[w] ? true : (zero == 0);
             else if (n == 0 || mn == 0) f = false;
@@ -1676,6 +1690,9 @@ int check_device_error(rewl_engine* e)
     if (h[0] & ERR_BOUNDS) return fail(REWL_EBOUNDS, "a walker's energy left its window (device error word %d)", h[0]);
     if (h[0] & ERR_ADJUST) return fail(REWL_EINVAL, "a walker could not reach its window");
     if (h[0] & ERR_REPLAY_EXHAUSTED) return fail(REWL_EINVAL, "replay uniform stream exhausted");
+    if (h[0] & ERR_RANGE)
+        return fail(REWL_ESTATE, "a window's logDoS passed 2^62 units (4.2e6 nats) without a flat event: "
+                                 "a replica is trapped away from part of its window");
     return REWL_OK;
 }
 
