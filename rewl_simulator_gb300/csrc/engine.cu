@@ -1024,7 +1024,9 @@ __global__ void k_exchange(DevPtrs P, const int32_t* pairs, int npairs, uint64_t
     const int R = I.R;
     int perm[kMaxReplicas];
     for (int r = 0; r < R; ++r) perm[r] = r;
-    const uint32_t xuid = 0x80000000u | (uint32_t)ii;
+    // keyed by the instance's own seed only, like its sweeps: an instance's trajectory does not
+    // depend on the other instances of the batch or on its position among them
+    const uint32_t xuid = 0x80000000u;
     const uint32_t w3 = (uint32_t)((round << 8) ^ (uint64_t)lw);
     for (int i = R - 1; i >= 1; --i) {
         const uint32_t word = philox_word(I.seed, xuid, (uint64_t)(R - 1 - i), kStreamExchange, w3);

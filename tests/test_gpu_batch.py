@@ -1,0 +1,73 @@
+"""Uneven batches: instances of different models, sizes and bin widths in one engine.
+
+Every random stream of an instance (initial spins, sweeps, exchange pairing and
+acceptance) is keyed by that instance's own seed and instance-relative walker
+index, and exchange, flatness and ln f act within an instance.  So an instance
+run inside a mixed batch must follow exactly the trajectory of the same instance
+run alone: here each one is compared bit for bit with its own CPU oracle after
+every check interval.
+"""
+import numpy as np
+import pytest
+
+SE, SC, LNF_FINAL = 20, 40, 1e-7
+
+# name, model, L, K, sigma_h, emin, emax, bw, nwin, R, seed
+INSTANCES = [
+    ("ising_L8", 0, 8, 0.0, 0.0, -128.0, 132.0, 4.0, 3, 2, 11),
+    ("ising_L12_bw8", 0, 12, 0.0, 0.0, -288.0, 296.0, 8.0, 4, 2, 3),      # general sweep kernel
+    ("at_L4_rf", 1, 4, 0.5, 0.5, -(2.5) * 2 * 16, 0.0, 0.05, 2, 2, 7),
+    ("ising_L16", 0, 16, 0.0, 0.0, -512.0, 516.0, 4.0, 4, 3, 17),
+]
+
+
+@pytest.mark.gpu
+def test_mixed_batch_instances_match_their_oracles(engine_lib, oracle_lib):
+    rg, po = engine_lib, oracle_lib
+    inss, orcs = [], []
+    for name, model, L, K, sig, emin, emax, bw, nwin, R, seed in INSTANCES:
+        N = L * L
+        fields = None
+        if sig > 0:
+            fields = np.round(np.random.default_rng(seed).normal(0, sig, N) * 2**20) / 2**20
+        inss.append(rg.Instance(model=model, L=L, K=K, fields=fields, energy_min=emin, energy_max=emax, bin_width=bw,
+                                num_windows=nwin, replicas_per_window=R, window_overlap=0.75, init_mode=0, seed=seed))
+        cfg = po.Config(model=model, L=L, K=K, escale_bits=0 if model == 0 else 20, nwin=nwin, R=R,
+                        sweeps_per_exchange=SE, sweeps_per_check=SC, emin=emin, emax=emax, bw=bw, overlap=0.75,
+                        lnf0=1.0, lnf_final=LNF_FINAL, flat_param=0.8, mask_mode=po.MASK_VISITED,
+                        semantics=po.SEM_ENGINE, seed=seed)
+        orcs.append(po.Oracle(cfg, fields=fields))
+    b = rg.Batch(instances=inss, sweeps_per_exchange=SE, sweeps_per_check=SC, flatness_param=0.8,
+                 lnf_initial=1.0, lnf_final=LNF_FINAL, mask_mode=rg.MASK_VISITED)
+    eng = rg.Engine(b)
+    try:
+        def compare(tag):
+            for i, (spec, orc) in enumerate(zip(INSTANCES, orcs)):
+                nwin, R = spec[8], spec[9]
+                for w in range(nwin):
+                    for r in range(R):
+                        out = eng.export_walker(eng.walker_id(i, w, r))
+                        s = w * R + r
+                        c, g, v = orc.tables(s)
+                        msg = f"{tag} {spec[0]} window {w} replica {r}"
+                        np.testing.assert_array_equal(out["dofs"], orc.dofs(s), err_msg=msg + " dofs")
+                        np.testing.assert_array_equal(out["state"], orc.state(s), err_msg=msg + " state")
+                        np.testing.assert_array_equal(out["counts"], c, err_msg=msg + " counts")
+                        np.testing.assert_array_equal(out["logdos"], g, err_msg=msg + " logdos")
+                    lnf, done = eng.window_state(i, w)
+                    assert lnf == orc.lnf(w * R), f"{tag} {spec[0]} window {w} lnf"
+                    assert done == bool(orc.done_flags()[w]), f"{tag} {spec[0]} window {w} done"
+
+        compare("init")
+        for k in range(4):
+            eng.run_cycles(1)
+            for orc in orcs:
+                orc.cycle()
+            compare(f"cycle {k}")
+        st = eng.status()
+        assert st.exchanges_attempted == sum(o.exchange_stats()[0] for o in orcs)
+        assert st.exchanges_accepted == sum(o.exchange_stats()[1] for o in orcs)
+    finally:
+        eng.close()
+        for o in orcs:
+            o.close()
