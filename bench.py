@@ -44,12 +44,46 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "time to ln g within 1e-2 of exact, MLP warm-start vs plain WL, 1 GB300; flips/s"
-WORKLOAD = dict(name="ising2d_L32_16win_x8walkers_rewl", model="ising2d", L=32, energy_min=-2048.0,
-                energy_max=2052.0, bin_width=4.0, num_windows=16, replicas_per_window=8, window_overlap=0.75,
-                sweeps_per_exchange=500, sweeps_per_check=1000, lnf_initial=1.0, lnf_final=1e-8,
-                flatness="min >= 0.8 mean over valid bins")
-BYTES_PER_FLIP = 46        # algorithmic bytes per attempted Ising flip (5+1 B spins, 24 B logDoS, 16 B histogram)
-FLIPS_PER_STEP = WORKLOAD["sweeps_per_check"] * WORKLOAD["num_windows"] * WORKLOAD["replicas_per_window"] * 32 * 32
+WORKLOADS = {
+    # the headline configuration (default)
+    "ising": dict(name="ising2d_L32_16win_x8walkers_rewl", model="ising2d", L=32, energy_min=-2048.0,
+                  energy_max=2052.0, bin_width=4.0, num_windows=16, replicas_per_window=8, window_overlap=0.75,
+                  sweeps_per_exchange=500, sweeps_per_check=1000, lnf_initial=1.0, lnf_final=1e-8,
+                  flatness="min >= 0.8 mean over valid bins", realizations=1,
+                  bytes_per_flip=46, kernel="k_sweep_ising_bins", profile="sweep_ising_L32_rewl.md"),
+    # 2D Ashkin-Teller, K = 0.5, Gaussian Baxter fields (sigma 0.5), 64 realisations x 8 windows x 4 walkers
+    "at": dict(name="ashkin_teller2d_L32_K0.5_h0.5_64real_8win_x4walkers_rewl", model="ashkin_teller2d", L=32, K=0.5,
+               sigma_h=0.5, energy_min=-5120.0, energy_max=0.0, bin_width=0.05, num_windows=8, replicas_per_window=4,
+               window_overlap=0.75, sweeps_per_exchange=100, sweeps_per_check=200, lnf_initial=1.0, lnf_final=1e-7,
+               flatness="min >= 0.8 mean over visited bins", realizations=64,
+               bytes_per_flip=51, kernel="k_sweep_at", profile="sweep_at_L32_64real_rewl.md"),
+}
+WORKLOAD = WORKLOADS["ising"]
+
+
+def select_workload(name: str) -> None:
+    global WORKLOAD
+    WORKLOAD = WORKLOADS[name]
+
+
+def step_text() -> str:
+    w = WORKLOAD
+    k = w["sweeps_per_check"] // w["sweeps_per_exchange"]
+    return f"one check interval: {k} x ({w['sweeps_per_exchange']} sweeps + exchange) + flatness/averaging/ln f"
+
+
+def ndof(w) -> int:
+    return w["L"] ** 2 * (2 if w["model"] == "ashkin_teller2d" else 1)
+
+
+def flips_per_sweep(w) -> int:
+    return w["realizations"] * w["num_windows"] * w["replicas_per_window"] * ndof(w)
+
+
+def at_fields(w, k: int) -> np.ndarray:
+    """Gaussian Baxter fields of realisation k, rounded to multiples of 2^-20."""
+    h = np.random.default_rng(100 + k).normal(0.0, w["sigma_h"], w["L"] ** 2)
+    return np.round(h * 2**20) / 2**20
 
 
 def dist_env():
@@ -66,7 +100,7 @@ def peaks():
 
 def traffic_per_launch():
     """dram bytes per sweep-kernel launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "sweep_ising_L32_rewl.md"
+    p = ROOT / "profiles" / WORKLOAD["profile"]
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -133,30 +167,41 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_batch(rg, seed: int, device: int, schedule: str = "halving"):
+def make_batch(rg, seed: int, device: int):
     w = WORKLOAD
-    ins = rg.Instance(model=rg.MODEL_ISING2D, L=w["L"], energy_min=w["energy_min"], energy_max=w["energy_max"],
-                      bin_width=w["bin_width"], num_windows=w["num_windows"],
-                      replicas_per_window=w["replicas_per_window"], window_overlap=w["window_overlap"], seed=seed)
-    one_over_t = schedule == "1/t"
-    return rg.Batch(instances=[ins], sweeps_per_exchange=w["sweeps_per_exchange"],
+    if w["model"] == "ising2d":
+        inss = [rg.Instance(model=rg.MODEL_ISING2D, L=w["L"], energy_min=w["energy_min"], energy_max=w["energy_max"],
+                            bin_width=w["bin_width"], num_windows=w["num_windows"],
+                            replicas_per_window=w["replicas_per_window"], window_overlap=w["window_overlap"],
+                            seed=seed)]
+        mask = rg.MASK_STATIC
+    else:
+        inss = [rg.Instance(model=rg.MODEL_ASHKIN_TELLER2D, L=w["L"], K=w["K"], fields=at_fields(w, k),
+                            energy_min=w["energy_min"], energy_max=w["energy_max"], bin_width=w["bin_width"],
+                            num_windows=w["num_windows"], replicas_per_window=w["replicas_per_window"],
+                            window_overlap=w["window_overlap"], seed=seed * 1000 + k)
+                for k in range(w["realizations"])]
+        mask = rg.MASK_VISITED
+    return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
                     sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
-                    lnf_final=w["lnf_final"], device=device, one_over_t=int(one_over_t),
-                    flatness_mode=rg.FLAT_ALL_VISITED if one_over_t else rg.FLAT_MIN_OVER_MEAN)
+                    lnf_final=w["lnf_final"], device=device, mask_mode=mask)
 
 
 # --------------------------------------------------------------------------- CPU leg
 def cpu_port_rate(target_seconds: float, threads: int, steps: int | None = None, warmup: int = 0):
-    """Flips/s of the oracle port (reference semantics) on `threads` host threads."""
+    """Flips/s of the oracle port (reference semantics) on `threads` host threads (one instance:
+    the port drives one instance at a time, so for a batch of realisations it times one of them)."""
     from oracle import pyoracle as po
     w = WORKLOAD
-    cfg = po.Config(model=po.MODEL_ISING, L=w["L"], nwin=w["num_windows"], R=w["replicas_per_window"],
+    at = w["model"] != "ising2d"
+    cfg = po.Config(model=po.MODEL_AT if at else po.MODEL_ISING, L=w["L"], K=w.get("K", 0.0),
+                    escale_bits=20 if at else 0, nwin=w["num_windows"], R=w["replicas_per_window"],
                     sweeps_per_exchange=w["sweeps_per_exchange"], sweeps_per_check=w["sweeps_per_check"],
                     emin=w["energy_min"], emax=w["energy_max"], bw=w["bin_width"], overlap=w["window_overlap"],
                     lnf0=w["lnf_initial"], lnf_final=w["lnf_final"], semantics=po.SEM_REFERENCE, nthreads=threads,
-                    seed=2024)
-    orc = po.Oracle(cfg)
-    flips_per_sweep = w["num_windows"] * w["replicas_per_window"] * w["L"] ** 2
+                    mask_mode=po.MASK_VISITED if at else po.MASK_STATIC, seed=2024)
+    orc = po.Oracle(cfg, fields=at_fields(w, 0) if at else None)
+    flips_per_sweep = w["num_windows"] * w["replicas_per_window"] * ndof(w)
     for _ in range(warmup):
         orc.run_sweeps(w["sweeps_per_exchange"])
     times = []
@@ -183,15 +228,17 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
+    w = WORKLOAD
     rate, n, total, times = cpu_port_rate(0, threads, steps=args.steps, warmup=args.warmup)
     line = {
         "metric": METRIC, "value": rate, "unit": "flips/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / n, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": WORKLOAD["name"], **{k: v for k, v in WORKLOAD.items() if k != "name"},
-                   "step": "one check interval: 2 x (500 sweeps + exchange) + flatness/averaging/ln f"},
+                   "step": step_text()},
         "cpu_baseline": {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} check intervals of the full workload (each 1000 sweeps x 128 walkers)"},
+                         "sample": f"{n} check intervals of one instance of the workload "
+                                   f"({w['num_windows'] * w['replicas_per_window']} walkers, {w['sweeps_per_check']} sweeps each)"},
         "e2e": {"value": rate, "unit": "flips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -372,12 +419,13 @@ def run_gpu(args):
         eng.snapshot_into(host.data_ptr(), nbytes)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    e2e_rate = e2e_steps * FLIPS_PER_STEP / e2e_s
+    flips_per_step = WORKLOAD["sweeps_per_check"] * flips_per_sweep(WORKLOAD)
+    e2e_rate = e2e_steps * flips_per_step / e2e_s
     eng.close()
 
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([total_ms, float(flips), e2e_s, float(e2e_steps * FLIPS_PER_STEP)], device=f"cuda:{device}",
+        t = torch.tensor([total_ms, float(flips), e2e_s, float(e2e_steps * flips_per_step)], device=f"cuda:{device}",
                          dtype=torch.float64)
         tmax = t.clone()
         dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
@@ -395,18 +443,18 @@ def run_gpu(args):
 
     peak, peak_kind = peaks()
     avg_launch_ms = kern_ms / max(kern_launches, 1)
-    flips_per_launch = WORKLOAD["sweeps_per_exchange"] * WORKLOAD["num_windows"] * WORKLOAD["replicas_per_window"] * 32 * 32
-    achieved = BYTES_PER_FLIP * flips_per_launch / (avg_launch_ms * 1e-3) / 1e9
+    flips_per_launch = WORKLOAD["sweeps_per_exchange"] * flips_per_sweep(WORKLOAD)
+    achieved = WORKLOAD["bytes_per_flip"] * flips_per_launch / (avg_launch_ms * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "flips/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64", "data": "synthetic",
         "config": {"workload": WORKLOAD["name"], **{k: v for k, v in WORKLOAD.items() if k != "name"},
-                   "step": "one check interval: 2 x (500 sweeps + exchange) + flatness/averaging/ln f",
+                   "step": step_text(),
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"instances x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic_per_launch(),
-                     "kernel": "k_sweep_ising", "bytes_per_flip": BYTES_PER_FLIP,
+                     "kernel": WORKLOAD["kernel"], "bytes_per_flip": WORKLOAD["bytes_per_flip"],
                      "avg_launch_ms": avg_launch_ms, "flips_per_launch": flips_per_launch},
         "e2e": {"value": e2e_rate, "unit": "flips/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps},
@@ -439,9 +487,12 @@ def main():
     ap.add_argument("--tta-seconds", type=float, default=90.0, help="wall-time limit of each time-to-accuracy arm")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="ising",
+                    help="ising: the headline configuration (default); at: 2D Ashkin-Teller, 64 realisations")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    select_workload(args.workload)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
