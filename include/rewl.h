@@ -88,7 +88,8 @@ typedef struct rewl_batch_desc {
     int32_t device;               /* CUDA device ordinal */
     int32_t warps_per_block;      /* 0: automatic; else 1, 2, 4 or 8 */
     int32_t walkers_per_warp;     /* 0: automatic; else 1, 2 or 4 (Ising bin-tracking kernel) */
-    int32_t reserved;
+    int32_t observables;          /* 1: keep per-bin observables (update_observables after every
+                                     attempted flip and exchange, rewl_walker.hpp / wang_landau.hpp:51-120) */
     const rewl_instance_desc* instances;
 } rewl_batch_desc;
 
@@ -185,6 +186,15 @@ int rewl_get_status(rewl_engine* eng, rewl_status* status);
  *  src/REWL/rewl_histograms.hpp:98-104) */
 int rewl_export_walker(rewl_engine* eng, int32_t walker, int8_t* dofs, double* state,
                        uint64_t* counts, double* logdos, uint64_t* visits);
+/* Per-bin observable averages of one walker (observables = 1), nb rows of K + 1 doubles: K
+ * averages and the number of updates, the layout of the reference's obs_array
+ * (Ising2d_Obs, src/Hamiltonians/Ising2d/ising2d_observables.hpp:134-145: K = 3, |m| m^2 m^4;
+ * Ashkin_Teller2d_Obs, src/Hamiltonians/Ashkin_Teller2d/ashkin_teller2d_observables.hpp:211-222:
+ * K = 12, |s| s^2 s^4 |t| t^2 t^4 |p| p^2 p^4 |b| b^2 b^4 with p^2 = s^2 + t^2). */
+int rewl_export_observables(rewl_engine* eng, int32_t walker, double* out);
+/* The same over a window's replicas, weighted by their counts (the final averaging of
+ * observables, src/Simulation/rewl_simulation.hpp:361-454). */
+int rewl_export_window_observables(rewl_engine* eng, int32_t instance, int32_t window, double* out);
 
 /* A window's logDoS averaged over its replicas with cumulative-visit weights
  * (the final average_and_redistribute_window, src/Simulation/rewl_simulation.hpp:687). */

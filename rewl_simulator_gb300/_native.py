@@ -97,6 +97,8 @@ def _declare(L: C.CDLL) -> None:
         "rewl_run_cycles": [vp, i64, i64, vp],
         "rewl_get_status": [vp, vp],
         "rewl_export_walker": [vp, i32, vp, vp, vp, vp, vp],
+        "rewl_export_observables": [vp, i32, vp],
+        "rewl_export_window_observables": [vp, i32, i32, vp],
         "rewl_export_window_logdos": [vp, i32, i32, vp],
         "rewl_export_window_mask": [vp, i32, i32, vp],
         "rewl_window_state": [vp, i32, i32, vp, vp],

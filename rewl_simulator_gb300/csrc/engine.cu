@@ -124,6 +124,8 @@ struct DevPtrs {
     int32_t* pairs;          // exchange pair lists: (instance, lower window) for dir 0 then dir 1
     int32_t* counters;       // [0] error word, [1] flat events (this call)
     unsigned long long* stats;  // [0] exch attempted, [1] exch accepted
+    double* obs;             // per-bin observable sums (obs_stride per bin), or null when off
+    int obs_stride;          // 3 (Ising) or 12 (a batch with Ashkin-Teller instances)
 };
 
 // --------------------------------------------------------------------------
@@ -288,6 +290,38 @@ __global__ void k_recalc(DevPtrs P, const int32_t* cfgs, const int32_t* insts, i
 // --------------------------------------------------------------------------
 // Sweep kernels
 // --------------------------------------------------------------------------
+// Per-bin observable sums (observables on): for every attempted flip and every
+// exchange touch, the walker's observables after it are added at its bin.  Ising:
+// |m|, m^2, m^4 with m = M / N (Ising2d::update_observables,
+// src/Hamiltonians/Ising2d/ising2d_hamiltonian.hpp:234-256); Ashkin-Teller: the 12
+// moments of Ashkin_Teller2d::update_observables (ashkin_teller2d_hamiltonian.hpp:267-318).
+// The reference keeps running means (v + c avg) / (c + 1) (ising2d_observables.hpp:134-145);
+// the export divides these sums by the visits instead, equal up to FP64 rounding.
+__device__ inline void obs_add_ising(double* o, int M, double invN)
+{
+    const double m = invN * fabs((double)M);
+    atomicAdd(o, m);
+    atomicAdd(o + 1, m * m);
+    atomicAdd(o + 2, m * m * m * m);
+}
+
+__device__ inline void obs_add_at(double* o, int sm, int tm, int bx, double invN)
+{
+    const double a = invN * fabs((double)sm), t = invN * fabs((double)tm), b = invN * fabs((double)bx);
+    const double p2 = a * a + t * t;
+    atomicAdd(o + 0, a); atomicAdd(o + 1, a * a); atomicAdd(o + 2, a * a * a * a);
+    atomicAdd(o + 3, t); atomicAdd(o + 4, t * t); atomicAdd(o + 5, t * t * t * t);
+    atomicAdd(o + 6, sqrt(p2)); atomicAdd(o + 7, p2); atomicAdd(o + 8, p2 * p2);
+    atomicAdd(o + 9, b); atomicAdd(o + 10, b * b); atomicAdd(o + 11, b * b * b * b);
+}
+
+// flips of a chunk's steps 0..j that turned a +1 into -1 minus those that turned -1 into +1
+__device__ __forceinline__ int chunk_dm(unsigned acc, unsigned plus, int j)
+{
+    const unsigned le = j >= 31 ? 0xFFFFFFFFu : ((2u << j) - 1u);
+    return -2 * ((int)__popc(acc & plus & le) - (int)__popc(acc & ~plus & le));
+}
+
 struct SweepParams {
     DevPtrs P;
     const int32_t* slots;    // walkers of this launch
@@ -305,6 +339,7 @@ struct Stage {
     int d0[32];
     int d1[32];
     int wc[32];
+    int seq[32];             // bin after each step (observables)
 };
 
 // Accept chain of one chunk of C sites, executed identically by all 32 lanes
@@ -397,7 +432,9 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
     const uint64_t sweeps0 = P.slot_sweeps[s];
     const uint32_t uid = (uint32_t)(s - I.first_slot);
     const uint64_t seed = I.seed;
-    const bool all_lanes = (!REPLAY) && VARIANT == 3 && (C == 32 || C == 16 || C == 24 || C == 8 || C == 4);
+    const bool obs_on = P.obs != nullptr;   // observables: the lane-0 resolver records each step's bin
+    const bool all_lanes = (!REPLAY) && VARIANT == 3 && !obs_on && (C == 32 || C == 16 || C == 24 || C == 8 || C == 4);
+    const double invN = 1.0 / (double)N;
 
     int E = (int)P.cfg_E[cfg];
     int M = P.cfg_M[3 * cfg];
@@ -479,6 +516,7 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
                         if (a) { E = En; b = bn; gc = gn; acc |= 1u << j; }
                         gc += lnf;
                         gs[b] = gc;
+                        if (obs_on) st->seq[j] = b;
                         En = a ? E1 : E0;
                         bn = a ? b1 : b0;
                         inr = a ? i1 : i0;
@@ -494,6 +532,12 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
                 if (REPLAY) { draws = __shfl_sync(kFull, draws, 0); err = __shfl_sync(kFull, err, 0); }
             }
             const unsigned plus = __ballot_sync(kFull, lane < C && si > 0);
+            if (obs_on) {
+                __syncwarp();
+                if (lane < C)
+                    obs_add_ising(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
+                                  M + chunk_dm(acc, plus, lane), invN);
+            }
             if (lane < C && ((acc >> lane) & 1u)) lat[row + x] = (int8_t)(-si);
             M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus));
             __syncwarp();
@@ -569,7 +613,7 @@ __device__ __forceinline__ long long lds64(const char* base, int off)
 }
 __device__ __forceinline__ void sts64(char* base, int off, long long v) { *reinterpret_cast<long long*>(base + off) = v; }
 
-template <int G, int C>
+template <int G, int C, bool OBS>
 __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
 {
     constexpr int P = 32 / G;
@@ -595,6 +639,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     int8_t* lat = reinterpret_cast<int8_t*>(base + gs_bytes);
     long long* Tb = reinterpret_cast<long long*>(base + gs_bytes + ((N + 15) & ~15));   // 2 x 4C thresholds
     int2* Db = reinterpret_cast<int2*>(Tb + 8 * C);                                   // 2 x C offset pairs
+    int* seqb = reinterpret_cast<int*>(Db + 2 * C);                                   // C bins (observables)
     // table positions are byte offsets from the start of shared memory, so that the
     // accesses need no address arithmetic
     char* const sm = reinterpret_cast<char*>(smem);
@@ -758,6 +803,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             const long long gnew = sel + lnf;
             const int bnew = a ? bp : bc;
             sts64(sm, bnew, gnew);
+            if (OBS) seqb[j] = bnew;
             if (a) acc |= 1u << j;
             if (j == 1 || j == 3) {
                 // next chunk's sites j-1, j: the neighbours they have in this chunk are decided
@@ -796,6 +842,17 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                 if (jj < C && ((acc >> jj) & 1u)) lat[c0 + jj] = (int8_t)(-cs[k]);
             }
             const unsigned full = C == 32 ? 0xFFFFFFFFu : ((1u << C) - 1u);
+            if (OBS) __syncwarp();
+            if (OBS && valid) {
+                double* ob = P_.obs + (size_t)P_.slot_tab[s] * P_.obs_stride;
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) {
+                    const int jj = q + k * P;
+                    if (jj < C)
+                        obs_add_ising(ob + (size_t)((seqb[jj] - gsoff) >> 3) * P_.obs_stride, M + chunk_dm(acc, plus, jj),
+                                      1.0 / (double)N);
+                }
+            }
             M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus & full));
         }
         // publish the next chunk: spins, offsets, wrap term, first thresholds
@@ -832,28 +889,42 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     }
 }
 
+template <int G, bool OBS>
+void launch_bins_t(int C, dim3 grid, dim3 block, size_t smem, cudaStream_t st, const SweepParams& sp)
+{
+    switch (C) {
+    case 32: k_sweep_ising_bins<G, 32, OBS><<<grid, block, smem, st>>>(sp); break;
+    case 24: k_sweep_ising_bins<G, 24, OBS><<<grid, block, smem, st>>>(sp); break;
+    case 16: k_sweep_ising_bins<G, 16, OBS><<<grid, block, smem, st>>>(sp); break;
+    case 8: k_sweep_ising_bins<G, 8, OBS><<<grid, block, smem, st>>>(sp); break;
+    default: k_sweep_ising_bins<G, 4, OBS><<<grid, block, smem, st>>>(sp); break;
+    }
+}
+
 template <int G>
 void launch_bins(int C, dim3 grid, dim3 block, size_t smem, cudaStream_t st, const SweepParams& sp)
 {
-    switch (C) {
-    case 32: k_sweep_ising_bins<G, 32><<<grid, block, smem, st>>>(sp); break;
-    case 24: k_sweep_ising_bins<G, 24><<<grid, block, smem, st>>>(sp); break;
-    case 16: k_sweep_ising_bins<G, 16><<<grid, block, smem, st>>>(sp); break;
-    case 8: k_sweep_ising_bins<G, 8><<<grid, block, smem, st>>>(sp); break;
-    default: k_sweep_ising_bins<G, 4><<<grid, block, smem, st>>>(sp); break;
-    }
+    if (sp.P.obs) launch_bins_t<G, true>(C, grid, block, smem, st, sp);
+    else launch_bins_t<G, false>(C, grid, block, smem, st, sp);
+}
+
+template <int G, bool OBS>
+cudaError_t allow_bins_smem_t()
+{
+    cudaError_t e = cudaSuccess;
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 32, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 24, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 16, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 8, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 4, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    return e;
 }
 
 template <int G>
 cudaError_t allow_bins_smem()
 {
-    cudaError_t e = cudaSuccess;
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    return e;
+    const cudaError_t e = allow_bins_smem_t<G, false>();
+    return e != cudaSuccess ? e : allow_bins_smem_t<G, true>();
 }
 
 // Ashkin-Teller: sweep = sigma pass then tau pass (wang_landau.hpp:109-119); the
@@ -863,6 +934,7 @@ struct StageAT {
     long long d0[32];
     long long d1[32];
     long long wc[32];
+    int seq[32];             // bin after each step (observables)
 };
 
 template <bool REPLAY>
@@ -966,11 +1038,23 @@ __global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
                         gg[b] = gc;
                         gH[b] += 1u;
                         gv[b] += 1u;
+                        if (P.obs) st->seq[j] = b;
                     }
                 }
                 acc = __shfl_sync(kFull, acc, 0);
                 const unsigned aplus = __ballot_sync(kFull, lane < C && ai > 0);
                 const unsigned abplus = __ballot_sync(kFull, lane < C && ai * bi > 0);
+                if (P.obs) {
+                    // magnetisations after each step of the chunk, from lane 0's values before it
+                    const int sm0 = __shfl_sync(kFull, sm, 0), tm0 = __shfl_sync(kFull, tm, 0);
+                    const int bx0 = __shfl_sync(kFull, bx, 0);
+                    if (lane < C) {
+                        const int da = chunk_dm(acc, aplus, lane), db = chunk_dm(acc, abplus, lane);
+                        obs_add_at(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
+                                   flavour == 0 ? sm0 + da : sm0, flavour == 0 ? tm0 : tm0 + da, bx0 + db,
+                                   1.0 / (double)N);
+                    }
+                }
                 if (lane < C && ((acc >> lane) & 1u)) A[c0 + lane] = (int8_t)(-ai);
                 if (lane == 0) {
                     const int da = -2 * ((int)__popc(acc & aplus) - (int)__popc(acc & ~aplus));
@@ -1013,6 +1097,12 @@ __device__ inline void touch(const DevPtrs& P, const InstDev& I, int slot)
     P.g[o] += P.win_lnf[w];
     P.H[o] += 1u;
     P.visits[o] += 1u;
+    if (P.obs) {
+        double* ob = P.obs + (size_t)o * P.obs_stride;
+        const double invN = 1.0 / (double)I.N;
+        if (I.model == REWL_MODEL_ISING2D) obs_add_ising(ob, P.cfg_M[3 * c], invN);
+        else obs_add_at(ob, P.cfg_M[3 * c], P.cfg_M[3 * c + 1], P.cfg_M[3 * c + 2], invN);
+    }
 }
 
 __global__ void k_exchange(DevPtrs P, const int32_t* pairs, int npairs, uint64_t round)
@@ -1303,6 +1393,8 @@ struct rewl_engine {
     DBuf<uint8_t> mask;
     DBuf<unsigned long long> stats;
     DBuf<int64_t> thr;
+    DBuf<double> obs;           // per-bin observable sums (observables on)
+    int obs_stride = 0;
     std::vector<int64_t> h_thr_off, h_thr_n;
     std::vector<int64_t> h_fields;
     std::vector<uint8_t> h_mask;
@@ -1318,6 +1410,7 @@ struct rewl_engine {
         P.g = g.p; P.H = H.p; P.visits = visits.p; P.mask = mask.p;
         P.win_lnf = win_lnf.p; P.win_done = win_done.p; P.win_oot = win_oot.p; P.win_iter = win_iter.p;
         P.win_sweepctr = win_sweepctr.p; P.pairs = nullptr; P.counters = counters.p; P.stats = stats.p;
+        P.obs = obs.p; P.obs_stride = obs_stride;
         return P;
     }
 
@@ -1326,6 +1419,7 @@ struct rewl_engine {
         d_inst.free_(); d_win.free_();
         slot_inst.free_(); slot_win.free_(); slot_cfg.free_(); slot_nb.free_(); slot_flavour.free_();
         pairs[0].free_(); pairs[1].free_();
+        obs.free_();
         slot_tab.free_(); slot_draws.free_(); slot_thr_off.free_(); slot_thr_n.free_(); cfg_off.free_();
         cfg_E.free_(); fields.free_(); g.free_(); win_lnf.free_(); slot_sweeps.free_(); visits.free_();
         win_iter.free_(); win_sweepctr.free_(); spins.free_(); cfg_M.free_(); win_done.free_(); win_oot.free_();
@@ -1432,6 +1526,7 @@ int build_host(rewl_engine* e)
     if (D.rng_mode != REWL_RNG_PHILOX && D.rng_mode != REWL_RNG_REPLAY) return fail(REWL_EINVAL, "bad rng mode");
     if (D.warps_per_block != 0 && D.warps_per_block != 1 && D.warps_per_block != 2 && D.warps_per_block != 4 && D.warps_per_block != 8)
         return fail(REWL_EINVAL, "warps_per_block must be 0, 1, 2, 4 or 8");
+    if (D.observables != 0 && D.observables != 1) return fail(REWL_EINVAL, "observables must be 0 or 1");
     if (D.walkers_per_warp != 0 && D.walkers_per_warp != 1 && D.walkers_per_warp != 2 && D.walkers_per_warp != 4)
         return fail(REWL_EINVAL, "walkers_per_warp must be 0, 1, 2 or 4");
     int slot = 0, win = 0;
@@ -1575,6 +1670,13 @@ int upload_all(rewl_engine* e)
         CUDA_TRY(cudaMemsetAsync(e->H.p, 0, tab * sizeof(uint32_t), s));
         CUDA_TRY(cudaMemsetAsync(e->visits.p, 0, tab * sizeof(uint64_t), s));
     }
+    if (D.observables && tab) {
+        bool any_at = false;
+        for (const auto& hi : e->inst) any_at = any_at || hi.d.model == REWL_MODEL_ASHKIN_TELLER2D;
+        e->obs_stride = any_at ? 12 : 3;
+        if ((rc = e->obs.alloc((size_t)tab * e->obs_stride))) return rc;
+        CUDA_TRY(cudaMemsetAsync(e->obs.p, 0, (size_t)tab * e->obs_stride * sizeof(double), s));
+    }
     std::vector<int64_t> lnf(win, std::max<int64_t>(1, (int64_t)std::llround(D.lnf_initial * kLogdosScale)));
     CUDA_TRY(cudaMemcpyAsync(e->win_lnf.p, lnf.data(), win * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     CUDA_TRY(cudaMemsetAsync(e->win_done.p, 0, win * sizeof(int32_t), s));
@@ -1644,7 +1746,7 @@ int plan_launches(rewl_engine* e)
             }
             l.walkers_per_warp = G;
             l.nbcap = (maxnb + 1) & ~1;
-            int raw = (((l.nbcap + 2 * kGuard) * 8 + 15) & ~15) + ((maxN + 15) & ~15) + 8 * l.chunk * 8 + 2 * l.chunk * 8;
+            int raw = (((l.nbcap + 2 * kGuard) * 8 + 15) & ~15) + ((maxN + 15) & ~15) + 8 * l.chunk * 8 + 2 * l.chunk * 8 + l.chunk * 4;
             l.smem_per_warp = ((raw + 127) & ~127) + 16;           // per walker; +16 skews the walkers' banks
             if ((size_t)l.smem_per_warp * G > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory", l.smem_per_warp);
             int wpb = e->desc.warps_per_block;
@@ -2145,6 +2247,52 @@ int rewl_run_cycles(rewl_engine* e, int64_t ncycles, int64_t timeout_ms, rewl_st
     return REWL_OK;
 }
 
+namespace {
+// [nb][K + 1] rows of K averages and the update count, from the sums of the given slots
+int export_obs(rewl_engine* e, int ii, const std::vector<int>& slots, double* out)
+{
+    if (!e->obs.p) return fail(REWL_ESTATE, "the engine was created without observables (rewl_batch_desc.observables)");
+    const int K = e->inst[ii].d.model == REWL_MODEL_ISING2D ? 3 : 12;
+    const int nb = e->h_slot_nb[slots[0]];
+    std::vector<double> sum((size_t)nb * K, 0.0), part((size_t)nb * e->obs_stride);
+    std::vector<uint64_t> cnt(nb, 0), v(nb);
+    for (int s : slots) {
+        const int64_t off = e->h_slot_tab[s];
+        CUDA_TRY(cudaMemcpyAsync(part.data(), e->obs.p + (size_t)off * e->obs_stride, part.size() * 8,
+                                 cudaMemcpyDeviceToHost, e->stream));
+        CUDA_TRY(cudaMemcpyAsync(v.data(), e->visits.p + off, nb * 8, cudaMemcpyDeviceToHost, e->stream));
+        CUDA_TRY(cudaStreamSynchronize(e->stream));
+        for (int b = 0; b < nb; ++b) {
+            for (int k = 0; k < K; ++k) sum[(size_t)b * K + k] += part[(size_t)b * e->obs_stride + k];
+            cnt[b] += v[b];
+        }
+    }
+    for (int b = 0; b < nb; ++b) {
+        for (int k = 0; k < K; ++k)
+            out[(size_t)b * (K + 1) + k] = cnt[b] ? sum[(size_t)b * K + k] / (double)cnt[b] : 0.0;
+        out[(size_t)b * (K + 1) + K] = (double)cnt[b];
+    }
+    return REWL_OK;
+}
+} // namespace
+
+int rewl_export_observables(rewl_engine* e, int32_t w, double* out)
+{
+    if (!valid_walker(e, w) || !out) return fail(REWL_EINVAL, "walker %d out of range or null output", w);
+    cudaSetDevice(e->desc.device);
+    return export_obs(e, e->h_slot_inst[w], {w}, out);
+}
+
+int rewl_export_window_observables(rewl_engine* e, int32_t ii, int32_t w, double* out)
+{
+    if (window_index(e, ii, w) < 0 || !out) return fail(REWL_EINVAL, "bad window or null output");
+    cudaSetDevice(e->desc.device);
+    const InstDev& I = e->inst[ii].dev;
+    std::vector<int> slots;
+    for (int r = 0; r < I.R; ++r) slots.push_back(I.first_slot + w * I.R + r);
+    return export_obs(e, ii, slots, out);
+}
+
 int rewl_export_walker(rewl_engine* e, int32_t w, int8_t* dofs, double* state, uint64_t* counts, double* logdos, uint64_t* visits)
 {
     if (!valid_walker(e, w)) return fail(REWL_EINVAL, "walker %d out of range", w);
@@ -2296,7 +2444,7 @@ std::vector<SnapPart> snapshot_parts(rewl_engine* e)
     auto P = [](auto& b) { return SnapPart{(void*)b.p, b.n * sizeof(*b.p)}; };
     return {P(e->slot_cfg), P(e->slot_flavour), P(e->slot_sweeps), P(e->slot_draws), P(e->cfg_E), P(e->cfg_M),
             P(e->spins), P(e->g), P(e->H), P(e->visits), P(e->win_lnf), P(e->win_done), P(e->win_oot),
-            P(e->win_iter), P(e->win_sweepctr), P(e->stats)};
+            P(e->win_iter), P(e->win_sweepctr), P(e->stats), P(e->obs)};
 }
 
 struct SnapHeader {

@@ -54,7 +54,7 @@ class _BatchDesc(C.Structure):
                 ("lnf_initial", C.c_double), ("lnf_final", C.c_double), ("mask_mode", C.c_int32),
                 ("one_over_t", C.c_int32), ("reduce_logdos", C.c_int32), ("rng_mode", C.c_int32),
                 ("device", C.c_int32), ("warps_per_block", C.c_int32), ("walkers_per_warp", C.c_int32),
-                ("reserved", C.c_int32), ("instances", C.c_void_p)]
+                ("observables", C.c_int32), ("instances", C.c_void_p)]
 
 
 class _Status(C.Structure):
@@ -107,6 +107,7 @@ class Batch:
     device: int = 0
     warps_per_block: int = 0
     walkers_per_warp: int = 0
+    observables: int = 0
 
 
 @dataclass
@@ -155,7 +156,7 @@ class Engine:
         b.num_instances = n
         for name in ("sweeps_per_exchange", "sweeps_per_check", "flatness_mode", "flatness_param", "lnf_initial",
                      "lnf_final", "mask_mode", "one_over_t", "reduce_logdos", "rng_mode", "device",
-                     "warps_per_block", "walkers_per_warp"):
+                     "warps_per_block", "walkers_per_warp", "observables"):
             setattr(b, name, getattr(batch, name))
         b.instances = C.cast(self._inst, C.c_void_p)
         self._desc = b
@@ -281,6 +282,22 @@ class Engine:
         if ins.model == MODEL_ISING2D:
             state = state[:2]
         return dict(dofs=dofs, state=state, counts=counts, logdos=logdos, visits=visits)
+
+    def _obs_cols(self, instance: int) -> int:
+        return 4 if self.batch.instances[instance].model == MODEL_ISING2D else 13
+
+    def export_observables(self, walker: int) -> np.ndarray:
+        """Per-bin observable averages of a walker, rows of [K averages, count] (observables=1)."""
+        inst, w, _ = self._walker_inst[walker]
+        out = np.zeros((self.windows[inst][w][2], self._obs_cols(inst)))
+        self._check(self.lib.rewl_export_observables(self.h, walker, _p(out)))
+        return out
+
+    def window_observables(self, instance: int, window: int) -> np.ndarray:
+        """Count-weighted average of the window's replicas' observables, same layout."""
+        out = np.zeros((self.windows[instance][window][2], self._obs_cols(instance)))
+        self._check(self.lib.rewl_export_window_observables(self.h, instance, window, _p(out)))
+        return out
 
     def window_logdos(self, instance: int, window: int) -> np.ndarray:
         out = np.zeros(self.windows[instance][window][2])

@@ -32,7 +32,8 @@ def test_replay_matches_reference(engine_lib, oracle_lib, name):
     ins = rg.Instance(model=model, L=int(z["L"]), J=1.0, K=float(z["K"]) if model else 0.0, fields=fields,
                       energy_min=float(z["wmin"]), energy_max=float(z["wmax"]), bin_width=float(z["bw"]),
                       num_windows=1, replicas_per_window=1, init_mode=1, seed=1)
-    b = rg.Batch(instances=[ins], rng_mode=rg.RNG_REPLAY, lnf_initial=float(z["lnf1"]), lnf_final=1e-9)
+    b = rg.Batch(instances=[ins], rng_mode=rg.RNG_REPLAY, lnf_initial=float(z["lnf1"]), lnf_final=1e-9,
+                 observables=1)
     with rg.Engine(b) as eng:
         which = int(z["state0"][4]) if model else 0
         eng.import_dofs(0, _engine_layout(z["dofs0"], model), which)
@@ -52,21 +53,25 @@ def test_replay_matches_reference(engine_lib, oracle_lib, name):
             np.testing.assert_array_equal(out["logdos"], z[f"logdos{stage}"])
             np.testing.assert_array_equal(out["state"], z[f"state{stage}"])
             np.testing.assert_array_equal(out["dofs"], _engine_layout(z[f"dofs{stage}"], model))
+            # per-bin observables: the reference's running means, to FP64 rounding
+            obs, ref = eng.export_observables(0), z[f"obs{stage}"]
+            np.testing.assert_array_equal(obs[:, -1], ref[:, -1])
+            np.testing.assert_allclose(obs[:, :-1], ref[:, :-1], rtol=1e-12, atol=1e-15)
 
 
 def _pair(rg, po, model, L, emin, emax, bw, nwin, R, se, sc, seed, K=0.5, fields=None, flat=0.8,
-          mask=0, lnf0=1.0, overlap=0.75, flat_mode=0, walkers_per_warp=0):
+          mask=0, lnf0=1.0, overlap=0.75, flat_mode=0, walkers_per_warp=0, observables=0):
     ins = rg.Instance(model=model, L=L, J=1.0, K=K if model else 0.0, fields=fields, energy_min=emin,
                       energy_max=emax, bin_width=bw, num_windows=nwin, replicas_per_window=R,
                       window_overlap=overlap, init_mode=0, seed=seed)
     b = rg.Batch(instances=[ins], sweeps_per_exchange=se, sweeps_per_check=sc, flatness_mode=flat_mode,
                  flatness_param=flat, lnf_initial=lnf0, lnf_final=1e-7, mask_mode=mask,
-                 walkers_per_warp=walkers_per_warp)
+                 walkers_per_warp=walkers_per_warp, observables=observables)
     eng = rg.Engine(b)
     cfg = po.Config(model=model, L=L, K=K, escale_bits=0 if model == 0 else 20, nwin=nwin, R=R,
                     sweeps_per_exchange=se, sweeps_per_check=sc, emin=emin, emax=emax, bw=bw, overlap=overlap,
                     lnf0=lnf0, lnf_final=1e-7, flat_param=flat, flat_mode=flat_mode, mask_mode=mask,
-                    semantics=po.SEM_ENGINE, seed=seed)
+                    semantics=po.SEM_ENGINE, seed=seed, observables=observables)
     orc = po.Oracle(cfg, fields=fields)
     return eng, orc
 
@@ -164,3 +169,47 @@ def test_ising_L8_converges_to_exact(engine_lib):
         np.testing.assert_array_equal(E, z["E"])
         err = np.abs(g - z["lng"]).max()
         assert err < 0.05, err
+
+
+OBS_CASES = [
+    # name, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles, walkers_per_warp, sigma_h, mask
+    ("ising_L8_bins", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 3, 0, 0.0, 0),
+    ("ising_L16_bins_2perwarp", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 3, 2, 0.0, 0),
+    ("ising_L12_bw8_general", 0, 12, -288.0, 296.0, 8.0, 4, 2, 10, 20, 3, 3, 0, 0.0, 0),
+    ("at_L4_rf", 1, 4, -(2.5) * 2 * 16, 0.0, 0.05, 2, 2, 20, 40, 7, 3, 0, 0.5, 1),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", OBS_CASES, ids=[c[0] for c in OBS_CASES])
+def test_engine_observables_match_oracle(engine_lib, oracle_lib, case):
+    """Per-bin observables of every walker, and their count-weighted window average, against
+    the oracle's running means after every check interval (all three sweep kernels)."""
+    _, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles, wpw, sig, mask = case
+    fields = None
+    if sig > 0:
+        fields = np.round(np.random.default_rng(seed).normal(0, sig, L * L) * 2**20) / 2**20
+    eng, orc = _pair(engine_lib, oracle_lib, model, L, emin, emax, bw, nwin, R, se, sc, seed, fields=fields,
+                     mask=mask, walkers_per_warp=wpw, observables=1)
+    try:
+        for k in range(cycles):
+            eng.run_cycles(1)
+            orc.cycle()
+            _compare(eng, orc, f"cycle {k}")
+            for w in range(nwin):
+                ws = []
+                for r in range(R):
+                    s = w * R + r
+                    got, ref = eng.export_observables(s), orc.obs(s)
+                    np.testing.assert_array_equal(got[:, -1], ref[:, -1], err_msg=f"cycle {k} walker {s} counts")
+                    np.testing.assert_allclose(got[:, :-1], ref[:, :-1], rtol=1e-12, atol=1e-15,
+                                               err_msg=f"cycle {k} walker {s}")
+                    ws.append(ref)
+                cnt = sum(o[:, -1] for o in ws)
+                avg = sum(o[:, :-1] * o[:, -1:] for o in ws) / np.maximum(cnt, 1)[:, None]
+                got = eng.window_observables(0, w)
+                np.testing.assert_array_equal(got[:, -1], cnt)
+                np.testing.assert_allclose(got[:, :-1], avg, rtol=1e-11, atol=1e-15, err_msg=f"cycle {k} window {w}")
+    finally:
+        eng.close()
+        orc.close()
