@@ -276,6 +276,25 @@ int rewl_mlp_launches(const rewl_mlp* mlp, int64_t* count);
  * caller.  Parameters must not change while a call is in flight. */
 int rewl_mlp_predict_noalloc(rewl_mlp* mlp, const float* X, int32_t n, int32_t in_dim, float* y, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Canonical thermodynamics from a density of states (FP64 log-sum-exp on the GPU).
+ * ------------------------------------------------------------------------ */
+const char* rewl_thermo_last_error_string(void);
+/* Thermodynamics::calculate_thermodynamics (src/Thermodynamics/thermodynamics.hpp:158-297)
+ * for num_T temperatures T_i = Tmin + i (Tmax - Tmin) / num_T: out holds num_T rows of
+ * [F, U, U2, S, C, num_obs observables] (per site; column counts_col of obs, if >= 0, is
+ * averaged over the bins instead of weighted), temperatures the T_i.  E, lng: nbins values;
+ * obs: nbins x num_obs (rewl_export_window_observables layout) or NULL; trapezoid: the
+ * reference's TRAPEZOIDAL_RULE (end bins weighted 1/2). */
+int rewl_thermodynamics(const double* E, const double* lng, const double* obs, int32_t nbins, int32_t num_obs,
+                        int32_t counts_col, double system_size, double Tmin, double Tmax, int32_t num_T,
+                        int32_t trapezoid, int32_t device, double* temperatures, double* out);
+/* Susceptibility N (<m^2> - <m>^2) / T and Binder cumulants from those rows
+ * (order_parameter_cumulants.hpp:17-48).  Ising: 2 values per T (susceptibility, cumulant);
+ * Ashkin-Teller: 8 (sigma, tau, Baxter, then phi with the two-component cumulant). */
+int rewl_nonlinear_observables(int32_t model, const double* rows, int32_t num_T, int32_t row_len,
+                               const double* temperatures, double system_size, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -138,6 +138,21 @@ def build(model: str, L: int, bw: float, K: float = 0.5, fields: bool = True, fo
     return so
 
 
+def build_thermo(trapezoid: bool = True, force: bool = False) -> Path:
+    """oracle/_ref/libref_thermo[_plain].so: the reference's thermodynamics.hpp driven by
+    oracle/ref_thermo.cpp (TRAPEZOIDAL_RULE on by default, as in the reference's build)."""
+    if not reference_available():
+        raise FileNotFoundError(f"reference sources not found under {REF}")
+    so = OUT / ("libref_thermo.so" if trapezoid else "libref_thermo_plain.so")
+    if so.exists() and not force:
+        return so
+    OUT.mkdir(parents=True, exist_ok=True)
+    cmd = (["g++", "-std=c++17", "-O2", "-fPIC", "-shared"] + (["-DTRAPEZOIDAL_RULE"] if trapezoid else [])
+           + [f"-I{REF / 'src' / 'Thermodynamics'}", str(HERE / "ref_thermo.cpp"), "-o", str(so)])
+    subprocess.run(cmd, check=True)
+    return so
+
+
 if __name__ == "__main__":
     m = sys.argv[1] if len(sys.argv) > 1 else "ising"
     L = int(sys.argv[2]) if len(sys.argv) > 2 else 8

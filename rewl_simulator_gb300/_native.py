@@ -16,7 +16,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 LIB = PKG / "librewl_gb300.so"
-SOURCES = [CSRC / "engine.cu", CSRC / "mlp.cu"]
+SOURCES = [CSRC / "engine.cu", CSRC / "mlp.cu", CSRC / "thermo.cu"]
 DEPS = SOURCES + [CSRC / "rng.cuh", INCLUDE / "rewl.h"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -79,6 +79,7 @@ def _declare(L: C.CDLL) -> None:
     vp, i32, i64, u64, sz, dp = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_size_t, C.c_void_p
     L.rewl_last_error_string.restype = C.c_char_p
     L.rewl_mlp_last_error_string.restype = C.c_char_p
+    L.rewl_thermo_last_error_string.restype = C.c_char_p
     sigs = {
         "rewl_create": [vp, vp],
         "rewl_destroy": [vp],
@@ -98,6 +99,8 @@ def _declare(L: C.CDLL) -> None:
         "rewl_get_status": [vp, vp],
         "rewl_export_walker": [vp, i32, vp, vp, vp, vp, vp],
         "rewl_export_observables": [vp, i32, vp],
+        "rewl_thermodynamics": [vp, vp, vp, i32, i32, i32, C.c_double, C.c_double, C.c_double, i32, i32, i32, vp, vp],
+        "rewl_nonlinear_observables": [i32, vp, i32, i32, vp, C.c_double, vp],
         "rewl_export_window_observables": [vp, i32, i32, vp],
         "rewl_export_window_logdos": [vp, i32, i32, vp],
         "rewl_export_window_mask": [vp, i32, i32, vp],

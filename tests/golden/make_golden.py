@@ -16,6 +16,11 @@ Groups
               (src/util/random_number_generators.hpp:14-31) for a few seeds.
   normalize-- normalize_logDoS (src/util/array_shift.hpp:15-43).
   exact    -- exact 2D Ising ln g(E) (oracle/beale.py) for L = 4..64.
+  thermo   -- the reference's Thermodynamics::calculate_thermodynamics
+              (src/Thermodynamics/thermodynamics.hpp:158-297, oracle/ref_thermo.cpp)
+              on the exact L = 16 Ising ln g with synthetic observables, and on a
+              synthetic Ashkin-Teller-like spectrum with 12 moments, with and without
+              the trapezoidal rule.
 """
 from __future__ import annotations
 
@@ -175,7 +180,47 @@ def gen_exact():
         print("wrote exact L", L)
 
 
+def _thermo_inputs(at: bool):
+    if not at:
+        z = np.load(OUT / "exact_ising_L16.npz")
+        ok = np.isfinite(z["lng"])
+        E, lng, N = z["E"][ok].astype(np.float64), z["lng"][ok], 256
+        m = np.sqrt(np.clip(1.0 - (E / E[-1]) ** 2, 0.0, None)) * (E < 0) + 0.05
+        obs = np.stack([m, m * m + 0.01, (m * m + 0.01) ** 2 + 0.001, 1000.0 + (np.arange(E.size) % 7) * 13.0], axis=1)
+        return E, lng, obs, N, 3
+    N = 64
+    E = np.arange(-320.0, 0.0, 0.5)                      # AT L = 8, K = 0.5 range, bins of 0.5
+    x = E / E[0]
+    lng = 2 * N * np.log(2.0) * (1.0 - x ** 2) + np.log(4.0) * x ** 8
+    cols = []
+    for k in range(12):
+        cols.append(0.1 + 0.8 * x ** (1 + k % 3) * (1.0 + 0.01 * k))
+    obs = np.stack(cols + [500.0 + (np.arange(E.size) % 5) * 11.0], axis=1)
+    return E, lng, obs, N, 12
+
+
+def gen_thermo():
+    import ctypes as C
+    for trap in (True, False):
+        lib = C.CDLL(str(build_ref.build_thermo(trapezoid=trap, force=True)))
+        lib.ref_thermo.restype = C.c_int
+        lib.ref_thermo.argtypes = [C.c_int, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_double,
+                                   C.c_double, C.c_size_t, C.c_void_p, C.c_void_p]
+        for at in (False, True):
+            E, lng, obs, N, cc = _thermo_inputs(at)
+            obs = np.ascontiguousarray(obs)
+            Tmin, Tmax, nT = 0.01, 50.01, 2000
+            out = np.zeros((nT, 5 + obs.shape[1]))
+            T = np.zeros(nT)
+            p = lambda a: a.ctypes.data_as(C.c_void_p)
+            lib.ref_thermo(int(at), E.size, p(E), p(lng), p(obs), N, Tmin, Tmax, nT, p(out), p(T))
+            name = f"thermo_{'at' if at else 'ising'}{'' if trap else '_plain'}.npz"
+            np.savez_compressed(OUT / name, E=E, lng=lng, obs=obs, N=N, counts_col=cc, Tmin=Tmin, Tmax=Tmax, nT=nT,
+                                trapezoid=int(trap), model=int(at), temperatures=T, out=out)
+            print("wrote", name)
+
+
 if __name__ == "__main__":
-    groups = sys.argv[1:] or ["replay", "glazier", "rng", "normalize", "exact"]
+    groups = sys.argv[1:] or ["replay", "glazier", "rng", "normalize", "exact", "thermo"]
     for g in groups:
         globals()[f"gen_{g}"]()
