@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kThreads) k_thermo(const double* E, const doub
     __shared__ double sh[kThreads / 32 + 1];
     const int t = blockIdx.x;
     if (t >= nT) return;
-    const double T = Tmin + dT * (double)t;
+    const double T = __dadd_rn(Tmin, __dmul_rn(dT, (double)t));   // rounded as the reference's Tmin + dT * i
     double mx = -INFINITY;
     for (int b = threadIdx.x; b < nb; b += kThreads) mx = fmax(mx, lng[b] - E[b] / T);
     mx = block_max(mx, sh);
