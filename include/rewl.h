@@ -295,6 +295,32 @@ int rewl_thermodynamics(const double* E, const double* lng, const double* obs, i
 int rewl_nonlinear_observables(int32_t model, const double* rows, int32_t num_T, int32_t row_len,
                                const double* temperatures, double system_size, double* out);
 
+/* ------------------------------------------------------------------------
+ * Output files in the reference's text formats (main.cpp:241-365): '#' header lines
+ * naming the columns, comma-delimited rows, std::scientific with 15 digits.
+ * names: the column names after the leading ones, separated by '\n'.
+ * ------------------------------------------------------------------------ */
+/* Observables on the energies of rewl_global_logdos (rows of K + 1: K averages, count),
+ * windows combined by the reference's running mean (concatenate_rewl_tables.hpp:241-256). */
+int rewl_global_observables(rewl_engine* eng, int32_t instance, double* obs, int32_t* count);
+/* microcanonical_observables-<file_string>.txt: E/N, ln g/N, num_obs observables per bin
+ * (write_microcanonical_observables.hpp:16-65) */
+int rewl_write_microcanonical(const char* dir, const char* file_string, const char* header, const char* names,
+                              int32_t num_bins, int32_t num_obs, double system_size, const double* energies,
+                              const double* logdos, const double* obs);
+/* self_averaged_observables-<file_string>.txt: T and num_cols values per row
+ * (write_self_averaged_observables.hpp:15-59) */
+int rewl_write_self_averaged(const char* dir, const char* file_string, const char* header, const char* names,
+                             int32_t num_T, int32_t num_cols, const double* temperatures, const double* rows);
+/* nonlinear_observables-<file_string>.txt (write_nonlinear_observables.hpp:13-57) */
+int rewl_write_nonlinear(const char* dir, const char* file_string, const char* header, const char* names,
+                         int32_t num_T, int32_t num_cols, const double* temperatures, const double* rows);
+/* All three files for one instance: concatenated normalised ln g (+ observables when the engine
+ * keeps them), thermodynamics over T_i = Tmin + i (Tmax - Tmin) / num_T on the GPU, and the
+ * nonlinear observables (src/Simulation/main.cpp:241-365). */
+int rewl_write_outputs(rewl_engine* eng, int32_t instance, const char* dir, const char* file_string,
+                       const char* header, double Tmin, double Tmax, int32_t num_T);
+
 #ifdef __cplusplus
 }
 #endif

@@ -153,6 +153,22 @@ def build_thermo(trapezoid: bool = True, force: bool = False) -> Path:
     return so
 
 
+def build_writers(force: bool = False) -> Path:
+    """oracle/_ref/libref_writers.so: the reference's three output writers (oracle/ref_writers.cpp)."""
+    if not reference_available():
+        raise FileNotFoundError(f"reference sources not found under {REF}")
+    so = OUT / "libref_writers.so"
+    if so.exists() and not force:
+        return so
+    OUT.mkdir(parents=True, exist_ok=True)
+    src = REF / "src"
+    cmd = (["g++", "-std=c++17", "-O1", "-fPIC", "-shared"]
+           + [f"-I{src / d}" for d in ("util", "Thermodynamics", "file_management")]
+           + [str(HERE / "ref_writers.cpp"), "-o", str(so)])
+    subprocess.run(cmd, check=True)
+    return so
+
+
 if __name__ == "__main__":
     m = sys.argv[1] if len(sys.argv) > 1 else "ising"
     L = int(sys.argv[2]) if len(sys.argv) > 2 else 8

@@ -35,6 +35,11 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
+#include <fstream>
+#include <iomanip>
+#include <limits>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -2416,6 +2421,178 @@ int rewl_global_logdos(rewl_engine* e, int32_t ii, int32_t half_spectrum, double
     for (size_t k = 0; k < fe.size(); ++k) { if (energies) energies[k] = fe[k]; if (logdos) logdos[k] = fg[k] + shift; }
     *count = (int)fe.size();
     return REWL_OK;
+}
+
+// Observables on the concatenated energy axis (the energies of rewl_global_logdos): every
+// window's count-weighted replica average (rewl_export_window_observables) is combined across
+// the windows that hold an energy by the reference's running mean
+// average_two_windows(final, window, overlapping_windows, 1)
+// (src/util/concatenate_rewl_tables.hpp:43-49, 241-256), in window order.
+int rewl_global_observables(rewl_engine* e, int32_t ii, double* obs, int32_t* count)
+{
+    if (!e || ii < 0 || ii >= (int)e->inst.size() || !count) return fail(REWL_EINVAL, "bad arguments");
+    if (!e->obs.p) return fail(REWL_ESTATE, "the engine was created without observables (rewl_batch_desc.observables)");
+    const HostInst& H = e->inst[ii];
+    const int cols = (H.d.model == REWL_MODEL_ISING2D ? 3 : 12) + 1;
+    const bool half = H.d.model != REWL_MODEL_ISING2D && H.d.energy_max <= 0.0;
+    int n = 0;
+    int rc = rewl_global_logdos(e, ii, half ? 1 : 0, nullptr, nullptr, &n);
+    if (rc && n == 0) return rc;
+    std::vector<double> E(n);
+    if ((rc = rewl_global_logdos(e, ii, half ? 1 : 0, E.data(), nullptr, &n))) return rc;
+    if (n > *count) { *count = n; return fail(REWL_EINVAL, "output capacity too small (%d rows needed)", n); }
+    // running means keyed by the global bin index
+    std::vector<double> mean;
+    std::vector<int64_t> key0;
+    std::vector<int> nwin;
+    int64_t kmin = INT64_MAX, kmax = INT64_MIN;
+    for (int w = 0; w < H.d.num_windows; ++w) {
+        kmin = std::min<int64_t>(kmin, H.wins[w].gblo);
+        kmax = std::max<int64_t>(kmax, H.wins[w].gblo + H.wins[w].nb);
+    }
+    mean.assign((size_t)(kmax - kmin) * cols, 0.0);
+    nwin.assign((size_t)(kmax - kmin), 0);
+    for (int w = 0; w < H.d.num_windows; ++w) {
+        const int nb = H.wins[w].nb;
+        std::vector<double> o((size_t)nb * cols);
+        std::vector<uint8_t> m(nb);
+        if ((rc = rewl_export_window_observables(e, ii, w, o.data())) || (rc = rewl_export_window_mask(e, ii, w, m.data())))
+            return rc;
+        for (int b = 0; b < nb; ++b) {
+            if (!m[b]) continue;
+            const size_t k = (size_t)(H.wins[w].gblo + b - kmin);
+            const int c = nwin[k];
+            for (int j = 0; j < cols; ++j) {
+                double& v = mean[k * cols + j];
+                v = c == 0 ? o[(size_t)b * cols + j] : ((double)c * v + o[(size_t)b * cols + j]) / (double)(c + 1);
+            }
+            ++nwin[k];
+        }
+    }
+    for (int r = 0; r < n; ++r) {
+        const int64_t k = (int64_t)std::llround((E[r] - H.d.energy_min) / H.bw) - kmin;
+        if (k < 0 || k >= kmax - kmin || nwin[k] == 0) return fail(REWL_ESTATE, "energy %g has no window observables", E[r]);
+        for (int j = 0; j < cols; ++j) obs[(size_t)r * cols + j] = mean[(size_t)k * cols + j];
+    }
+    *count = n;
+    return REWL_OK;
+}
+
+namespace {
+std::vector<std::string> split_names(const char* names)
+{
+    std::vector<std::string> v;
+    if (!names) return v;
+    std::stringstream ss(names);
+    std::string line;
+    while (std::getline(ss, line, '\n'))
+        if (!line.empty()) v.push_back(line);
+    return v;
+}
+
+// '#' header lines naming the columns (first_cols, then names), as the reference's writers do
+void column_header(std::ofstream& f, const char* title, const std::vector<std::string>& first_cols,
+                   const std::vector<std::string>& names)
+{
+    f << "# " << title;
+    int col = 0;
+    for (const auto& c : first_cols) f << "\n#    " << ++col << ": " << c;
+    for (const auto& c : names) f << "\n#    " << ++col << ": " << c;
+    f << "\n#\n";
+}
+
+int write_table(const char* dir, const char* stem, const char* file_string, const char* header, const char* title,
+                const std::vector<std::string>& first_cols, const char* names, int32_t rows, int32_t cols,
+                const double* a, const double* b, double scale, const double* values)
+{
+    if (!dir || !file_string || rows < 1 || cols < 0 || !a || (cols > 0 && !values))
+        return fail(REWL_EINVAL, "bad arguments");
+    const std::filesystem::path path = std::filesystem::path(dir) / (std::string(stem) + "-" + file_string + ".txt");
+    std::ofstream f(path);
+    if (!f) return fail(REWL_EINVAL, "cannot open %s for writing", path.string().c_str());
+    if (header) f << header;
+    column_header(f, title, first_cols, split_names(names));
+    f << std::setprecision(std::numeric_limits<double>::digits10) << std::scientific;
+    for (int32_t r = 0; r < rows; ++r) {
+        f << a[r] / scale << ",";
+        if (b) f << b[r] / scale << (cols > 0 ? "," : "");
+        for (int32_t c = 0; c < cols; ++c) f << values[(size_t)r * cols + c] << (c + 1 < cols ? "," : "");
+        if (r + 1 < rows) f << "\n";
+    }
+    return f.good() ? REWL_OK : fail(REWL_EINVAL, "write to %s failed", path.string().c_str());
+}
+} // namespace
+
+// Text formats of the reference's writers (comma-delimited rows, src/Simulation/main_headers.hpp:18;
+// '#' header lines; std::scientific with 15 digits): write_microcanonical_observables
+// (src/util/write_microcanonical_observables.hpp:16-65), write_observables_to_file
+// (src/Thermodynamics/write_self_averaged_observables.hpp:15-59), write_nonlinear_obs_to_file
+// (src/Thermodynamics/write_nonlinear_observables.hpp:13-57).
+int rewl_write_microcanonical(const char* dir, const char* file_string, const char* header, const char* names,
+                              int32_t num_bins, int32_t num_obs, double system_size, const double* energies,
+                              const double* logdos, const double* obs)
+{
+    if (!logdos || !(system_size > 0)) return fail(REWL_EINVAL, "bad arguments");
+    return write_table(dir, "microcanonical_observables", file_string, header, "Intensive Observable Names by Column",
+                       {"Energy", "logDoS"}, names, num_bins, num_obs, energies, logdos, system_size, obs);
+}
+
+int rewl_write_self_averaged(const char* dir, const char* file_string, const char* header, const char* names,
+                             int32_t num_T, int32_t num_cols, const double* temperatures, const double* rows)
+{
+    return write_table(dir, "self_averaged_observables", file_string, header, "Intensive Observable Names by Column",
+                       {"Temperature"}, names, num_T, num_cols, temperatures, nullptr, 1.0, rows);
+}
+
+int rewl_write_nonlinear(const char* dir, const char* file_string, const char* header, const char* names,
+                         int32_t num_T, int32_t num_cols, const double* temperatures, const double* rows)
+{
+    return write_table(dir, "nonlinear_observables", file_string, header,
+                       "Intensive Nonlinear Observable Names by Column", {"Temperature"}, names, num_T, num_cols,
+                       temperatures, nullptr, 1.0, rows);
+}
+
+// The reference's post-processing of one instance (src/Simulation/main.cpp:241-365): concatenated,
+// normalised ln g and observables -> microcanonical file; canonical thermodynamics over the
+// temperature ladder (GPU, FP64) -> self-averaged file; susceptibilities and cumulants ->
+// nonlinear file.  Without observables the files carry the energy columns only.
+int rewl_write_outputs(rewl_engine* e, int32_t ii, const char* dir, const char* file_string, const char* header,
+                       double Tmin, double Tmax, int32_t num_T)
+{
+    if (!e || ii < 0 || ii >= (int)e->inst.size() || !dir || !file_string || num_T < 1) return fail(REWL_EINVAL, "bad arguments");
+    const HostInst& H = e->inst[ii];
+    const bool ising = H.d.model == REWL_MODEL_ISING2D;
+    const bool half = !ising && H.d.energy_max <= 0.0;
+    int n = 0;
+    rewl_global_logdos(e, ii, half ? 1 : 0, nullptr, nullptr, &n);
+    std::vector<double> E(n), G(n);
+    int rc = rewl_global_logdos(e, ii, half ? 1 : 0, E.data(), G.data(), &n);
+    if (rc) return rc;
+    const int cols = e->obs.p ? (ising ? 4 : 13) : 0;
+    std::vector<double> O((size_t)n * std::max(cols, 1));
+    if (cols && (rc = rewl_global_observables(e, ii, O.data(), &n))) return rc;
+    const char* sys_names = !cols ? "" : ising
+        ? "Magnetization\nMagnetization2\nMagnetization4\nCounts per Bin"
+        : "Sigma Mag\nSigma Mag2\nSigma Mag4\nTau Mag\nTau Mag2\nTau Mag4\nPhi\nPhi2\nPhi4\nBaxter\nBaxter2\nBaxter4\nCounts per Bin";
+    const double N = (double)H.dev.N;
+    if ((rc = rewl_write_microcanonical(dir, file_string, header, sys_names, n, cols, N, E.data(), G.data(), O.data())))
+        return rc;
+    std::vector<double> T(num_T), rows((size_t)num_T * (5 + cols));
+    rc = rewl_thermodynamics(E.data(), G.data(), cols ? O.data() : nullptr, n, cols, cols - 1, N, Tmin, Tmax, num_T, 1,
+                             e->desc.device, T.data(), rows.data());
+    if (rc) return fail(rc, "thermodynamics: %s", rewl_thermo_last_error_string());
+    const std::string thermal = std::string("Free Energy\nEnergy\nEnergy2\nEntropy\nSpecific Heat") + (cols ? "\n" : "") + sys_names;
+    if ((rc = rewl_write_self_averaged(dir, file_string, header, thermal.c_str(), num_T, 5 + cols, T.data(), rows.data())))
+        return rc;
+    if (!cols) return REWL_OK;
+    const int nl = ising ? 2 : 8;
+    std::vector<double> nonlin((size_t)num_T * nl);
+    if ((rc = rewl_nonlinear_observables(H.d.model, rows.data(), num_T, 5 + cols, T.data(), N, nonlin.data())))
+        return fail(rc, "nonlinear observables: %s", rewl_thermo_last_error_string());
+    const char* nl_names = ising ? "Susceptibility\nBinder Cumulant"
+                                 : "Sigma Susceptibility\nSigma Binder Cumulant\nTau Susceptibility\nTau Binder Cumulant\n"
+                                   "Baxter Susceptibility\nBaxter Binder Cumulant\nPhi Susceptibility\nPhi Binder Cumulant";
+    return rewl_write_nonlinear(dir, file_string, header, nl_names, num_T, nl, T.data(), nonlin.data());
 }
 
 int rewl_sweep_kernel_time(rewl_engine* e, double* ms, int64_t* launches)

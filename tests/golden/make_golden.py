@@ -21,6 +21,8 @@ Groups
               on the exact L = 16 Ising ln g with synthetic observables, and on a
               synthetic Ashkin-Teller-like spectrum with 12 moments, with and without
               the trapezoidal rule.
+  writers  -- the reference's three output writers (oracle/ref_writers.cpp) on
+              the thermo_ising inputs: tests/golden/writers/*.txt.
 """
 from __future__ import annotations
 
@@ -220,7 +222,37 @@ def gen_thermo():
             print("wrote", name)
 
 
+WRITER_HEADER = "# Model: 2D Ising, L = 16\n# REWL: 4 windows, 75 % overlap\n"
+WRITER_NAMES = "Magnetization\nMagnetization2\nMagnetization4\nCounts per Bin"
+THERMAL_NAMES = "Free Energy\nEnergy\nEnergy2\nEntropy\nSpecific Heat\n" + WRITER_NAMES
+
+
+def gen_writers():
+    import ctypes as C
+    lib = C.CDLL(str(build_ref.build_writers(force=True)))
+    lib.ref_write.argtypes = [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_size_t, C.c_size_t,
+                              C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+    z = np.load(OUT / "thermo_ising.npz")
+    d = OUT / "writers"
+    d.mkdir(exist_ok=True)
+    p = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.c_void_p)
+    E, lng, obs, out, T = z["E"], z["lng"], np.ascontiguousarray(z["obs"]), np.ascontiguousarray(z["out"]), z["temperatures"]
+    nl = np.ascontiguousarray(out[:, 5:7])
+    args = [(0, WRITER_NAMES, E.size, obs.shape[1], 256.0, E, lng, obs),
+            (1, THERMAL_NAMES, T.size, out.shape[1], 1.0, T, None, out),
+            (2, "Susceptibility\nBinder Cumulant", T.size, 2, 1.0, T, None, nl)]
+    keep = []
+    for kind, names, rows, cols, N, a, b, v in args:
+        arrs = [np.ascontiguousarray(a, dtype=np.float64), None if b is None else np.ascontiguousarray(b, dtype=np.float64),
+                np.ascontiguousarray(v, dtype=np.float64)]
+        keep.append(arrs)
+        lib.ref_write(kind, str(d).encode(), b"golden", WRITER_HEADER.encode(), names.encode(), rows, cols, N,
+                      arrs[0].ctypes.data_as(C.c_void_p), None if arrs[1] is None else arrs[1].ctypes.data_as(C.c_void_p),
+                      arrs[2].ctypes.data_as(C.c_void_p))
+    print("wrote", sorted(x.name for x in d.iterdir()))
+
+
 if __name__ == "__main__":
-    groups = sys.argv[1:] or ["replay", "glazier", "rng", "normalize", "exact", "thermo"]
+    groups = sys.argv[1:] or ["replay", "glazier", "rng", "normalize", "exact", "thermo", "writers"]
     for g in groups:
         globals()[f"gen_{g}"]()
