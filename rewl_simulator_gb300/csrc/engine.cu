@@ -118,6 +118,7 @@ struct DevPtrs {
     int32_t* cfg_M;          // 3 per configuration
     int64_t* fields;         // Baxter field per site (units)
     int64_t* g;
+    int64_t* gsnap;          // logDoS at the start of an Ashkin-Teller sweep launch
     uint32_t* H;
     uint64_t* visits;
     uint8_t* mask;
@@ -933,7 +934,12 @@ cudaError_t allow_bins_smem()
 }
 
 // Ashkin-Teller: sweep = sigma pass then tau pass (wang_landau.hpp:109-119); the
-// flavour toggles after each pass.  Tables stay in global memory.
+// flavour toggles after each pass.  A window holds tens of thousands of bins, so
+// its logDoS stays in global memory: each step reads g at the proposal and writes
+// g at the current bin, nothing else.  The counts and visits of the launch are
+// derived at its end from the change of g against a copy taken at its start
+// (every visit adds the same ln f), and the chain loads both possible proposals
+// of the next step one step ahead, so a load's latency overlaps a decision.
 struct StageAT {
     long long T[32];
     long long d0[32];
@@ -943,7 +949,7 @@ struct StageAT {
 };
 
 template <bool REPLAY>
-__global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
+__global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -965,8 +971,8 @@ __global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
     int8_t* gl = P.spins + P.cfg_off[cfg];
     for (int i = lane; i < 2 * N; i += 32) sig[i] = gl[i];
     long long* gg = reinterpret_cast<long long*>(P.g + P.slot_tab[s]);
-    uint32_t* gH = P.H + P.slot_tab[s];
-    uint64_t* gv = P.visits + P.slot_tab[s];
+    long long* g0 = reinterpret_cast<long long*>(P.gsnap + P.slot_tab[s]);
+    for (int k = lane; k < nb; k += 32) g0[k] = gg[k];
     __syncwarp();
 
     const long long J = I.J_u, K = I.K_u;
@@ -979,7 +985,7 @@ __global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
     int flavour = P.slot_flavour[s];
 
     long long E = 0;
-    int sm = 0, tm = 0, bx = 0, b = 0;
+    int sm = 0, tm = 0, bx = 0, b = 0, bmin = 0, bmax = -1;
     long long gc = 0;
     long long draws = 0, thr_off = 0, thr_n = 0;
     int err = 0;
@@ -989,6 +995,7 @@ __global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
         const long long gb = (((E - eglo) * mul) >> sh) - gblo;
         if (gb < 0 || gb >= nb) err = ERR_BOUNDS;
         b = (int)(err ? 0 : gb);
+        bmin = bmax = b;
         gc = gg[b];
         if (REPLAY) { draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
     }
@@ -1021,13 +1028,29 @@ __global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
                 __syncwarp();
                 unsigned acc = 0;
                 if (lane == 0) {
+                    // step j's proposal (En, bn) and its logDoS gn are known before step j
+                    // starts; during step j the two proposals step j+1 can make (step j
+                    // rejected: E0, accepted: E1) are loaded.  A load issued before step
+                    // j's write to bin b reads a stale value when it hits b: gc replaces it.
+                    long long En = E + st->d0[0];
+                    long long bn = (((En - eglo) * mul) >> sh) - gblo;
+                    bool inr = bn >= 0 && bn < nb;
+                    long long gn = gg[inr ? bn : b];
                     for (int j = 0; j < C; ++j) {
-                        long long dE = (j > 0 && ((acc >> (j - 1)) & 1u)) ? st->d1[j] : st->d0[j];
-                        dE += (acc & 1u) ? st->wc[j] : 0;
-                        const long long En = E + dE;
-                        const long long bn = (((En - eglo) * mul) >> sh) - gblo;
-                        const bool inr = bn >= 0 && bn < nb;
-                        const long long gn = gg[inr ? bn : b];
+                        long long E0 = 0, E1 = 0, b0 = 0, b1 = 0, G0 = 0, G1 = 0;
+                        bool i0 = false, i1 = false;
+                        if (j + 1 < C) {
+                            const long long w0 = (acc & 1u) ? st->wc[j + 1] : 0;
+                            const long long w1 = (j == 0 || (acc & 1u)) ? st->wc[j + 1] : 0;
+                            E0 = E + st->d0[j + 1] + w0;
+                            E1 = En + st->d1[j + 1] + w1;
+                            b0 = (((E0 - eglo) * mul) >> sh) - gblo;
+                            b1 = (((E1 - eglo) * mul) >> sh) - gblo;
+                            i0 = b0 >= 0 && b0 < nb;
+                            i1 = b1 >= 0 && b1 < nb;
+                            G0 = gg[i0 ? b0 : b];
+                            G1 = gg[i1 ? b1 : b];
+                        }
                         const long long d = gn - gc;
                         bool a;
                         if (!REPLAY) {
@@ -1041,9 +1064,14 @@ __global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
                         if (a) { E = En; b = (int)bn; gc = gn; acc |= 1u << j; }
                         gc += lnf;
                         gg[b] = gc;
-                        gH[b] += 1u;
-                        gv[b] += 1u;
+                        bmin = min(bmin, b);
+                        bmax = max(bmax, b);
                         if (P.obs) st->seq[j] = b;
+                        En = a ? E1 : E0;
+                        bn = a ? b1 : b0;
+                        inr = a ? i1 : i0;
+                        gn = a ? G1 : G0;
+                        if (bn == b) gn = gc;
                     }
                 }
                 acc = __shfl_sync(kFull, acc, 0);
@@ -1073,6 +1101,21 @@ __global__ void __launch_bounds__(256) k_sweep_at(const SweepParams p)
         }
     }
     for (int i = lane; i < 2 * N; i += 32) gl[i] = sig[i];
+    // counts and visits from the logDoS change over the bins the chain visited
+    // (lane 0's stores to g are ordered before the other lanes' loads by the barrier)
+    bmin = __shfl_sync(kFull, bmin, 0);
+    bmax = __shfl_sync(kFull, bmax, 0);
+    __syncwarp();
+    uint32_t* gH = P.H + P.slot_tab[s];
+    uint64_t* gv = P.visits + P.slot_tab[s];
+    for (int k = bmin + lane; k <= bmax; k += 32) {
+        const long long dg = gg[k] - g0[k];
+        if (dg != 0) {
+            const long long dv = dg / lnf;
+            gH[k] += (uint32_t)dv;
+            gv[k] += (uint64_t)dv;
+        }
+    }
     if (lane == 0) {
         P.cfg_E[cfg] = E;
         P.cfg_M[3 * cfg] = sm; P.cfg_M[3 * cfg + 1] = tm; P.cfg_M[3 * cfg + 2] = bx;
@@ -1399,6 +1442,7 @@ struct rewl_engine {
     DBuf<unsigned long long> stats;
     DBuf<int64_t> thr;
     DBuf<double> obs;           // per-bin observable sums (observables on)
+    DBuf<int64_t> gsnap;        // Ashkin-Teller engines: logDoS copy taken by each sweep launch
     int obs_stride = 0;
     std::vector<int64_t> h_thr_off, h_thr_n;
     std::vector<int64_t> h_fields;
@@ -1412,7 +1456,7 @@ struct rewl_engine {
         P.slot_nb = slot_nb.p; P.slot_flavour = slot_flavour.p; P.slot_sweeps = slot_sweeps.p;
         P.slot_draws = slot_draws.p; P.slot_thr_off = slot_thr_off.p; P.slot_thr_n = slot_thr_n.p; P.thr = thr.p;
         P.cfg_off = cfg_off.p; P.spins = spins.p; P.cfg_E = cfg_E.p; P.cfg_M = cfg_M.p; P.fields = fields.p;
-        P.g = g.p; P.H = H.p; P.visits = visits.p; P.mask = mask.p;
+        P.g = g.p; P.gsnap = gsnap.p; P.H = H.p; P.visits = visits.p; P.mask = mask.p;
         P.win_lnf = win_lnf.p; P.win_done = win_done.p; P.win_oot = win_oot.p; P.win_iter = win_iter.p;
         P.win_sweepctr = win_sweepctr.p; P.pairs = nullptr; P.counters = counters.p; P.stats = stats.p;
         P.obs = obs.p; P.obs_stride = obs_stride;
@@ -1675,9 +1719,10 @@ int upload_all(rewl_engine* e)
         CUDA_TRY(cudaMemsetAsync(e->H.p, 0, tab * sizeof(uint32_t), s));
         CUDA_TRY(cudaMemsetAsync(e->visits.p, 0, tab * sizeof(uint64_t), s));
     }
+    bool any_at = false;
+    for (const auto& hi : e->inst) any_at = any_at || hi.d.model == REWL_MODEL_ASHKIN_TELLER2D;
+    if (any_at && tab && (rc = e->gsnap.alloc(tab))) return rc;
     if (D.observables && tab) {
-        bool any_at = false;
-        for (const auto& hi : e->inst) any_at = any_at || hi.d.model == REWL_MODEL_ASHKIN_TELLER2D;
         e->obs_stride = any_at ? 12 : 3;
         if ((rc = e->obs.alloc((size_t)tab * e->obs_stride))) return rc;
         CUDA_TRY(cudaMemsetAsync(e->obs.p, 0, (size_t)tab * e->obs_stride * sizeof(double), s));
