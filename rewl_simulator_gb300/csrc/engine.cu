@@ -941,14 +941,77 @@ cudaError_t allow_bins_smem()
 // (every visit adds the same ln f), and the chain loads both possible proposals
 // of the next step one step ahead, so a load's latency overlaps a decision.
 struct StageAT {
-    long long T[32];
-    long long d0[32];
-    long long d1[32];
-    long long wc[32];
+    longlong2 du[32];        // per site: {proposal, proposal after its left neighbour flipped in this chunk}
+    long long T[32];         // acceptance thresholds of the chunk's sites
+    long long wcu;           // row-wrap correction of the last site when the chunk is a whole row
     int seq[32];             // bin after each step (observables)
 };
 
-template <bool REPLAY>
+// Chain state of one Ashkin-Teller walker (lane 0).  The energy is carried as its
+// position v = (E - E_lo) * bin_mul - gblo << bin_shift, in units of the bin
+// numerator within the window, so that a proposal's bin is (v + dv) >> bin_shift:
+// one add and one shift instead of a multiply per candidate.
+struct ChainAT {
+    long long v, vn, gc, gn, draws;
+    int b, bn, err;
+    bool inr;
+    unsigned acc;
+};
+
+// One step j of the chunk.  On entry (vn, bn, inr, gn) is step j's proposal and its
+// logDoS; with PREFETCH the two proposals of step j+1 (step j rejected: from v;
+// accepted: from vn) are loaded before step j's decision.  A value loaded before
+// step j's write to bin b is stale exactly when the proposal is b: gc replaces it.
+// WRAPFIX: step j+1 is the last site of a whole-row chunk, whose right neighbour
+// is the row's first site, flipped in this chunk iff bit 0 of acc.
+template <bool REPLAY, bool OBS, bool PREFETCH, bool WRAPFIX>
+__device__ __forceinline__ void at_step(ChainAT& c, const int j, StageAT* st, long long* gg, const int nb,
+                                        const int sh, const long long lnf, const DevPtrs& P,
+                                        const long long thr_off, const long long thr_n)
+{
+    long long t0 = 0, t1 = 0, G0 = 0, G1 = 0;
+    int b0 = 0, b1 = 0;
+    bool i0 = false, i1 = false;
+    if (PREFETCH) {
+        const longlong2 q = st->du[j + 1];
+        t0 = c.v + q.x;
+        t1 = c.vn + q.y;
+        if (WRAPFIX) {
+            const long long wcu = st->wcu;
+            if (c.acc & 1u) t0 += wcu;
+            if (j == 0 || (c.acc & 1u)) t1 += wcu;
+        }
+        b0 = (int)(t0 >> sh);
+        b1 = (int)(t1 >> sh);
+        i0 = (unsigned)b0 < (unsigned)nb;
+        i1 = (unsigned)b1 < (unsigned)nb;
+        G0 = gg[min((unsigned)b0, (unsigned)(nb - 1))];
+        G1 = gg[min((unsigned)b1, (unsigned)(nb - 1))];
+    }
+    const long long d = c.gn - c.gc;
+    bool a;
+    if (!REPLAY) {
+        a = c.inr && (d < st->T[j]);
+    } else if (c.inr && d > 0) {
+        if (c.draws >= thr_n) { c.err = ERR_REPLAY_EXHAUSTED; a = false; }
+        else { a = d < P.thr[thr_off + c.draws]; ++c.draws; }
+    } else {
+        a = c.inr;
+    }
+    if (a) { c.v = c.vn; c.b = c.bn; c.gc = c.gn; c.acc |= 1u << j; }
+    c.gc += lnf;
+    gg[c.b] = c.gc;
+    if (OBS) st->seq[j] = c.b;
+    if (PREFETCH) {
+        c.vn = a ? t1 : t0;
+        c.bn = a ? b1 : b0;
+        c.inr = a ? i1 : i0;
+        c.gn = a ? G1 : G0;
+        if (c.bn == c.b) c.gn = c.gc;
+    }
+}
+
+template <bool REPLAY, bool OBS>
 __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -980,24 +1043,25 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
     const uint64_t sweeps0 = P.slot_sweeps[s];
     const uint32_t uid = (uint32_t)(s - I.first_slot);
     const uint64_t seed = I.seed;
-    const long long eglo = I.eglo_u, mul = I.bin_mul, gblo = W.gblo;
+    const long long eglo = I.eglo_u, mul = I.bin_mul;
     const int sh = I.bin_shift;
+    const long long vlo = (long long)W.gblo << sh;     // window start in bin-numerator units
+    const bool wraps = C == L;
     int flavour = P.slot_flavour[s];
 
-    long long E = 0;
-    int sm = 0, tm = 0, bx = 0, b = 0, bmin = 0, bmax = -1;
-    long long gc = 0;
-    long long draws = 0, thr_off = 0, thr_n = 0;
+    ChainAT c{};
+    int sm = 0, tm = 0, bx = 0;
+    long long thr_off = 0, thr_n = 0;
     int err = 0;
     if (lane == 0) {
-        E = P.cfg_E[cfg];
+        const long long E = P.cfg_E[cfg];
         sm = P.cfg_M[3 * cfg]; tm = P.cfg_M[3 * cfg + 1]; bx = P.cfg_M[3 * cfg + 2];
-        const long long gb = (((E - eglo) * mul) >> sh) - gblo;
+        c.v = (E - eglo) * mul - vlo;
+        const long long gb = c.v >> sh;
         if (gb < 0 || gb >= nb) err = ERR_BOUNDS;
-        b = (int)(err ? 0 : gb);
-        bmin = bmax = b;
-        gc = gg[b];
-        if (REPLAY) { draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
+        c.b = (int)(err ? 0 : gb);
+        c.gc = gg[c.b];
+        if (REPLAY) { c.draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
     }
     err = __shfl_sync(kFull, err, 0);
     if (err) {
@@ -1017,70 +1081,40 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
                     ai = A[i]; bi = B[i];
                     const int l = nb_left(i, L), r = nb_right(i, L);
                     const long long d0 = at_dE(A, B, i, L, J, K, hf ? hf[i] : 0);
-                    st->d0[lane] = d0;
-                    st->d1[lane] = lane > 0 ? d0 - 4 * (long long)ai * A[l] * (J + K * (long long)bi * B[l]) : d0;
-                    st->wc[lane] = (C == L && lane == L - 1) ? -4 * (long long)ai * A[r] * (J + K * (long long)bi * B[r]) : 0;
+                    const long long d1 = lane > 0 ? d0 - 4 * (long long)ai * A[l] * (J + K * (long long)bi * B[l]) : d0;
+                    st->du[lane] = make_longlong2(d0 * mul, d1 * mul);
+                    if (wraps && lane == C - 1) st->wcu = -4 * (long long)ai * A[r] * (J + K * (long long)bi * B[r]) * mul;
                     if (!REPLAY) {
                         const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)i, kStreamWL);
                         st->T[lane] = accept_threshold(neglog_u32(word));
                     }
                 }
                 __syncwarp();
-                unsigned acc = 0;
                 if (lane == 0) {
-                    // step j's proposal (En, bn) and its logDoS gn are known before step j
-                    // starts; during step j the two proposals step j+1 can make (step j
-                    // rejected: E0, accepted: E1) are loaded.  A load issued before step
-                    // j's write to bin b reads a stale value when it hits b: gc replaces it.
-                    long long En = E + st->d0[0];
-                    long long bn = (((En - eglo) * mul) >> sh) - gblo;
-                    bool inr = bn >= 0 && bn < nb;
-                    long long gn = gg[inr ? bn : b];
-                    for (int j = 0; j < C; ++j) {
-                        long long E0 = 0, E1 = 0, b0 = 0, b1 = 0, G0 = 0, G1 = 0;
-                        bool i0 = false, i1 = false;
-                        if (j + 1 < C) {
-                            const long long w0 = (acc & 1u) ? st->wc[j + 1] : 0;
-                            const long long w1 = (j == 0 || (acc & 1u)) ? st->wc[j + 1] : 0;
-                            E0 = E + st->d0[j + 1] + w0;
-                            E1 = En + st->d1[j + 1] + w1;
-                            b0 = (((E0 - eglo) * mul) >> sh) - gblo;
-                            b1 = (((E1 - eglo) * mul) >> sh) - gblo;
-                            i0 = b0 >= 0 && b0 < nb;
-                            i1 = b1 >= 0 && b1 < nb;
-                            G0 = gg[i0 ? b0 : b];
-                            G1 = gg[i1 ? b1 : b];
-                        }
-                        const long long d = gn - gc;
-                        bool a;
-                        if (!REPLAY) {
-                            a = inr && (d < st->T[j]);
-                        } else {
-                            if (inr && d > 0) {
-                                if (draws >= thr_n) { err = ERR_REPLAY_EXHAUSTED; a = false; }
-                                else { a = d < P.thr[thr_off + draws]; ++draws; }
-                            } else a = inr;
-                        }
-                        if (a) { E = En; b = (int)bn; gc = gn; acc |= 1u << j; }
-                        gc += lnf;
-                        gg[b] = gc;
-                        bmin = min(bmin, b);
-                        bmax = max(bmax, b);
-                        if (P.obs) st->seq[j] = b;
-                        En = a ? E1 : E0;
-                        bn = a ? b1 : b0;
-                        inr = a ? i1 : i0;
-                        gn = a ? G1 : G0;
-                        if (bn == b) gn = gc;
+                    c.acc = 0;
+                    c.vn = c.v + st->du[0].x;
+                    c.bn = (int)(c.vn >> sh);
+                    c.inr = (unsigned)c.bn < (unsigned)nb;
+                    c.gn = gg[min((unsigned)c.bn, (unsigned)(nb - 1))];
+                    if (C == 1) {
+                        at_step<REPLAY, OBS, false, false>(c, 0, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                    } else {
+#pragma unroll 4
+                        for (int j = 0; j < C - 2; ++j)
+                            at_step<REPLAY, OBS, true, false>(c, j, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        if (wraps) at_step<REPLAY, OBS, true, true>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        else at_step<REPLAY, OBS, true, false>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        at_step<REPLAY, OBS, false, false>(c, C - 1, st, gg, nb, sh, lnf, P, thr_off, thr_n);
                     }
                 }
-                acc = __shfl_sync(kFull, acc, 0);
+                const unsigned acc = __shfl_sync(kFull, c.acc, 0);
                 const unsigned aplus = __ballot_sync(kFull, lane < C && ai > 0);
                 const unsigned abplus = __ballot_sync(kFull, lane < C && ai * bi > 0);
-                if (P.obs) {
+                if (OBS) {
                     // magnetisations after each step of the chunk, from lane 0's values before it
                     const int sm0 = __shfl_sync(kFull, sm, 0), tm0 = __shfl_sync(kFull, tm, 0);
                     const int bx0 = __shfl_sync(kFull, bx, 0);
+                    __syncwarp();
                     if (lane < C) {
                         const int da = chunk_dm(acc, aplus, lane), db = chunk_dm(acc, abplus, lane);
                         obs_add_at(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
@@ -1101,14 +1135,12 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
         }
     }
     for (int i = lane; i < 2 * N; i += 32) gl[i] = sig[i];
-    // counts and visits from the logDoS change over the bins the chain visited
-    // (lane 0's stores to g are ordered before the other lanes' loads by the barrier)
-    bmin = __shfl_sync(kFull, bmin, 0);
-    bmax = __shfl_sync(kFull, bmax, 0);
+    // counts and visits from the logDoS change (lane 0's stores to g are ordered
+    // before the other lanes' loads by the barrier)
     __syncwarp();
     uint32_t* gH = P.H + P.slot_tab[s];
     uint64_t* gv = P.visits + P.slot_tab[s];
-    for (int k = bmin + lane; k <= bmax; k += 32) {
+    for (int k = lane; k < nb; k += 32) {
         const long long dg = gg[k] - g0[k];
         if (dg != 0) {
             const long long dv = dg / lnf;
@@ -1117,12 +1149,12 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
         }
     }
     if (lane == 0) {
-        P.cfg_E[cfg] = E;
+        P.cfg_E[cfg] = eglo + (c.v + vlo) / mul;
         P.cfg_M[3 * cfg] = sm; P.cfg_M[3 * cfg + 1] = tm; P.cfg_M[3 * cfg + 2] = bx;
         P.slot_sweeps[s] = sweeps0 + (uint64_t)p.nsweeps;
         P.slot_flavour[s] = flavour;
-        if (REPLAY) P.slot_draws[s] = draws;
-        if (err) atomicOr(&P.counters[0], err);
+        if (REPLAY) P.slot_draws[s] = c.draws;
+        if (c.err) atomicOr(&P.counters[0], c.err);
     }
 }
 
@@ -1402,8 +1434,17 @@ struct Launch {
     int bins = 0;           // Ising bin-tracking kernel with `walkers_per_warp` walkers per warp and chunk `chunk`
     int walkers_per_warp = 1;
     int chunk = 32;
+    int carveout = -1;      // Ashkin-Teller: shared-memory carveout (percent) that leaves the rest to L1
     DBuf<int32_t> d_slots;
 };
+
+using SweepKernel = void (*)(const SweepParams);
+
+SweepKernel at_kernel(bool replay, bool obs)
+{
+    if (replay) return obs ? k_sweep_at<true, true> : k_sweep_at<true, false>;
+    return obs ? k_sweep_at<false, true> : k_sweep_at<false, false>;
+}
 
 } // namespace
 
@@ -1828,8 +1869,26 @@ int plan_launches(rewl_engine* e)
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-    CUDA_TRY(cudaFuncSetAttribute(k_sweep_at<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-    CUDA_TRY(cudaFuncSetAttribute(k_sweep_at<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    for (int r = 0; r < 2; ++r)
+        for (int o = 0; o < 2; ++o)
+            CUDA_TRY(cudaFuncSetAttribute(at_kernel(r, o), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    for (auto& l : e->launches) {
+        if (l.bins || l.model == REWL_MODEL_ISING2D) continue;
+        // The logDoS tables of this kernel live in global memory and are read through
+        // L1, so the shared-memory carveout is the smallest that still holds the
+        // blocks resident on an SM; the driver's default leaves L1 far less.
+        const SweepKernel fn = at_kernel(e->desc.rng_mode == REWL_RNG_REPLAY, e->desc.observables != 0);
+        const int threads = 32 * l.wpb;
+        const size_t smem = (size_t)l.wpb * l.smem_per_warp;
+        int occ = 0;
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem));
+        const int blocks = ((int)l.slots.size() + l.wpb - 1) / l.wpb;
+        const int per_sm = std::max(1, std::min(occ, (blocks + nsm - 1) / nsm));
+        int smem_sm = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->desc.device));
+        const size_t need = (size_t)per_sm * (smem + 1024);
+        l.carveout = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / (size_t)smem_sm);
+    }
     CUDA_TRY(allow_bins_smem<1>());
     CUDA_TRY(allow_bins_smem<2>());
     CUDA_TRY(allow_bins_smem<4>());
@@ -1889,8 +1948,9 @@ int launch_sweeps(rewl_engine* e, int nsweeps)
             else if (e->sweep_variant == 2) k_sweep_ising<false, 2><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
             else k_sweep_ising<false, 3><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
         } else {
-            if (replay) k_sweep_at<true><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
-            else k_sweep_at<false><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+            const SweepKernel fn = at_kernel(replay, e->desc.observables != 0);
+            if (l.carveout >= 0) CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, l.carveout));
+            fn<<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
         }
         CUDA_TRY(cudaGetLastError());
         e->kernel_launches++;
