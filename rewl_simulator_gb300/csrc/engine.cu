@@ -952,30 +952,38 @@ struct StageAT {
 // numerator within the window, so that a proposal's bin is (v + dv) >> bin_shift:
 // one add and one shift instead of a multiply per candidate.
 struct ChainAT {
-    long long v, vn, gc, gn, draws;
+    long long v, vn, gc, draws;
+    long long G0, G1;        // logDoS loaded for step j's proposal if step j-1 was rejected / accepted
+    long long T;             // step j's threshold
+    longlong2 q;             // step j+1's proposals
     int b, bn, err;
-    bool inr;
+    bool inr, ap;            // step j's proposal in the window; step j-1 accepted
     unsigned acc;
 };
 
-// One step j of the chunk.  On entry (vn, bn, inr, gn) is step j's proposal and its
-// logDoS; with PREFETCH the two proposals of step j+1 (step j rejected: from v;
-// accepted: from vn) are loaded before step j's decision.  A value loaded before
-// step j's write to bin b is stale exactly when the proposal is b: gc replaces it.
+// One step j of the chunk, software-pipelined two deep.  On entry (vn, bn, inr) is
+// step j's proposal, and its logDoS is G1 or G0 (as step j-1 was accepted or not),
+// loaded during step j-1.  With PREFETCH the two proposals of step j+1 (step j
+// rejected: from v; accepted: from vn) are loaded first, before step j waits on
+// its own loads, so two steps' loads are in flight at once.  A value loaded before
+// step j-1's write to bin b is stale exactly when the proposal is b: gc replaces
+// it.  LOADQ: step j+2 exists and its proposals are read from shared memory now.
 // WRAPFIX: step j+1 is the last site of a whole-row chunk, whose right neighbour
 // is the row's first site, flipped in this chunk iff bit 0 of acc.
-template <bool REPLAY, bool OBS, bool PREFETCH, bool WRAPFIX>
+template <bool REPLAY, bool OBS, bool PREFETCH, bool LOADQ, bool WRAPFIX>
 __device__ __forceinline__ void at_step(ChainAT& c, const int j, StageAT* st, long long* gg, const int nb,
                                         const int sh, const long long lnf, const DevPtrs& P,
                                         const long long thr_off, const long long thr_n)
 {
-    long long t0 = 0, t1 = 0, G0 = 0, G1 = 0;
+    long long t0 = 0, t1 = 0, G0 = 0, G1 = 0, Tn = 0;
+    longlong2 qn = make_longlong2(0, 0);
     int b0 = 0, b1 = 0;
     bool i0 = false, i1 = false;
+    if (LOADQ) qn = st->du[j + 2];
     if (PREFETCH) {
-        const longlong2 q = st->du[j + 1];
-        t0 = c.v + q.x;
-        t1 = c.vn + q.y;
+        if (!REPLAY) Tn = st->T[j + 1];
+        t0 = c.v + c.q.x;
+        t1 = c.vn + c.q.y;
         if (WRAPFIX) {
             const long long wcu = st->wcu;
             if (c.acc & 1u) t0 += wcu;
@@ -988,17 +996,18 @@ __device__ __forceinline__ void at_step(ChainAT& c, const int j, StageAT* st, lo
         G0 = gg[min((unsigned)b0, (unsigned)(nb - 1))];
         G1 = gg[min((unsigned)b1, (unsigned)(nb - 1))];
     }
-    const long long d = c.gn - c.gc;
+    const long long gn = c.bn == c.b ? c.gc : (c.ap ? c.G1 : c.G0);
+    const long long d = gn - c.gc;
     bool a;
     if (!REPLAY) {
-        a = c.inr && (d < st->T[j]);
+        a = c.inr && (d < c.T);
     } else if (c.inr && d > 0) {
         if (c.draws >= thr_n) { c.err = ERR_REPLAY_EXHAUSTED; a = false; }
         else { a = d < P.thr[thr_off + c.draws]; ++c.draws; }
     } else {
         a = c.inr;
     }
-    if (a) { c.v = c.vn; c.b = c.bn; c.gc = c.gn; c.acc |= 1u << j; }
+    if (a) { c.v = c.vn; c.b = c.bn; c.gc = gn; c.acc |= 1u << j; }
     c.gc += lnf;
     gg[c.b] = c.gc;
     if (OBS) st->seq[j] = c.b;
@@ -1006,8 +1015,9 @@ __device__ __forceinline__ void at_step(ChainAT& c, const int j, StageAT* st, lo
         c.vn = a ? t1 : t0;
         c.bn = a ? b1 : b0;
         c.inr = a ? i1 : i0;
-        c.gn = a ? G1 : G0;
-        if (c.bn == c.b) c.gn = c.gc;
+        c.G0 = G0; c.G1 = G1; c.ap = a;
+        c.T = Tn;
+        c.q = qn;
     }
 }
 
@@ -1095,16 +1105,19 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
                     c.vn = c.v + st->du[0].x;
                     c.bn = (int)(c.vn >> sh);
                     c.inr = (unsigned)c.bn < (unsigned)nb;
-                    c.gn = gg[min((unsigned)c.bn, (unsigned)(nb - 1))];
+                    c.G0 = c.G1 = gg[min((unsigned)c.bn, (unsigned)(nb - 1))];
+                    c.ap = false;
+                    if (!REPLAY) c.T = st->T[0];
                     if (C == 1) {
-                        at_step<REPLAY, OBS, false, false>(c, 0, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        at_step<REPLAY, OBS, false, false, false>(c, 0, st, gg, nb, sh, lnf, P, thr_off, thr_n);
                     } else {
+                        c.q = st->du[1];
 #pragma unroll 4
                         for (int j = 0; j < C - 2; ++j)
-                            at_step<REPLAY, OBS, true, false>(c, j, st, gg, nb, sh, lnf, P, thr_off, thr_n);
-                        if (wraps) at_step<REPLAY, OBS, true, true>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
-                        else at_step<REPLAY, OBS, true, false>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
-                        at_step<REPLAY, OBS, false, false>(c, C - 1, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                            at_step<REPLAY, OBS, true, true, false>(c, j, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        if (wraps) at_step<REPLAY, OBS, true, false, true>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        else at_step<REPLAY, OBS, true, false, false>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        at_step<REPLAY, OBS, false, false, false>(c, C - 1, st, gg, nb, sh, lnf, P, thr_off, thr_n);
                     }
                 }
                 const unsigned acc = __shfl_sync(kFull, c.acc, 0);
