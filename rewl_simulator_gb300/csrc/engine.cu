@@ -938,26 +938,19 @@ cudaError_t allow_bins_smem()
 // its logDoS stays in global memory: each step reads g at the proposal and writes
 // g at the current bin, nothing else.  The counts and visits of the launch are
 // derived at its end from the change of g against a copy taken at its start
-// (every visit adds the same ln f).  All 32 lanes run the walker's chain in
-// lockstep (the same loads, decisions and stores), which costs no more issue
-// slots than one lane and leaves each lane free to prefetch a different bin.
+// (every visit adds the same ln f), and the chain loads both possible proposals
+// of the next step one step ahead, so a load's latency overlaps a decision.
 struct StageAT {
     longlong2 du[32];        // per site: {proposal, proposal after its left neighbour flipped in this chunk}
     long long T[32];         // acceptance thresholds of the chunk's sites
-    int2 db[32];             // the proposals' bin offsets, rounded down (prefetch addresses only)
     long long wcu;           // row-wrap correction of the last site when the chunk is a whole row
     int seq[32];             // bin after each step (observables)
 };
 
-__device__ __forceinline__ void prefetch_l1(const void* p)
-{
-    asm volatile("prefetch.L1 [%0];" ::"l"(p));
-}
-
-// Chain state of one Ashkin-Teller walker.  The energy is carried as its position
-// v = (E - E_lo) * bin_mul - gblo << bin_shift, in units of the bin numerator
-// within the window, so that a proposal's bin is (v + dv) >> bin_shift: one add
-// and one shift instead of a multiply per candidate.
+// Chain state of one Ashkin-Teller walker (lane 0).  The energy is carried as its
+// position v = (E - E_lo) * bin_mul - gblo << bin_shift, in units of the bin
+// numerator within the window, so that a proposal's bin is (v + dv) >> bin_shift:
+// one add and one shift instead of a multiply per candidate.
 struct ChainAT {
     long long v, vn, gc, draws;
     long long G0, G1;        // logDoS loaded for step j's proposal if step j-1 was rejected / accepted
@@ -968,24 +961,19 @@ struct ChainAT {
     unsigned acc;
 };
 
-// One step j of the chunk, software-pipelined.  On entry (vn, bn, inr) is step j's
-// proposal, and its logDoS is G1 or G0 (as step j-1 was accepted or not), loaded
-// during step j-1.  With PREFETCH the two proposals of step j+1 (step j rejected:
-// from v; accepted: from vn) are loaded first, before step j waits on its own
-// loads.  A value loaded before step j-1's write to bin b is stale exactly when
-// the proposal is b; the proposal then stays in the current bin and is accepted
-// (d = 0 < T).  Otherwise the test d = G - gc < T is evaluated as G - T < gc, so
-// that only a compare and a select lie between one step's gc and the next.
-// LOADQ: step j+2 exists and its proposals are read from shared memory now.
+// One step j of the chunk, software-pipelined two deep.  On entry (vn, bn, inr) is
+// step j's proposal, and its logDoS is G1 or G0 (as step j-1 was accepted or not),
+// loaded during step j-1.  With PREFETCH the two proposals of step j+1 (step j
+// rejected: from v; accepted: from vn) are loaded first, before step j waits on
+// its own loads, so two steps' loads are in flight at once.  A value loaded before
+// step j-1's write to bin b is stale exactly when the proposal is b: gc replaces
+// it.  LOADQ: step j+2 exists and its proposals are read from shared memory now.
 // WRAPFIX: step j+1 is the last site of a whole-row chunk, whose right neighbour
 // is the row's first site, flipped in this chunk iff bit 0 of acc.
-// AHEAD: step j+3 exists; lane bits 0-2 pick the outcomes of steps j, j+1, j+2 and
-// each lane prefetches the bin of the proposal step j+3 makes on that path
-// (offsets rounded to whole bins: a prefetch address needs no exactness).
-template <bool REPLAY, bool OBS, bool PREFETCH, bool LOADQ, bool WRAPFIX, bool AHEAD>
+template <bool REPLAY, bool OBS, bool PREFETCH, bool LOADQ, bool WRAPFIX>
 __device__ __forceinline__ void at_step(ChainAT& c, const int j, StageAT* st, long long* gg, const int nb,
                                         const int sh, const long long lnf, const DevPtrs& P,
-                                        const long long thr_off, const long long thr_n, const int lane)
+                                        const long long thr_off, const long long thr_n)
 {
     long long t0 = 0, t1 = 0, G0 = 0, G1 = 0, Tn = 0;
     longlong2 qn = make_longlong2(0, 0);
@@ -1008,37 +996,21 @@ __device__ __forceinline__ void at_step(ChainAT& c, const int j, StageAT* st, lo
         G0 = gg[min((unsigned)b0, (unsigned)(nb - 1))];
         G1 = gg[min((unsigned)b1, (unsigned)(nb - 1))];
     }
-    if (AHEAD) {
-        const int2 q2 = st->db[j + 2], q3 = st->db[j + 3];
-        int pb = (lane & 1) ? c.bn : c.b;
-        int pc = (lane & 1) ? b1 : b0;
-        pb = (lane & 2) ? pc : pb;
-        pc = pb + ((lane & 2) ? q2.y : q2.x);
-        pb = (lane & 4) ? pc : pb;
-        pc = pb + ((lane & 4) ? q3.y : q3.x);
-        prefetch_l1(gg + min((unsigned)pc, (unsigned)(nb - 1)));
-    }
-    const bool stale = c.bn == c.b;
-    const long long Gs = c.ap ? c.G1 : c.G0;
-    bool a, take;
+    const long long gn = c.bn == c.b ? c.gc : (c.ap ? c.G1 : c.G0);
+    const long long d = gn - c.gc;
+    bool a;
     if (!REPLAY) {
-        const bool lt = Gs - c.T < c.gc;
-        a = c.inr && (stale || lt);
-        take = c.inr && !stale && lt;
+        a = c.inr && (d < c.T);
+    } else if (c.inr && d > 0) {
+        if (c.draws >= thr_n) { c.err = ERR_REPLAY_EXHAUSTED; a = false; }
+        else { a = d < P.thr[thr_off + c.draws]; ++c.draws; }
     } else {
-        const long long d = stale ? 0 : Gs - c.gc;
-        if (c.inr && d > 0) {
-            if (c.draws >= thr_n) { c.err = ERR_REPLAY_EXHAUSTED; a = false; }
-            else { a = d < P.thr[thr_off + c.draws]; ++c.draws; }
-        } else {
-            a = c.inr;
-        }
-        take = a && !stale;
+        a = c.inr;
     }
-    c.gc = take ? Gs + lnf : c.gc + lnf;
-    if (a) { c.v = c.vn; c.b = c.bn; c.acc |= 1u << j; }
+    if (a) { c.v = c.vn; c.b = c.bn; c.gc = gn; c.acc |= 1u << j; }
+    c.gc += lnf;
     gg[c.b] = c.gc;
-    if (OBS && lane == 0) st->seq[j] = c.b;
+    if (OBS) st->seq[j] = c.b;
     if (PREFETCH) {
         c.vn = a ? t1 : t0;
         c.bn = a ? b1 : b0;
@@ -1087,22 +1059,25 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
     const bool wraps = C == L;
     int flavour = P.slot_flavour[s];
 
-    // every lane holds the same chain state
     ChainAT c{};
-    const long long E0 = P.cfg_E[cfg];
-    int sm = P.cfg_M[3 * cfg], tm = P.cfg_M[3 * cfg + 1], bx = P.cfg_M[3 * cfg + 2];
-    c.v = (E0 - eglo) * mul - vlo;
-    {
-        const long long gb = c.v >> sh;
-        if (gb < 0 || gb >= nb) {
-            if (lane == 0) atomicOr(&P.counters[0], ERR_BOUNDS);
-            return;
-        }
-        c.b = (int)gb;
-    }
-    c.gc = gg[c.b];
+    int sm = 0, tm = 0, bx = 0;
     long long thr_off = 0, thr_n = 0;
-    if (REPLAY) { c.draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
+    int err = 0;
+    if (lane == 0) {
+        const long long E = P.cfg_E[cfg];
+        sm = P.cfg_M[3 * cfg]; tm = P.cfg_M[3 * cfg + 1]; bx = P.cfg_M[3 * cfg + 2];
+        c.v = (E - eglo) * mul - vlo;
+        const long long gb = c.v >> sh;
+        if (gb < 0 || gb >= nb) err = ERR_BOUNDS;
+        c.b = (int)(err ? 0 : gb);
+        c.gc = gg[c.b];
+        if (REPLAY) { c.draws = P.slot_draws[s]; thr_off = P.slot_thr_off[s]; thr_n = P.slot_thr_n[s]; }
+    }
+    err = __shfl_sync(kFull, err, 0);
+    if (err) {
+        if (lane == 0) atomicOr(&P.counters[0], err);
+        return;
+    }
 
     for (int sw = 0; sw < p.nsweeps; ++sw) {
         for (int pass = 0; pass < 2; ++pass) {
@@ -1117,9 +1092,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
                     const int l = nb_left(i, L), r = nb_right(i, L);
                     const long long d0 = at_dE(A, B, i, L, J, K, hf ? hf[i] : 0);
                     const long long d1 = lane > 0 ? d0 - 4 * (long long)ai * A[l] * (J + K * (long long)bi * B[l]) : d0;
-                    const long long u0 = d0 * mul, u1 = d1 * mul;
-                    st->du[lane] = make_longlong2(u0, u1);
-                    st->db[lane] = make_int2((int)(u0 >> sh), (int)(u1 >> sh));
+                    st->du[lane] = make_longlong2(d0 * mul, d1 * mul);
                     if (wraps && lane == C - 1) st->wcu = -4 * (long long)ai * A[r] * (J + K * (long long)bi * B[r]) * mul;
                     if (!REPLAY) {
                         const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)i, kStreamWL);
@@ -1127,50 +1100,56 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
                     }
                 }
                 __syncwarp();
-                c.acc = 0;
-                c.vn = c.v + st->du[0].x;
-                c.bn = (int)(c.vn >> sh);
-                c.inr = (unsigned)c.bn < (unsigned)nb;
-                c.G0 = c.G1 = gg[min((unsigned)c.bn, (unsigned)(nb - 1))];
-                c.ap = false;
-                if (!REPLAY) c.T = st->T[0];
-                if (C == 1) {
-                    at_step<REPLAY, OBS, false, false, false, false>(c, 0, st, gg, nb, sh, lnf, P, thr_off, thr_n, lane);
-                } else {
-                    c.q = st->du[1];
+                if (lane == 0) {
+                    c.acc = 0;
+                    c.vn = c.v + st->du[0].x;
+                    c.bn = (int)(c.vn >> sh);
+                    c.inr = (unsigned)c.bn < (unsigned)nb;
+                    c.G0 = c.G1 = gg[min((unsigned)c.bn, (unsigned)(nb - 1))];
+                    c.ap = false;
+                    if (!REPLAY) c.T = st->T[0];
+                    if (C == 1) {
+                        at_step<REPLAY, OBS, false, false, false>(c, 0, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                    } else {
+                        c.q = st->du[1];
 #pragma unroll 4
-                    for (int j = 0; j < C - 3; ++j)
-                        at_step<REPLAY, OBS, true, true, false, true>(c, j, st, gg, nb, sh, lnf, P, thr_off, thr_n, lane);
-                    if (C >= 3) at_step<REPLAY, OBS, true, true, false, false>(c, C - 3, st, gg, nb, sh, lnf, P, thr_off, thr_n, lane);
-                    if (wraps) at_step<REPLAY, OBS, true, false, true, false>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n, lane);
-                    else at_step<REPLAY, OBS, true, false, false, false>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n, lane);
-                    at_step<REPLAY, OBS, false, false, false, false>(c, C - 1, st, gg, nb, sh, lnf, P, thr_off, thr_n, lane);
+                        for (int j = 0; j < C - 2; ++j)
+                            at_step<REPLAY, OBS, true, true, false>(c, j, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        if (wraps) at_step<REPLAY, OBS, true, false, true>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        else at_step<REPLAY, OBS, true, false, false>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        at_step<REPLAY, OBS, false, false, false>(c, C - 1, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                    }
                 }
-                const unsigned acc = c.acc;
+                const unsigned acc = __shfl_sync(kFull, c.acc, 0);
                 const unsigned aplus = __ballot_sync(kFull, lane < C && ai > 0);
                 const unsigned abplus = __ballot_sync(kFull, lane < C && ai * bi > 0);
                 if (OBS) {
-                    // magnetisations after each step of the chunk, from the values before it
+                    // magnetisations after each step of the chunk, from lane 0's values before it
+                    const int sm0 = __shfl_sync(kFull, sm, 0), tm0 = __shfl_sync(kFull, tm, 0);
+                    const int bx0 = __shfl_sync(kFull, bx, 0);
                     __syncwarp();
                     if (lane < C) {
                         const int da = chunk_dm(acc, aplus, lane), db = chunk_dm(acc, abplus, lane);
                         obs_add_at(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
-                                   flavour == 0 ? sm + da : sm, flavour == 0 ? tm : tm + da, bx + db,
+                                   flavour == 0 ? sm0 + da : sm0, flavour == 0 ? tm0 : tm0 + da, bx0 + db,
                                    1.0 / (double)N);
                     }
                 }
                 if (lane < C && ((acc >> lane) & 1u)) A[c0 + lane] = (int8_t)(-ai);
-                const int da = -2 * ((int)__popc(acc & aplus) - (int)__popc(acc & ~aplus));
-                const int db = -2 * ((int)__popc(acc & abplus) - (int)__popc(acc & ~abplus));
-                if (flavour == 0) sm += da; else tm += da;
-                bx += db;
+                if (lane == 0) {
+                    const int da = -2 * ((int)__popc(acc & aplus) - (int)__popc(acc & ~aplus));
+                    const int db = -2 * ((int)__popc(acc & abplus) - (int)__popc(acc & ~abplus));
+                    if (flavour == 0) sm += da; else tm += da;
+                    bx += db;
+                }
                 __syncwarp();
             }
             flavour ^= 1;
         }
     }
     for (int i = lane; i < 2 * N; i += 32) gl[i] = sig[i];
-    // counts and visits from the logDoS change
+    // counts and visits from the logDoS change (lane 0's stores to g are ordered
+    // before the other lanes' loads by the barrier)
     __syncwarp();
     uint32_t* gH = P.H + P.slot_tab[s];
     uint64_t* gv = P.visits + P.slot_tab[s];
