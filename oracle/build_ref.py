@@ -103,17 +103,20 @@ namespace Ashkin_Teller2d_Parameters
 """
 
 
-def tag(model: str, L: int, bw: float, K: float = 0.5, fields: bool = True) -> str:
+def tag(model: str, L: int, bw: float, K: float = 0.5, fields: bool = True, corr: bool = False) -> str:
+    c = "_corr" if corr else ""
     if model == "ising":
-        return f"ising_L{L}_bw{bw:g}"
-    return f"at_L{L}_K{K:g}_bw{bw:g}_{'rf' if fields else 'clean'}"
+        return f"ising_L{L}_bw{bw:g}{c}"
+    return f"at_L{L}_K{K:g}_bw{bw:g}_{'rf' if fields else 'clean'}{c}"
 
 
-def build(model: str, L: int, bw: float, K: float = 0.5, fields: bool = True, force: bool = False) -> Path:
-    """Build (or reuse) oracle/_ref/<tag>.so and return its path."""
+def build(model: str, L: int, bw: float, K: float = 0.5, fields: bool = True, force: bool = False,
+          corr: bool = False) -> Path:
+    """Build (or reuse) oracle/_ref/<tag>.so and return its path.  corr: the reference's
+    CORRELATION_LENGTHS build (its CMake default), whose observables carry G(q_min) columns."""
     if not reference_available():
         raise FileNotFoundError(f"reference sources not found under {REF}")
-    t = tag(model, L, bw, K, fields)
+    t = tag(model, L, bw, K, fields, corr)
     so = OUT / f"libref_{t}.so"
     if so.exists() and not force:
         return so
@@ -131,6 +134,8 @@ def build(model: str, L: int, bw: float, K: float = 0.5, fields: bool = True, fo
         defs = ["-DASHKIN_TELLER2D", "-DGAUSSIAN_DISORDER"] + (["-DRFAT_BAXTER"] if fields else [])
     src = REF / "src"
     incs = [stub, src / "REWL", src / "util", src / "Hamiltonians", src / "Thermodynamics"]
+    if corr:
+        defs.append("-DCORRELATION_LENGTHS=1")
     cmd = (["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-DREDUCE_LOGDOS", "-DEQUAL_WINDOWS"]
            + defs + ["-include", str(params)] + [f"-I{p}" for p in incs]
            + [str(HERE / "ref_harness.cpp"), "-o", str(so)])

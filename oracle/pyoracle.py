@@ -252,7 +252,8 @@ class Oracle:
         return c, g, v
 
     def obs(self, slot: int) -> np.ndarray:
-        k = 4 if self.cfg.model == MODEL_ISING else 13
+        corr = self.cfg.observables == 2
+        k = (5 if corr else 4) if self.cfg.model == MODEL_ISING else (17 if corr else 13)
         out = np.zeros(self.nbins(slot) * k)
         lib().orc_walker_obs(self.h, slot, _p(out))
         return out.reshape(-1, k)

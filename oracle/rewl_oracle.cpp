@@ -170,11 +170,53 @@ static inline void neighbours(size_t site, size_t L, size_t nb[4])
 // ----------------------------------------------------------------------------
 enum { MODEL_ISING = 0, MODEL_AT = 1 };
 
+// Transform_Kernel (src/Hamiltonians/Correlations/fourier_correlator.hpp:14-42):
+// cos and sin of q_min * x, q_min = 2 pi / L, for x = 0 .. L-1.
+struct QTable
+{
+    std::vector<double> re, im;
+    void build(size_t L)
+    {
+        const double qmin = 2. * std::acos(-1.) / static_cast<double>(L);
+        re.resize(L); im.resize(L);
+        for (size_t i = 0; i != L; ++i) { re[i] = std::cos(qmin * static_cast<double>(i)); im[i] = std::sin(qmin * static_cast<double>(i)); }
+    }
+};
+
+// Fourier_Correlator::compute_correlator (fourier_correlator.hpp:65-118) in the
+// reference's summation order: f(row, col) = field[(row L + col) nt + t1], times
+// field[... + t2] when mixed.  The x part transforms the row sums against the row
+// index, the y part every site against its column index; the result is half the
+// sum of the two squared magnitudes.
+static double fourier_correlator(const QTable& q, size_t L, const double* field, size_t t1, size_t t2, size_t nt, bool mixed)
+{
+    double rx = 0., ix = 0., ry = 0., iy = 0.;
+    for (size_t row = 0; row != L; ++row)
+    {
+        double rowsum = 0.;
+        for (size_t col = 0; col != L; ++col)
+        {
+            double v = field[(row * L + col) * nt + t1];
+            v *= (!mixed) + mixed * field[(row * L + col) * nt + t2];
+            rowsum += v;
+            ry += v * q.re[col];
+            iy += v * q.im[col];
+        }
+        rx += rowsum * q.re[row];
+        ix += rowsum * q.im[row];
+    }
+    rx = rx * rx + ix * ix;
+    ry = ry * ry + iy * iy;
+    return 0.5 * (rx + ry);
+}
+
 struct IsingState { double energy = 0, magnetization = 0, dof = 0; };
 
 struct Ising
 {
     static constexpr int num_obs = 4;                  // |m|, m^2, m^4, counts
+    static constexpr int num_obs_corr = 5;             // |m|, m^2, m^4, G(q_min), counts
+    static int corr_col(int k) { return k; }
     size_t L = 0, N = 0; double J = 1.0;
     std::vector<double> spin, field;                   // field empty => h = 0
     IsingState st;
@@ -213,6 +255,12 @@ struct Ising
         const double m = (1.0 / (double)N) * std::fabs(st.magnetization);
         upd(0, m); upd(1, m * m); upd(2, m * m * m * m);
     }
+    // Ising2d::update_observables, CORRELATION_LENGTHS (ising2d_hamiltonian.hpp:246-252)
+    template <class F> void correlators(const QTable& q, F&& upd) const
+    {
+        const double dn = 1.0 / (double)N;
+        upd(3, dn * dn * fourier_correlator(q, L, spin.data(), 0, 0, 1, false));
+    }
 };
 
 struct ATState { int which = 0; double energy = 0, sm = 0, tm = 0, bax = 0; double dof[2] = {1., 1.}; };
@@ -220,6 +268,8 @@ struct ATState { int which = 0; double energy = 0, sm = 0, tm = 0, bax = 0; doub
 struct AshkinTeller
 {
     static constexpr int num_obs = 13;                 // 12 moments + counts
+    static constexpr int num_obs_corr = 17;            // 4 x (3 moments, G(q_min)) + counts
+    static int corr_col(int k) { return k + k / 3; }
     size_t L = 0, N = 0; double J = 1.0, K = 0.5;
     std::vector<double> spin;                          // interleaved [sigma, tau] per site
     std::vector<double> field;                         // Baxter field per site (may be empty)
@@ -280,6 +330,17 @@ struct AshkinTeller
         upd(3, t); upd(4, t * t); upd(5, t * t * t * t);
         upd(6, std::sqrt(p2)); upd(7, p2); upd(8, p2 * p2);
         upd(9, b); upd(10, b * b); upd(11, b * b * b * b);
+    }
+    // Ashkin_Teller2d::update_observables, CORRELATION_LENGTHS (ashkin_teller2d_hamiltonian.hpp:295-315):
+    // the tau correlator is computed from sigma as in the reference (:298-299), phi's is their sum,
+    // the Baxter one from sigma * tau.
+    template <class F> void correlators(const QTable& q, F&& upd) const
+    {
+        const double dn = 1.0 / (double)N;
+        const double gs = dn * dn * fourier_correlator(q, L, spin.data(), 0, 1, 2, false);
+        const double gt = dn * dn * fourier_correlator(q, L, spin.data(), 0, 1, 2, false);
+        const double gb = dn * dn * fourier_correlator(q, L, spin.data(), 0, 1, 2, true);
+        upd(3, gs); upd(7, gt); upd(11, gs + gt); upd(15, gb);
     }
 };
 
@@ -400,6 +461,8 @@ template <class M> struct Sim
     uint64_t exch_round = 0;
     uint64_t total_sweeps = 0;
     uint64_t exch_accepted = 0, exch_attempted = 0;
+    int nobs = M::num_obs;              // observable columns per bin (with correlators: M::num_obs_corr)
+    QTable q;                           // correlator kernel (observables == 2)
 
     int64_t gbin(double e) const { return bn.gbin(e); }
     bool in_range(const Walker<M>& w, double e) const
@@ -481,6 +544,8 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
     auto* S = new Sim<M>();
     S->c = c;
     S->bn = make_binning(c);
+    S->nobs = c.observables == 2 ? M::num_obs_corr : M::num_obs;
+    if (c.observables == 2) S->q.build((size_t)c.L);
     S->wins = make_windows(c, S->bn);
     const int W = c.nwin, R = c.R;
     S->wk.resize((size_t)W * R);
@@ -502,7 +567,7 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
             // spare capacity keeps neighbouring walkers' hot entries on separate cache lines
             k.count.reserve(k.nb + 32); k.visits.reserve(k.nb + 32); k.logdos.reserve(k.nb + 32);
             k.count.assign(k.nb, 0); k.visits.assign(k.nb, 0); k.logdos.assign(k.nb, 0.0);
-            k.obs.assign(k.nb * M::num_obs, 0.0);
+            k.obs.assign(k.nb * S->nobs, 0.0);
             k.lnf = c.lnf0;
             k.lnf_u = std::max<int64_t>(1, (int64_t)std::llround(c.lnf0 * QSCALE));
             init_model<M>(*S, k.sys, fields);
@@ -552,6 +617,27 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
 }
 
 // ---------------------------- the Wang-Landau update -------------------------
+// update_observables at bin b: the running means (v + c avg) / (c + 1) of the model's
+// moments over the bin's count c (ising2d_observables.hpp:134-145); with correlators
+// (observables == 2, the reference's default CORRELATION_LENGTHS build) the G(q_min)
+// columns are updated by update_qmin_correlator (ising2d_observables.hpp:148-159) with
+// the number of earlier transforms whenever c is a multiple of counts_per_transform
+// = 1000 (fourier_correlator.hpp:11; ising2d_hamiltonian.hpp:246-252); then c += 1.
+template <class M> static void observe(const Sim<M>& S, Walker<M>& w, size_t b)
+{
+    const int n = S.nobs;
+    const bool corr = S.c.observables == 2;
+    double* o = &w.obs[b * n];
+    const double c = o[n - 1];
+    w.sys.observables([&](int k, double v) { double& x = o[corr ? M::corr_col(k) : k]; x = (v + c * x) / (c + 1); });
+    if (corr && static_cast<size_t>(c) % 1000 == 0)
+    {
+        const size_t t = static_cast<size_t>(c / static_cast<double>(1000));
+        w.sys.correlators(S.q, [&](int col, double v) { o[col] = (v + t * o[col]) / (t + 1); });
+    }
+    o[n - 1] += 1;
+}
+
 template <class M, int SEM> static inline void wl_update(Sim<M>& S, Walker<M>& w, size_t idx, uint64_t attempt)
 {
     typename std::conditional<std::is_same<M, Ising>::value, IsingState, ATState>::type t;
@@ -577,13 +663,7 @@ template <class M, int SEM> static inline void wl_update(Sim<M>& S, Walker<M>& w
     w.count[cur] += 1;
     w.visits[cur] += 1;
     w.logdos[cur] += (SEM == SEM_REFERENCE) ? w.lnf : (double)w.lnf_u / QSCALE;
-    if (S.c.observables)
-    {
-        double* o = &w.obs[cur * M::num_obs];
-        const double c = o[M::num_obs - 1];
-        w.sys.observables([&](int k, double v) { o[k] = (v + c * o[k]) / (c + 1); });
-        o[M::num_obs - 1] += 1;
-    }
+    if (S.c.observables) observe(S, w, cur);
 }
 
 template <class M> static void walk(Sim<M>& S, Walker<M>& w, uint64_t nsweeps)
@@ -609,13 +689,7 @@ template <class M> static void touch(Sim<M>& S, Walker<M>& w)
     const size_t b = S.lbin(w, w.sys.st.energy);
     w.count[b] += 1; w.visits[b] += 1;
     w.logdos[b] += (S.c.semantics == SEM_REFERENCE) ? w.lnf : (double)w.lnf_u / QSCALE;
-    if (S.c.observables)
-    {
-        double* o = &w.obs[b * M::num_obs];
-        const double c = o[M::num_obs - 1];
-        w.sys.observables([&](int k, double v) { o[k] = (v + c * o[k]) / (c + 1); });
-        o[M::num_obs - 1] += 1;
-    }
+    if (S.c.observables) observe(S, w, b);
 }
 
 template <class M> static void swap_configs(Walker<M>& a, Walker<M>& b);

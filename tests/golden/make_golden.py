@@ -11,6 +11,9 @@ Groups
               ln f = 1/2.  Records lattices, states, histograms, logDoS and
               per-bin observables (src/REWL/wang_landau.hpp:51-120,
               src/REWL/rewl_walker.hpp:79-158).
+  replay_corr -- the same on a subset of the cases with the reference's
+              CORRELATION_LENGTHS build (its CMake default): the observables carry
+              G(q_min) columns (src/Hamiltonians/Correlations/fourier_correlator.hpp).
   glazier  -- glazier::construct_windows windows (src/REWL/glazier.hpp:305-351).
   rng      -- the first uniforms of random_number_generator<double>
               (src/util/random_number_generators.hpp:14-31) for a few seeds.
@@ -64,11 +67,11 @@ def _stage(ref, orc):
                 draws=np.array(orc.draws(0), dtype=np.uint64))
 
 
-def _replay_case(model, name, L, K, wmin, wmax, bw, nb, seed, k1, k2, fields=None):
+def _replay_case(model, name, L, K, wmin, wmax, bw, nb, seed, k1, k2, fields=None, corr=False):
     if model == "ising":
-        so = build_ref.build("ising", L, bw)
+        so = build_ref.build("ising", L, bw, corr=corr)
     else:
-        so = build_ref.build("at", L, bw, K=K, fields=fields is not None)
+        so = build_ref.build("at", L, bw, K=K, fields=fields is not None, corr=corr)
     ref = pyoracle.RefWalker(so, wmin, wmax, bw, nb, seed)
     rng = np.random.default_rng(seed)
     if fields is not None:
@@ -80,7 +83,7 @@ def _replay_case(model, name, L, K, wmin, wmax, bw, nb, seed, k1, k2, fields=Non
     # the port follows along so that the number of uniforms consumed is known
     cfg = pyoracle.Config(model=pyoracle.MODEL_ISING if model == "ising" else pyoracle.MODEL_AT, L=L, K=K,
                           escale_bits=0 if model == "ising" else 20, nwin=1, R=1, emin=wmin, emax=wmax, bw=bw,
-                          semantics=pyoracle.SEM_REFERENCE, observables=1)
+                          semantics=pyoracle.SEM_REFERENCE, observables=2 if corr else 1)
     orc = pyoracle.Oracle(cfg, fields=fields, init_dofs=dofs0)
     orc.set_dofs(0, dofs0, int(st0[4]) if model != "ising" else 0)
     orc.set_rng(0, seed, 1)
@@ -106,21 +109,50 @@ def _replay_case(model, name, L, K, wmin, wmax, bw, nb, seed, k1, k2, fields=Non
         data[f"{k}1"] = v
     for k, v in s2.items():
         data[f"{k}2"] = v
-    np.savez_compressed(OUT / f"replay_{name}.npz", **data)
+    if corr:
+        # the port's correlators follow the reference's summation order: equal bit for bit
+        o2 = orc.obs(0)
+        assert np.array_equal(o2, s2["obs"]), (name, np.abs(o2 - s2["obs"]).max())
+    np.savez_compressed(OUT / (f"replay_corr_{name}.npz" if corr else f"replay_{name}.npz"), **data)
     print("wrote", name, "state", s2["state"], "draws", s1["draws"], s2["draws"])
 
 
-def gen_replay():
+def gen_replay(corr=False, only=None):
     for name, L, wmin, wmax, bw, seed, k1, k2 in ISING_CASES:
+        if only and name not in only:
+            continue
         nb = int(round((wmax - wmin) / bw))
-        _replay_case("ising", name, L, 0.0, wmin, wmax, bw, nb, seed, k1, k2)
+        _replay_case("ising", name, L, 0.0, wmin, wmax, bw, nb, seed, k1, k2, corr=corr)
     for name, L, K, sig, wlo, nb, seed, k1, k2 in AT_CASES:
+        if only and name not in only:
+            continue
         N = L * L
         emin = -(2.0 + K) * 2 * N
         wmin, wmax = emin + wlo / 20.0, emin + (wlo + nb) / 20.0
         rng = np.random.default_rng(seed + 1000)
         fields = quantised_fields(rng, N, sig) if sig > 0 else None
-        _replay_case("at", name, L, K, wmin, wmax, 0.05, nb, seed, k1, k2, fields=fields)
+        _replay_case("at", name, L, K, wmin, wmax, 0.05, nb, seed, k1, k2, fields=fields, corr=corr)
+
+
+# the reference's CORRELATION_LENGTHS build (its CMake default): observables with G(q_min) columns
+CORR_CASES = ("ising_L4_full", "ising_L8_low", "ising_L16_c1w1", "at_L4_rf", "at_L8_rf")
+
+
+# long runs so that bins see several transforms (counts past 1000, 2000, ...)
+CORR_LONG_ISING = [("ising_L4_long", 4, -32, 36, 4, 101, 2000, 2000)]
+CORR_LONG_AT = [("at_L4_rf_long", 4, 0.5, 0.5, 400, 900, 5, 1500, 1500)]
+
+
+def gen_replay_corr():
+    gen_replay(corr=True, only=CORR_CASES)
+    for name, L, wmin, wmax, bw, seed, k1, k2 in CORR_LONG_ISING:
+        _replay_case("ising", name, L, 0.0, wmin, wmax, bw, int(round((wmax - wmin) / bw)), seed, k1, k2, corr=True)
+    for name, L, K, sig, wlo, nb, seed, k1, k2 in CORR_LONG_AT:
+        N = L * L
+        emin = -(2.0 + K) * 2 * N
+        wmin, wmax = emin + wlo / 20.0, emin + (wlo + nb) / 20.0
+        fields = quantised_fields(np.random.default_rng(seed + 1000), N, sig)
+        _replay_case("at", name, L, K, wmin, wmax, 0.05, nb, seed, k1, k2, fields=fields, corr=True)
 
 
 def gen_glazier():
@@ -253,6 +285,6 @@ def gen_writers():
 
 
 if __name__ == "__main__":
-    groups = sys.argv[1:] or ["replay", "glazier", "rng", "normalize", "exact", "thermo", "writers"]
+    groups = sys.argv[1:] or ["replay", "replay_corr", "glazier", "rng", "normalize", "exact", "thermo", "writers"]
     for g in groups:
         globals()[f"gen_{g}"]()

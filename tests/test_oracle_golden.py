@@ -16,12 +16,12 @@ from conftest import GOLDEN
 REPLAY = sorted(p.name for p in GOLDEN.glob("replay_*.npz"))
 
 
-def _oracle_for(po, z):
+def _oracle_for(po, z, observables=1):
     model = int(z["model"])
     L = int(z["L"])
     cfg = po.Config(model=model, L=L, K=float(z["K"]), escale_bits=0 if model == 0 else 20, nwin=1, R=1,
                     emin=float(z["wmin"]), emax=float(z["wmax"]), bw=float(z["bw"]),
-                    semantics=po.SEM_REFERENCE, observables=1)
+                    semantics=po.SEM_REFERENCE, observables=observables)
     fields = z["fields"] if z["fields"].size else None
     dofs0 = z["dofs0"].astype(np.float64)
     orc = po.Oracle(cfg, fields=fields, init_dofs=dofs0)
@@ -39,9 +39,11 @@ def _engine_layout(dofs_ref: np.ndarray, model: int) -> np.ndarray:
 
 @pytest.mark.parametrize("name", REPLAY)
 def test_replay_bit_exact(oracle_lib, name):
+    """replay_corr_* fixtures come from the reference's CORRELATION_LENGTHS build: their
+    observables carry the G(q_min) columns, reproduced in the reference's summation order."""
     po = oracle_lib
     z = np.load(GOLDEN / name)
-    orc = _oracle_for(po, z)
+    orc = _oracle_for(po, z, observables=2 if name.startswith("replay_corr_") else 1)
     np.testing.assert_array_equal(orc.state(0), z["state0"])
     for stage in (1, 2):
         if stage == 2:
