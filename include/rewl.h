@@ -89,7 +89,10 @@ typedef struct rewl_batch_desc {
     int32_t warps_per_block;      /* 0: automatic; else 1, 2, 4 or 8 */
     int32_t walkers_per_warp;     /* 0: automatic; else 1, 2 or 4 (Ising bin-tracking kernel) */
     int32_t observables;          /* 1: keep per-bin observables (update_observables after every
-                                     attempted flip and exchange, rewl_walker.hpp / wang_landau.hpp:51-120) */
+                                     attempted flip and exchange, rewl_walker.hpp / wang_landau.hpp:51-120);
+                                     2: also the G(q_min) Fourier correlators of the reference's default
+                                     CORRELATION_LENGTHS build (src/Hamiltonians/Correlations/
+                                     fourier_correlator.hpp), one transform at every 1000th count of a bin */
     const rewl_instance_desc* instances;
 } rewl_batch_desc;
 
@@ -186,11 +189,15 @@ int rewl_get_status(rewl_engine* eng, rewl_status* status);
  *  src/REWL/rewl_histograms.hpp:98-104) */
 int rewl_export_walker(rewl_engine* eng, int32_t walker, int8_t* dofs, double* state,
                        uint64_t* counts, double* logdos, uint64_t* visits);
-/* Per-bin observable averages of one walker (observables = 1), nb rows of K + 1 doubles: K
+/* Per-bin observable averages of one walker (observables = 1 or 2), nb rows of K + 1 doubles: K
  * averages and the number of updates, the layout of the reference's obs_array
  * (Ising2d_Obs, src/Hamiltonians/Ising2d/ising2d_observables.hpp:134-145: K = 3, |m| m^2 m^4;
  * Ashkin_Teller2d_Obs, src/Hamiltonians/Ashkin_Teller2d/ashkin_teller2d_observables.hpp:211-222:
- * K = 12, |s| s^2 s^4 |t| t^2 t^4 |p| p^2 p^4 |b| b^2 b^4 with p^2 = s^2 + t^2). */
+ * K = 12, |s| s^2 s^4 |t| t^2 t^4 |p| p^2 p^4 |b| b^2 b^4 with p^2 = s^2 + t^2).  With
+ * observables = 2 the CORRELATION_LENGTHS layout (ising2d_observables.hpp:22-28,
+ * ashkin_teller2d_observables.hpp:36-47): Ising K = 4 with G(q_min) after m^4; Ashkin-Teller
+ * K = 16 with a G(q_min) after each group of three (sigma, tau computed from sigma as the
+ * reference does, phi = their sum, Baxter); G is the mean over the bin's transforms. */
 int rewl_export_observables(rewl_engine* eng, int32_t walker, double* out);
 /* The same over a window's replicas, weighted by their counts (the final averaging of
  * observables, src/Simulation/rewl_simulation.hpp:361-454). */
@@ -291,9 +298,13 @@ int rewl_thermodynamics(const double* E, const double* lng, const double* obs, i
                         int32_t trapezoid, int32_t device, double* temperatures, double* out);
 /* Susceptibility N (<m^2> - <m>^2) / T and Binder cumulants from those rows
  * (order_parameter_cumulants.hpp:17-48).  Ising: 2 values per T (susceptibility, cumulant);
- * Ashkin-Teller: 8 (sigma, tau, Baxter, then phi with the two-component cumulant). */
-int rewl_nonlinear_observables(int32_t model, const double* rows, int32_t num_T, int32_t row_len,
-                               const double* temperatures, double system_size, double* out);
+ * Ashkin-Teller: 8 (sigma, tau, Baxter, then phi with the two-component cumulant).  With
+ * correlators (rows in the observables = 2 layout) each pair is followed by the correlation
+ * length over L, (L / 2 pi) sqrt((<m^2> - <G>) / <G>) / L (order_parameter_cumulants.hpp:52-59;
+ * calculate_nonlinear_observables, ising2d_observables.hpp:166-193,
+ * ashkin_teller2d_observables.hpp:240-300): Ising 3 values per T, Ashkin-Teller 12. */
+int rewl_nonlinear_observables(int32_t model, int32_t correlators, const double* rows, int32_t num_T,
+                               int32_t row_len, const double* temperatures, double system_size, double* out);
 
 /* ------------------------------------------------------------------------
  * Output files in the reference's text formats (main.cpp:241-365): '#' header lines

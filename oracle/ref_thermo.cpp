@@ -32,3 +32,21 @@ extern "C" int ref_thermo(int at, size_t nb, const double* E, const double* lng,
     else run<IsingObs>(nb, E, lng, obs, N, Tmin, Tmax, nT, out, temps);
     return 0;
 }
+
+// The reference's nonlinear observables (src/Thermodynamics/order_parameter_cumulants.hpp:17-59)
+// on given thermal averages: susceptibility, Binder cumulant, two-component Binder cumulant and
+// calculate_correlation_length(G0, Gq, L) / L as calculate_nonlinear_observables uses it
+// (src/Hamiltonians/Ising2d/ising2d_observables.hpp:190).
+#include "order_parameter_cumulants.hpp"
+
+extern "C" void ref_cumulants(size_t n, const double* m, const double* m2, const double* m4, const double* G,
+                              const double* T, size_t N, double* out)
+{
+    const size_t L = static_cast<size_t>(std::sqrt(N));
+    for (size_t i = 0; i < n; ++i) {
+        out[4 * i + 0] = calculate_susceptibility<double>(m2[i], m[i], T[i], N);
+        out[4 * i + 1] = calculate_Binder_cumulant(m4[i], m2[i]);
+        out[4 * i + 2] = calculate_two_component_Binder_cumulant(m4[i], m2[i]);
+        out[4 * i + 3] = calculate_correlation_length(m2[i], G[i], L) / L;
+    }
+}

@@ -64,10 +64,36 @@ def binder_two_component(m4, m2):
     return 2.0 * (1.0 - 0.5 * (m4 / (m2 * m2)))
 
 
-def nonlinear(model: int, rows, T, N):
+def correlation_length_over_L(G0, Gq, N):
+    """calculate_correlation_length(G0, Gq, L) / L with L = (size_t) sqrt(N)
+    (order_parameter_cumulants.hpp:52-59, ising2d_observables.hpp:180-190)."""
+    L = float(int(np.sqrt(N)))
+    G0, Gq = np.asarray(G0, dtype=np.float64), np.asarray(Gq, dtype=np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        x = (L / (2.0 * np.arccos(-1.0))) * np.sqrt((G0 - Gq) / Gq)
+    x = np.where(Gq == 0.0, np.finfo(np.float64).max, x)
+    return x / L
+
+
+def nonlinear(model: int, rows, T, N, correlators: bool = False):
     """Ising: [susceptibility, Binder cumulant]; Ashkin-Teller: sigma, tau, Baxter
-    (susceptibility, Binder cumulant) then phi (susceptibility, two-component cumulant)."""
+    (susceptibility, Binder cumulant) then phi (susceptibility, two-component cumulant).
+    With correlators (CORRELATION_LENGTHS layout: G(q_min) after each group of three moments)
+    each pair is followed by the correlation length over L."""
     o = rows[:, 5:]
+    if correlators:
+        if model == 0:
+            return np.stack([susceptibility(o[:, 1], o[:, 0], T, N), binder(o[:, 2], o[:, 1]),
+                             correlation_length_over_L(o[:, 1], o[:, 3], N)], axis=1)
+        cols = []
+        for base in (0, 4, 12):     # sigma, tau, Baxter
+            g = o[:, base:base + 4]
+            cols += [susceptibility(g[:, 1], g[:, 0], T, N), binder(g[:, 2], g[:, 1]),
+                     correlation_length_over_L(g[:, 1], g[:, 3], N)]
+        g = o[:, 8:12]              # phi
+        cols += [susceptibility(g[:, 1], g[:, 0], T, N), binder_two_component(g[:, 2], g[:, 1]),
+                 correlation_length_over_L(g[:, 1], g[:, 3], N)]
+        return np.stack(cols, axis=1)
     if model == 0:
         return np.stack([susceptibility(o[:, 1], o[:, 0], T, N), binder(o[:, 2], o[:, 1])], axis=1)
     cols = []

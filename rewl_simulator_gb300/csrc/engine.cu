@@ -88,6 +88,7 @@ struct InstDev {
     int64_t eglo_u;          // global range start in energy units
     int64_t bin_mul;         // global bin = ((E - eglo_u) * bin_mul) >> bin_shift
     int64_t field_off;       // offset into fields (int64 units per site) or -1
+    int64_t qtab_off;        // offset into qtab (cos then sin of q_min x, x < L) or -1 without correlators
     uint64_t seed;
 };
 
@@ -131,7 +132,9 @@ struct DevPtrs {
     int32_t* counters;       // [0] error word, [1] flat events (this call)
     unsigned long long* stats;  // [0] exch attempted, [1] exch accepted
     double* obs;             // per-bin observable sums (obs_stride per bin), or null when off
-    int obs_stride;          // 3 (Ising) or 12 (a batch with Ashkin-Teller instances)
+    int obs_stride;          // 3 (Ising) or 12 (a batch with Ashkin-Teller instances); 4 or 16 with correlators
+    int corr;                // observables carry the G(q_min) correlators
+    const double* qtab;      // per instance: cos(q_min x) then sin(q_min x), x < L
 };
 
 // --------------------------------------------------------------------------
@@ -311,14 +314,86 @@ __device__ inline void obs_add_ising(double* o, int M, double invN)
     atomicAdd(o + 2, m * m * m * m);
 }
 
-__device__ inline void obs_add_at(double* o, int sm, int tm, int bx, double invN)
+// With correlators each Ashkin-Teller group of three moments is followed by its
+// G(q_min) column (sigma, tau, phi, Baxter: ashkin_teller2d_observables.hpp:36-41).
+__device__ inline void obs_add_at(double* o, int sm, int tm, int bx, double invN, int corr)
 {
     const double a = invN * fabs((double)sm), t = invN * fabs((double)tm), b = invN * fabs((double)bx);
     const double p2 = a * a + t * t;
+    const int g = corr ? 1 : 0;
     atomicAdd(o + 0, a); atomicAdd(o + 1, a * a); atomicAdd(o + 2, a * a * a * a);
+    o += g;
     atomicAdd(o + 3, t); atomicAdd(o + 4, t * t); atomicAdd(o + 5, t * t * t * t);
+    o += g;
     atomicAdd(o + 6, sqrt(p2)); atomicAdd(o + 7, p2); atomicAdd(o + 8, p2 * p2);
+    o += g;
     atomicAdd(o + 9, b); atomicAdd(o + 10, b * b); atomicAdd(o + 11, b * b * b * b);
+}
+
+// G(q_min) correlators (CORRELATION_LENGTHS, on in the reference's default build).  At
+// every visit of a bin whose count before the visit is a multiple of counts_per_transform
+// = 1000 (src/Hamiltonians/Correlations/fourier_correlator.hpp:11), the walker's G is added
+// at the bin (Ising2d::update_observables, ising2d_hamiltonian.hpp:246-252;
+// Ashkin_Teller2d::update_observables, ashkin_teller2d_hamiltonian.hpp:295-315).  The
+// reference keeps the running mean over those transforms (ising2d_observables.hpp:148-159);
+// the export divides the sum by their number, ceil(visits / 1000).
+constexpr unsigned long long kCountsPerTransform = 1000;
+
+// Fourier_Correlator::compute_correlator (fourier_correlator.hpp:65-118) of one plane of
+// +-1 values v(y, x): half the squared magnitude of the transform of the row sums over y
+// plus that of the column sums over x, both at q_min = 2 pi / L (q: L cosines then L sines).
+// rs and cs are the plane's row and column sums before the chunk; the chunk (row y,
+// columns x0 ..) has flipped the sites of its steps 0..j whose acceptance bit is set: row
+// y changes by dr and column x0 + k by -2 val(k), val(k) the site's value before the
+// chunk.  The reference adds the same products site by site in row-major order; the two
+// agree to FP64 rounding.
+template <class V>
+__device__ double plane_corr(const int* rs, const int* cs, const double* q, int L, int y, int dr, int x0, int j,
+                             unsigned acc, V val)
+{
+    double rx = 0.0, ix = 0.0, ry = 0.0, iy = 0.0;
+    for (int t = 0; t < L; ++t) {
+        const double c = q[t], sn = q[L + t];
+        const double r = (double)(rs[t] + (t == y ? dr : 0));
+        const int k = t - x0;
+        const int cl = cs[t] - ((k >= 0 && k <= j && ((acc >> k) & 1u)) ? 2 * val(k) : 0);
+        rx += r * c;
+        ix += r * sn;
+        ry += (double)cl * c;
+        iy += (double)cl * sn;
+    }
+    return 0.5 * ((rx * rx + ix * ix) + (ry * ry + iy * iy));
+}
+
+// The same from a whole configuration, in the reference's order (one thread): plane a,
+// or the product plane a * b.
+__device__ double full_corr(const int8_t* a, const int8_t* b, const double* q, int L)
+{
+    double rx = 0.0, ix = 0.0, ry = 0.0, iy = 0.0;
+    for (int y = 0; y < L; ++y) {
+        int rsum = 0;
+        for (int x = 0; x < L; ++x) {
+            const int v = b ? a[y * L + x] * b[y * L + x] : a[y * L + x];
+            rsum += v;
+            ry += (double)v * q[x];
+            iy += (double)v * q[L + x];
+        }
+        rx += (double)rsum * q[y];
+        ix += (double)rsum * q[L + y];
+    }
+    return 0.5 * ((rx * rx + ix * ix) + (ry * ry + iy * iy));
+}
+
+// Row and column sums of a plane (value(i) for site i) into rs, cs, by the warp's lanes.
+template <class V>
+__device__ void plane_sums(int* rs, int* cs, int L, int lane, V value)
+{
+    for (int t = lane; t < L; t += 32) {
+        int r = 0, c = 0;
+        for (int u = 0; u < L; ++u) { r += value(t * L + u); c += value(u * L + t); }
+        rs[t] = r;
+        cs[t] = c;
+    }
 }
 
 // flips of a chunk's steps 0..j that turned a +1 into -1 minus those that turned -1 into +1
@@ -423,6 +498,8 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
     long long* gs = reinterpret_cast<long long*>(base);
     Stage* st = reinterpret_cast<Stage*>(gs + p.nbcap);
     int8_t* lat = reinterpret_cast<int8_t*>(st + 1);
+    int* rsum = reinterpret_cast<int*>(lat + ((N + 15) & ~15));   // correlators: row and column sums
+    int* csum = rsum + L;
 
     const int cfg = P.slot_cfg[s];
     int8_t* gl = P.spins + P.cfg_off[cfg];
@@ -430,6 +507,11 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
     long long* gg = reinterpret_cast<long long*>(P.g + P.slot_tab[s]);
     for (int k = lane; k < nb; k += 32) gs[k] = gg[k];
     __syncwarp();
+    const bool corr = P.obs != nullptr && P.corr;
+    if (corr) {
+        plane_sums(rsum, csum, L, lane, [&](int i) { return (int)lat[i]; });
+        __syncwarp();
+    }
 
     const int J = (int)I.J_u;
     const int sh = I.bin_shift;
@@ -458,7 +540,7 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
         const uint64_t A0 = (sweeps0 + (uint64_t)sw) * (uint64_t)N;
         for (int c0 = 0; c0 < N; c0 += C) {
             // chunk = sites c0 .. c0+C-1 of one row (C divides L)
-            const int y = c0 / L, x = c0 - y * L + lane;
+            const int y = c0 / L, x0 = c0 - y * L, x = x0 + lane;
             const int row = y * L;
             const int up = (y == 0 ? L - 1 : y - 1) * L, down = (y == L - 1 ? 0 : y + 1) * L;
             int si = 0, d0 = 0, d1 = 0, wc = 0;
@@ -543,6 +625,27 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
                 if (lane < C)
                     obs_add_ising(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
                                   M + chunk_dm(acc, plus, lane), invN);
+                if (corr) {
+                    const int bin = lane < C ? st->seq[lane] : -1 - lane;
+                    const unsigned grp = __match_any_sync(kFull, bin);
+                    if (lane < C) {
+                        // the bin's count before step `lane`: its visits after the chunk (the
+                        // launch's start value plus the change of g over ln f) minus the chunk's
+                        // visits to it from step `lane` on
+                        const unsigned long long after =
+                            P.visits[P.slot_tab[s] + bin] + (unsigned long long)((gs[bin] - gg[bin]) / lnf);
+                        const unsigned long long seen = after - (unsigned long long)__popc(grp >> lane);
+                        if (seen % kCountsPerTransform == 0) {
+                            const double G = plane_corr(rsum, csum, P.qtab + I.qtab_off, L, y, chunk_dm(acc, plus, lane),
+                                                        x0, lane, acc, [&](int k) { return (int)lat[row + x0 + k]; });
+                            atomicAdd(P.obs + (size_t)(P.slot_tab[s] + bin) * P.obs_stride + 3, invN * invN * G);
+                        }
+                    }
+                    __syncwarp();
+                    // the chunk's flips into the row and column sums
+                    if (lane < C && ((acc >> lane) & 1u)) csum[x] -= 2 * si;
+                    if (lane == 0) rsum[y] += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus));
+                }
             }
             if (lane < C && ((acc >> lane) & 1u)) lat[row + x] = (int8_t)(-si);
             M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus));
@@ -1047,6 +1150,18 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
     long long* g0 = reinterpret_cast<long long*>(P.gsnap + P.slot_tab[s]);
     for (int k = lane; k < nb; k += 32) g0[k] = gg[k];
     __syncwarp();
+    // correlators: row and column sums of the sigma plane and of the Baxter plane sigma * tau
+    int* rs_s = reinterpret_cast<int*>(sig + ((2 * N + 15) & ~15));
+    int* cs_s = rs_s + L;
+    int* rs_b = cs_s + L;
+    int* cs_b = rs_b + L;
+    const bool corr = OBS && P.corr;
+    const double invN = 1.0 / (double)N;
+    if (corr) {
+        plane_sums(rs_s, cs_s, L, lane, [&](int i) { return (int)sig[i]; });
+        plane_sums(rs_b, cs_b, L, lane, [&](int i) { return (int)sig[i] * (int)tau[i]; });
+        __syncwarp();
+    }
 
     const long long J = I.J_u, K = I.K_u;
     const long long lnf = P.win_lnf[w];
@@ -1132,7 +1247,42 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
                         const int da = chunk_dm(acc, aplus, lane), db = chunk_dm(acc, abplus, lane);
                         obs_add_at(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
                                    flavour == 0 ? sm0 + da : sm0, flavour == 0 ? tm0 : tm0 + da, bx0 + db,
-                                   1.0 / (double)N);
+                                   invN, P.corr);
+                    }
+                    if (corr) {
+                        const int y = c0 / L, x0 = c0 - y * L, row = y * L;
+                        const int bin = lane < C ? st->seq[lane] : -1 - lane;
+                        const unsigned grp = __match_any_sync(kFull, bin);
+                        if (lane < C) {
+                            // the bin's count before step `lane` (see the Ising kernel)
+                            const unsigned long long after =
+                                P.visits[P.slot_tab[s] + bin] + (unsigned long long)((gg[bin] - g0[bin]) / lnf);
+                            const unsigned long long seen = after - (unsigned long long)__popc(grp >> lane);
+                            if (seen % kCountsPerTransform == 0) {
+                                const double* q = P.qtab + I.qtab_off;
+                                // sigma changes in the sigma pass only, the Baxter product in both
+                                const double gsig = plane_corr(rs_s, cs_s, q, L, y, flavour == 0 ? chunk_dm(acc, aplus, lane) : 0,
+                                                               x0, lane, flavour == 0 ? acc : 0u,
+                                                               [&](int k) { return (int)sig[row + x0 + k]; });
+                                const double gbax = plane_corr(rs_b, cs_b, q, L, y, chunk_dm(acc, abplus, lane), x0, lane, acc,
+                                                               [&](int k) { return (int)sig[row + x0 + k] * (int)tau[row + x0 + k]; });
+                                const double gs = invN * invN * gsig, gb = invN * invN * gbax;
+                                // the tau correlator is computed from sigma, as the reference does
+                                // (ashkin_teller2d_hamiltonian.hpp:298-299); phi's is the sum of the two
+                                double* o = P.obs + (size_t)(P.slot_tab[s] + bin) * P.obs_stride;
+                                atomicAdd(o + 3, gs); atomicAdd(o + 7, gs); atomicAdd(o + 11, gs + gs); atomicAdd(o + 15, gb);
+                            }
+                        }
+                        __syncwarp();
+                        // the chunk's flips into the sums
+                        if (lane < C && ((acc >> lane) & 1u)) {
+                            if (flavour == 0) cs_s[x0 + lane] -= 2 * ai;
+                            cs_b[x0 + lane] -= 2 * ai * bi;
+                        }
+                        if (lane == 0) {
+                            if (flavour == 0) rs_s[y] += -2 * ((int)__popc(acc & aplus) - (int)__popc(acc & ~aplus));
+                            rs_b[y] += -2 * ((int)__popc(acc & abplus) - (int)__popc(acc & ~abplus));
+                        }
                     }
                 }
                 if (lane < C && ((acc >> lane) & 1u)) A[c0 + lane] = (int8_t)(-ai);
@@ -1189,12 +1339,27 @@ __device__ inline void touch(const DevPtrs& P, const InstDev& I, int slot)
     const int64_t o = P.slot_tab[slot] + b;
     P.g[o] += P.win_lnf[w];
     P.H[o] += 1u;
-    P.visits[o] += 1u;
+    const uint64_t seen = P.visits[o];         // the bin's count before this visit
+    P.visits[o] = seen + 1u;
     if (P.obs) {
         double* ob = P.obs + (size_t)o * P.obs_stride;
         const double invN = 1.0 / (double)I.N;
         if (I.model == REWL_MODEL_ISING2D) obs_add_ising(ob, P.cfg_M[3 * c], invN);
-        else obs_add_at(ob, P.cfg_M[3 * c], P.cfg_M[3 * c + 1], P.cfg_M[3 * c + 2], invN);
+        else obs_add_at(ob, P.cfg_M[3 * c], P.cfg_M[3 * c + 1], P.cfg_M[3 * c + 2], invN, P.corr);
+        if (P.corr && seen % kCountsPerTransform == 0) {
+            const double* q = P.qtab + I.qtab_off;
+            const int8_t* sp = P.spins + P.cfg_off[c];
+            const double in2 = invN * invN;
+            if (I.model == REWL_MODEL_ISING2D) {
+                atomicAdd(ob + 3, in2 * full_corr(sp, nullptr, q, I.L));
+            } else {
+                // the tau correlator is computed from sigma, as the reference does
+                // (ashkin_teller2d_hamiltonian.hpp:298-299); phi's is the sum of the two
+                const double gs = in2 * full_corr(sp, nullptr, q, I.L);
+                const double gb = in2 * full_corr(sp, sp + I.N, q, I.L);
+                atomicAdd(ob + 3, gs); atomicAdd(ob + 7, gs); atomicAdd(ob + 11, gs + gs); atomicAdd(ob + 15, gb);
+            }
+        }
     }
 }
 
@@ -1497,10 +1662,12 @@ struct rewl_engine {
     DBuf<int64_t> thr;
     DBuf<double> obs;           // per-bin observable sums (observables on)
     DBuf<int64_t> gsnap;        // Ashkin-Teller engines: logDoS copy taken by each sweep launch
+    DBuf<double> qtab;          // correlator kernels (observables == 2)
     int obs_stride = 0;
     std::vector<int64_t> h_thr_off, h_thr_n;
     std::vector<int64_t> h_fields;
     std::vector<uint8_t> h_mask;
+    std::vector<double> h_qtab;
 
     DevPtrs ptrs() const
     {
@@ -1514,6 +1681,7 @@ struct rewl_engine {
         P.win_lnf = win_lnf.p; P.win_done = win_done.p; P.win_oot = win_oot.p; P.win_iter = win_iter.p;
         P.win_sweepctr = win_sweepctr.p; P.pairs = nullptr; P.counters = counters.p; P.stats = stats.p;
         P.obs = obs.p; P.obs_stride = obs_stride;
+        P.corr = desc.observables == 2 ? 1 : 0; P.qtab = qtab.p;
         return P;
     }
 
@@ -1522,7 +1690,7 @@ struct rewl_engine {
         d_inst.free_(); d_win.free_();
         slot_inst.free_(); slot_win.free_(); slot_cfg.free_(); slot_nb.free_(); slot_flavour.free_();
         pairs[0].free_(); pairs[1].free_();
-        obs.free_();
+        obs.free_(); gsnap.free_(); qtab.free_();
         slot_tab.free_(); slot_draws.free_(); slot_thr_off.free_(); slot_thr_n.free_(); cfg_off.free_();
         cfg_E.free_(); fields.free_(); g.free_(); win_lnf.free_(); slot_sweeps.free_(); visits.free_();
         win_iter.free_(); win_sweepctr.free_(); spins.free_(); cfg_M.free_(); win_done.free_(); win_oot.free_();
@@ -1629,13 +1797,15 @@ int build_host(rewl_engine* e)
     if (D.rng_mode != REWL_RNG_PHILOX && D.rng_mode != REWL_RNG_REPLAY) return fail(REWL_EINVAL, "bad rng mode");
     if (D.warps_per_block != 0 && D.warps_per_block != 1 && D.warps_per_block != 2 && D.warps_per_block != 4 && D.warps_per_block != 8)
         return fail(REWL_EINVAL, "warps_per_block must be 0, 1, 2, 4 or 8");
-    if (D.observables != 0 && D.observables != 1) return fail(REWL_EINVAL, "observables must be 0 or 1");
+    if (D.observables < 0 || D.observables > 2)
+        return fail(REWL_EINVAL, "observables must be 0 (off), 1 (moments) or 2 (moments and G(q_min) correlators)");
     if (D.walkers_per_warp != 0 && D.walkers_per_warp != 1 && D.walkers_per_warp != 2 && D.walkers_per_warp != 4)
         return fail(REWL_EINVAL, "walkers_per_warp must be 0, 1, 2 or 4");
     int slot = 0, win = 0;
     int64_t tab = 0, spin = 0, maskoff = 0, fieldoff = 0;
     std::vector<int64_t> h_fields;
     std::vector<uint8_t> h_mask;
+    std::vector<double> h_qtab;
     e->inst.resize(D.num_instances);
     for (int ii = 0; ii < D.num_instances; ++ii) {
         const rewl_instance_desc& d = D.instances[ii];
@@ -1685,6 +1855,14 @@ int build_host(rewl_engine* e)
             }
             fieldoff += I.N;
         } else I.field_off = -1;
+        if (D.observables == 2) {
+            // Transform_Kernel (src/Hamiltonians/Correlations/fourier_correlator.hpp:14-42), from the
+            // host's libm like the reference's own table
+            I.qtab_off = (int64_t)h_qtab.size();
+            const double qmin = 2. * std::acos(-1.) / static_cast<double>(d.L);
+            for (int x = 0; x < d.L; ++x) h_qtab.push_back(std::cos(qmin * static_cast<double>(x)));
+            for (int x = 0; x < d.L; ++x) h_qtab.push_back(std::sin(qmin * static_cast<double>(x)));
+        } else I.qtab_off = -1;
         std::vector<double> mins, maxs; std::vector<int64_t> gblo; std::vector<int> nbins;
         if (make_windows(d, mins, maxs, gblo, nbins))
             return fail(REWL_EINVAL, "instance %d: the energy range is not a whole number of bins", ii);
@@ -1734,6 +1912,7 @@ int build_host(rewl_engine* e)
             for (int lw = dir; lw + 1 < D.instances[ii].num_windows; lw += 2) { e->pairs_dir[dir].push_back(ii); e->pairs_dir[dir].push_back(lw); }
     }
     e->h_fields = std::move(h_fields);
+    e->h_qtab = std::move(h_qtab);
     e->h_mask = std::move(h_mask);
     return REWL_OK;
 }
@@ -1751,6 +1930,7 @@ int upload_all(rewl_engine* e)
         (rc = upload(e->slot_inst, e->h_slot_inst, s)) || (rc = upload(e->slot_win, e->h_slot_win, s)) ||
         (rc = upload(e->slot_nb, e->h_slot_nb, s)) || (rc = upload(e->slot_tab, e->h_slot_tab, s)) ||
         (rc = upload(e->cfg_off, e->h_cfg_off, s)) || (rc = upload(e->fields, e->h_fields, s)) ||
+        (rc = upload(e->qtab, e->h_qtab, s)) ||
         (rc = upload(e->mask, e->h_mask, s)) || (rc = upload(e->pairs[0], e->pairs_dir[0], s)) ||
         (rc = upload(e->pairs[1], e->pairs_dir[1], s)))
         return rc;
@@ -1777,7 +1957,7 @@ int upload_all(rewl_engine* e)
     for (const auto& hi : e->inst) any_at = any_at || hi.d.model == REWL_MODEL_ASHKIN_TELLER2D;
     if (any_at && tab && (rc = e->gsnap.alloc(tab))) return rc;
     if (D.observables && tab) {
-        e->obs_stride = any_at ? 12 : 3;
+        e->obs_stride = any_at ? (D.observables == 2 ? 16 : 12) : (D.observables == 2 ? 4 : 3);
         if ((rc = e->obs.alloc((size_t)tab * e->obs_stride))) return rc;
         CUDA_TRY(cudaMemsetAsync(e->obs.p, 0, (size_t)tab * e->obs_stride * sizeof(double), s));
     }
@@ -1796,6 +1976,7 @@ int upload_all(rewl_engine* e)
 bool bins_eligible(const InstDev& I, const rewl_batch_desc& D)
 {
     if (I.model != REWL_MODEL_ISING2D || D.rng_mode != REWL_RNG_PHILOX) return false;
+    if (D.observables == 2) return false;   // the correlators are kept by the general kernel
     const int C = I.chunk;
     if (!(C == 32 || C == 24 || C == 16 || C == 8 || C == 4)) return false;
     const long long step = 4 * std::llabs(I.J_u);            // every energy change is a multiple of 4|J|
@@ -1835,9 +2016,11 @@ int plan_launches(rewl_engine* e)
         plans[idx].slots.push_back(s);
     }
     for (auto& l : plans) {
-        int maxN = 0, maxnb = 0;
+        int maxN = 0, maxnb = 0, maxL = 0;
+        const bool corr = e->desc.observables == 2;
         for (int s : l.slots) {
             maxN = std::max(maxN, e->inst[e->h_slot_inst[s]].dev.N);
+            maxL = std::max(maxL, e->inst[e->h_slot_inst[s]].dev.L);
             maxnb = std::max(maxnb, e->h_slot_nb[s]);
         }
         const int n = (int)l.slots.size();
@@ -1862,10 +2045,10 @@ int plan_launches(rewl_engine* e)
             l.wpb = wpb;
         } else if (l.model == REWL_MODEL_ISING2D) {
             l.nbcap = (maxnb + 1) & ~1;
-            l.smem_per_warp = (int)(l.nbcap * 8 + sizeof(Stage) + ((maxN + 15) & ~15));
+            l.smem_per_warp = (int)(l.nbcap * 8 + sizeof(Stage) + ((maxN + 15) & ~15) + (corr ? 8 * maxL : 0));
         } else {
             l.nbcap = 0;
-            l.smem_per_warp = (int)(sizeof(StageAT) + ((2 * maxN + 15) & ~15));
+            l.smem_per_warp = (int)(sizeof(StageAT) + ((2 * maxN + 15) & ~15) + (corr ? 16 * maxL : 0));
         }
         if (!l.bins) {
             l.smem_per_warp = (l.smem_per_warp + 15) & ~15;
@@ -2371,12 +2554,23 @@ int rewl_run_cycles(rewl_engine* e, int64_t ncycles, int64_t timeout_ms, rewl_st
 }
 
 namespace {
-// [nb][K + 1] rows of K averages and the update count, from the sums of the given slots
+// Observable columns of a model, before the count column: Ising |m|, m^2, m^4 (+ G(q_min));
+// Ashkin-Teller 12 moments (+ a G(q_min) after each group of three).
+int obs_columns(int model, bool corr) { return model == REWL_MODEL_ISING2D ? (corr ? 4 : 3) : (corr ? 16 : 12); }
+bool is_corr_column(int model, bool corr, int k) { return corr && (model == REWL_MODEL_ISING2D ? k == 3 : (k & 3) == 3); }
+
+// [nb][K + 1] rows of K averages and the update count, from the sums of the given slots.
+// Moments: sum over the slots / total count (the count-weighted mean of the replicas' running
+// means).  G(q_min): each slot's sum over its transforms, ceil(count / 1000) of them, weighted
+// by the slot's count in the same way.
 int export_obs(rewl_engine* e, int ii, const std::vector<int>& slots, double* out)
 {
     if (!e->obs.p) return fail(REWL_ESTATE, "the engine was created without observables (rewl_batch_desc.observables)");
-    const int K = e->inst[ii].d.model == REWL_MODEL_ISING2D ? 3 : 12;
+    const int model = e->inst[ii].d.model;
+    const bool corr = e->desc.observables == 2;
+    const int K = obs_columns(model, corr);
     const int nb = e->h_slot_nb[slots[0]];
+    const bool single = slots.size() == 1;
     std::vector<double> sum((size_t)nb * K, 0.0), part((size_t)nb * e->obs_stride);
     std::vector<uint64_t> cnt(nb, 0), v(nb);
     for (int s : slots) {
@@ -2386,13 +2580,21 @@ int export_obs(rewl_engine* e, int ii, const std::vector<int>& slots, double* ou
         CUDA_TRY(cudaMemcpyAsync(v.data(), e->visits.p + off, nb * 8, cudaMemcpyDeviceToHost, e->stream));
         CUDA_TRY(cudaStreamSynchronize(e->stream));
         for (int b = 0; b < nb; ++b) {
-            for (int k = 0; k < K; ++k) sum[(size_t)b * K + k] += part[(size_t)b * e->obs_stride + k];
+            for (int k = 0; k < K; ++k) {
+                const double x = part[(size_t)b * e->obs_stride + k];
+                if (!is_corr_column(model, corr, k)) { sum[(size_t)b * K + k] += x; continue; }
+                if (!v[b]) continue;
+                const double mean = x / (double)((v[b] + kCountsPerTransform - 1) / kCountsPerTransform);
+                sum[(size_t)b * K + k] += single ? mean : (double)v[b] * mean;
+            }
             cnt[b] += v[b];
         }
     }
     for (int b = 0; b < nb; ++b) {
-        for (int k = 0; k < K; ++k)
-            out[(size_t)b * (K + 1) + k] = cnt[b] ? sum[(size_t)b * K + k] / (double)cnt[b] : 0.0;
+        for (int k = 0; k < K; ++k) {
+            const double x = sum[(size_t)b * K + k];
+            out[(size_t)b * (K + 1) + k] = !cnt[b] ? 0.0 : (single && is_corr_column(model, corr, k)) ? x : x / (double)cnt[b];
+        }
         out[(size_t)b * (K + 1) + K] = (double)cnt[b];
     }
     return REWL_OK;
@@ -2551,7 +2753,7 @@ int rewl_global_observables(rewl_engine* e, int32_t ii, double* obs, int32_t* co
     if (!e || ii < 0 || ii >= (int)e->inst.size() || !count) return fail(REWL_EINVAL, "bad arguments");
     if (!e->obs.p) return fail(REWL_ESTATE, "the engine was created without observables (rewl_batch_desc.observables)");
     const HostInst& H = e->inst[ii];
-    const int cols = (H.d.model == REWL_MODEL_ISING2D ? 3 : 12) + 1;
+    const int cols = obs_columns(H.d.model, e->desc.observables == 2) + 1;
     const bool half = H.d.model != REWL_MODEL_ISING2D && H.d.energy_max <= 0.0;
     int n = 0;
     int rc = rewl_global_logdos(e, ii, half ? 1 : 0, nullptr, nullptr, &n);
@@ -2686,12 +2888,17 @@ int rewl_write_outputs(rewl_engine* e, int32_t ii, const char* dir, const char* 
     std::vector<double> E(n), G(n);
     int rc = rewl_global_logdos(e, ii, half ? 1 : 0, E.data(), G.data(), &n);
     if (rc) return rc;
-    const int cols = e->obs.p ? (ising ? 4 : 13) : 0;
+    const bool corr = e->desc.observables == 2;
+    const int cols = e->obs.p ? obs_columns(H.d.model, corr) + 1 : 0;
     std::vector<double> O((size_t)n * std::max(cols, 1));
     if (cols && (rc = rewl_global_observables(e, ii, O.data(), &n))) return rc;
+    // Obs::string_names (ising2d_observables.hpp:40-46, ashkin_teller2d_observables.hpp:64-82)
     const char* sys_names = !cols ? "" : ising
-        ? "Magnetization\nMagnetization2\nMagnetization4\nCounts per Bin"
-        : "Sigma Mag\nSigma Mag2\nSigma Mag4\nTau Mag\nTau Mag2\nTau Mag4\nPhi\nPhi2\nPhi4\nBaxter\nBaxter2\nBaxter4\nCounts per Bin";
+        ? (corr ? "Magnetization\nMagnetization2\nMagnetization4\nG(qmin)\nCounts per Bin"
+                : "Magnetization\nMagnetization2\nMagnetization4\nCounts per Bin")
+        : (corr ? "Sigma Mag\nSigma Mag2\nSigma Mag4\nSigma G(qmin)\nTau Mag\nTau Mag2\nTau Mag4\nTau G(qmin)\n"
+                  "Phi\nPhi2\nPhi4\nPhi G(qmin)\nBaxter\nBaxter2\nBaxter4\nBaxter G(qmin)\nCounts per Bin"
+                : "Sigma Mag\nSigma Mag2\nSigma Mag4\nTau Mag\nTau Mag2\nTau Mag4\nPhi\nPhi2\nPhi4\nBaxter\nBaxter2\nBaxter4\nCounts per Bin");
     const double N = (double)H.dev.N;
     if ((rc = rewl_write_microcanonical(dir, file_string, header, sys_names, n, cols, N, E.data(), G.data(), O.data())))
         return rc;
@@ -2703,13 +2910,19 @@ int rewl_write_outputs(rewl_engine* e, int32_t ii, const char* dir, const char* 
     if ((rc = rewl_write_self_averaged(dir, file_string, header, thermal.c_str(), num_T, 5 + cols, T.data(), rows.data())))
         return rc;
     if (!cols) return REWL_OK;
-    const int nl = ising ? 2 : 8;
+    const int nl = ising ? (corr ? 3 : 2) : (corr ? 12 : 8);
     std::vector<double> nonlin((size_t)num_T * nl);
-    if ((rc = rewl_nonlinear_observables(H.d.model, rows.data(), num_T, 5 + cols, T.data(), N, nonlin.data())))
+    if ((rc = rewl_nonlinear_observables(H.d.model, corr ? 1 : 0, rows.data(), num_T, 5 + cols, T.data(), N, nonlin.data())))
         return fail(rc, "nonlinear observables: %s", rewl_thermo_last_error_string());
-    const char* nl_names = ising ? "Susceptibility\nBinder Cumulant"
-                                 : "Sigma Susceptibility\nSigma Binder Cumulant\nTau Susceptibility\nTau Binder Cumulant\n"
-                                   "Baxter Susceptibility\nBaxter Binder Cumulant\nPhi Susceptibility\nPhi Binder Cumulant";
+    // Obs::nonlinear_obs_strings (ising2d_observables.hpp:40-46, ashkin_teller2d_observables.hpp:64-82)
+    const char* nl_names = ising
+        ? (corr ? "Susceptibility\nBinder Cumulant\nCorrelation Length over L" : "Susceptibility\nBinder Cumulant")
+        : (corr ? "Sigma Susceptibility\nSigma Binder Cumulant\nSigma Correlation Length over L\n"
+                  "Tau Susceptibility\nTau Binder Cumulant\nTau Correlation Length over L\n"
+                  "Baxter Susceptibility\nBaxter Binder Cumulant\nBaxter Correlation Length over L\n"
+                  "Phi Susceptibility\nPhi Binder Cumulant\nPhi Correlation Length over L"
+                : "Sigma Susceptibility\nSigma Binder Cumulant\nTau Susceptibility\nTau Binder Cumulant\n"
+                  "Baxter Susceptibility\nBaxter Binder Cumulant\nPhi Susceptibility\nPhi Binder Cumulant");
     return rewl_write_nonlinear(dir, file_string, header, nl_names, num_T, nl, T.data(), nonlin.data());
 }
 

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cfloat>
 #include <cstdarg>
 #include <cstdio>
 #include <string>
@@ -170,22 +171,31 @@ int rewl_thermodynamics(const double* E, const double* lng, const double* obs, i
 // Susceptibilities and Binder cumulants from the rows of rewl_thermodynamics
 // (order_parameter_cumulants.hpp:17-48; calculate_nonlinear_observables,
 // ising2d_observables.hpp:166-198 and ashkin_teller2d_observables.hpp:243-282).
-int rewl_nonlinear_observables(int32_t model, const double* rows, int32_t num_T, int32_t row_len,
-                               const double* temperatures, double system_size, double* out)
+int rewl_nonlinear_observables(int32_t model, int32_t correlators, const double* rows, int32_t num_T,
+                               int32_t row_len, const double* temperatures, double system_size, double* out)
 {
-    const int need = model == REWL_MODEL_ISING2D ? 5 + 3 : 5 + 12;
-    if (!rows || !temperatures || !out || num_T < 1 || row_len < need ||
+    const bool corr = correlators != 0;
+    const int need = 5 + (model == REWL_MODEL_ISING2D ? (corr ? 4 : 3) : (corr ? 16 : 12));
+    if (!rows || !temperatures || !out || num_T < 1 || row_len < need || (correlators != 0 && correlators != 1) ||
         (model != REWL_MODEL_ISING2D && model != REWL_MODEL_ASHKIN_TELLER2D))
         return tfail(REWL_EINVAL, "bad arguments (rows of at least %d columns)", need);
     auto susc = [&](double m2, double m, double T) { return system_size * (m2 - m * m) / T; };
     auto binder = [](double m4, double m2) { return 1.0 - (m4 / (m2 * m2)) / 3.0; };
+    // calculate_correlation_length(G0, Gq, L) / L with L = (size_t) sqrt(N)
+    const size_t Ls = static_cast<size_t>(std::sqrt(system_size));
+    auto xi = [&](double G0, double Gq) {
+        const double x = Gq == 0. ? DBL_MAX : (static_cast<double>(Ls) / (2. * std::acos(-1.))) * std::sqrt((G0 - Gq) / Gq);
+        return x / static_cast<double>(Ls);
+    };
     for (int t = 0; t < num_T; ++t) {
         const double* o = rows + (size_t)t * row_len + 5;
         const double T = temperatures[t];
         if (model == REWL_MODEL_ISING2D) {
-            out[2 * t] = susc(o[1], o[0], T);
-            out[2 * t + 1] = binder(o[2], o[1]);
-        } else {
+            double* r = out + (size_t)t * (corr ? 3 : 2);
+            r[0] = susc(o[1], o[0], T);
+            r[1] = binder(o[2], o[1]);
+            if (corr) r[2] = xi(o[1], o[3]);
+        } else if (!corr) {
             double* r = out + 8 * (size_t)t;
             const int bases[3] = {0, 3, 9};            // sigma, tau, Baxter
             for (int k = 0; k < 3; ++k) {
@@ -194,6 +204,21 @@ int rewl_nonlinear_observables(int32_t model, const double* rows, int32_t num_T,
             }
             r[6] = susc(o[7], o[6], T);                 // phi: two-component order parameter
             r[7] = 2.0 * (1.0 - 0.5 * (o[8] / (o[7] * o[7])));
+        } else {
+            // groups of (|x|, x^2, x^4, G): sigma 0, tau 4, phi 8, Baxter 12; output order
+            // sigma, tau, Baxter, phi with (susceptibility, cumulant, correlation length)
+            double* r = out + 12 * (size_t)t;
+            const int bases[3] = {0, 4, 12};
+            for (int k = 0; k < 3; ++k) {
+                const double* g = o + bases[k];
+                r[3 * k] = susc(g[1], g[0], T);
+                r[3 * k + 1] = binder(g[2], g[1]);
+                r[3 * k + 2] = xi(g[1], g[3]);
+            }
+            const double* g = o + 8;
+            r[9] = susc(g[1], g[0], T);
+            r[10] = 2.0 * (1.0 - 0.5 * (g[2] / (g[1] * g[1])));
+            r[11] = xi(g[1], g[3]);
         }
     }
     return REWL_OK;

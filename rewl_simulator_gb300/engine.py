@@ -107,7 +107,7 @@ class Batch:
     device: int = 0
     warps_per_block: int = 0
     walkers_per_warp: int = 0
-    observables: int = 0
+    observables: int = 0            # 1: per-bin moments; 2: also the G(q_min) correlators
 
 
 @dataclass
@@ -127,6 +127,13 @@ class Status:
 
 def _p(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def obs_columns(model: int, observables: int) -> int:
+    """Columns of an exported observables row: the averages and the count.  Ising |m|, m^2, m^4
+    (+ G(q_min)); Ashkin-Teller 12 moments (+ a G(q_min) after each group of three)."""
+    corr = observables == 2
+    return (5 if corr else 4) if model == MODEL_ISING2D else (17 if corr else 13)
 
 
 class Engine:
@@ -284,10 +291,10 @@ class Engine:
         return dict(dofs=dofs, state=state, counts=counts, logdos=logdos, visits=visits)
 
     def _obs_cols(self, instance: int) -> int:
-        return 4 if self.batch.instances[instance].model == MODEL_ISING2D else 13
+        return obs_columns(self.batch.instances[instance].model, self.batch.observables)
 
     def export_observables(self, walker: int) -> np.ndarray:
-        """Per-bin observable averages of a walker, rows of [K averages, count] (observables=1)."""
+        """Per-bin observable averages of a walker, rows of [K averages, count] (observables=1 or 2)."""
         inst, w, _ = self._walker_inst[walker]
         out = np.zeros((self.windows[inst][w][2], self._obs_cols(inst)))
         self._check(self.lib.rewl_export_observables(self.h, walker, _p(out)))

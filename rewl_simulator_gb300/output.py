@@ -16,7 +16,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _native
-from .engine import Engine, REWLError
+from .engine import Engine, REWLError, obs_columns
 
 
 def _p(a):
@@ -43,7 +43,7 @@ def global_observables(engine: Engine, instance: int) -> np.ndarray:
     """Observables on the energies of global_logdos (rows: K averages, count)."""
     E, _ = engine.global_logdos(instance, half_spectrum=engine.batch.instances[instance].model != 0
                                 and engine.batch.instances[instance].energy_max <= 0.0)
-    cols = 4 if engine.batch.instances[instance].model == 0 else 13
+    cols = obs_columns(engine.batch.instances[instance].model, engine.batch.observables)
     out = np.zeros((E.size, cols))
     n = C.c_int32(E.size)
     _check(engine.lib, engine.lib.rewl_global_observables(engine.h, instance, _p(out), C.byref(n)))

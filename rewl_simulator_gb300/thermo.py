@@ -42,13 +42,16 @@ def thermodynamics(E, lng, N: int, obs=None, counts_col: int = -1, Tmin: float =
     return T, out
 
 
-def nonlinear(model: int, T: np.ndarray, rows: np.ndarray, N: int) -> np.ndarray:
-    """Susceptibilities and Binder cumulants per temperature (Ising: 2 columns; AT: 8)."""
+def nonlinear(model: int, T: np.ndarray, rows: np.ndarray, N: int, correlators: bool = False) -> np.ndarray:
+    """Susceptibilities and Binder cumulants per temperature (Ising: 2 columns; AT: 8); with
+    correlators (rows in the observables = 2 layout) each pair is followed by the correlation
+    length over L (Ising: 3 columns; AT: 12)."""
     lib = _native.load()
     rows = np.ascontiguousarray(rows, dtype=np.float64)
     T = np.ascontiguousarray(T, dtype=np.float64)
-    out = np.zeros((T.size, 2 if model == 0 else 8))
-    rc = lib.rewl_nonlinear_observables(model, _p(rows), T.size, rows.shape[1], _p(T), float(N), _p(out))
+    out = np.zeros((T.size, (2 if model == 0 else 8) * (3 if correlators else 2) // 2))
+    rc = lib.rewl_nonlinear_observables(model, int(bool(correlators)), _p(rows), T.size, rows.shape[1], _p(T),
+                                        float(N), _p(out))
     if rc != 0:
         raise REWLError(rc, lib.rewl_thermo_last_error_string().decode())
     return out

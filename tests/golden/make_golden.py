@@ -24,6 +24,8 @@ Groups
               on the exact L = 16 Ising ln g with synthetic observables, and on a
               synthetic Ashkin-Teller-like spectrum with 12 moments, with and without
               the trapezoidal rule.
+  cumulants-- the reference's susceptibility, Binder cumulants and correlation length
+              (src/Thermodynamics/order_parameter_cumulants.hpp:17-59) on random averages.
   writers  -- the reference's three output writers (oracle/ref_writers.cpp) on
               the thermo_ising inputs: tests/golden/writers/*.txt.
 """
@@ -284,7 +286,28 @@ def gen_writers():
     print("wrote", sorted(x.name for x in d.iterdir()))
 
 
+def gen_cumulants():
+    """The reference's order_parameter_cumulants.hpp on random thermal averages (including a
+    vanishing G, where the correlation length is DBL_MAX / L, and G above <m^2>)."""
+    import ctypes as C
+    lib = C.CDLL(str(build_ref.build_thermo(True, force=True)))
+    rng = np.random.default_rng(77)
+    n, N = 64, 256
+    m = rng.uniform(0.05, 0.95, n)
+    m2 = m * m + rng.uniform(0.0, 0.05, n)
+    m4 = m2 * m2 + rng.uniform(0.0, 0.05, n)
+    G = m2 * rng.uniform(0.01, 0.9, n)
+    G[0], G[1] = 0.0, 1.5 * m2[1]
+    T = rng.uniform(0.1, 10.0, n)
+    out = np.zeros((n, 4))
+    p = lambda a: np.ascontiguousarray(a).ctypes.data_as(C.c_void_p)
+    lib.ref_cumulants(C.c_size_t(n), p(m), p(m2), p(m4), p(G), p(T), C.c_size_t(N), p(out))
+    np.savez_compressed(OUT / "cumulants.npz", m=m, m2=m2, m4=m4, G=G, T=T, N=N, out=out)
+    print("wrote cumulants", out[:2])
+
+
 if __name__ == "__main__":
-    groups = sys.argv[1:] or ["replay", "replay_corr", "glazier", "rng", "normalize", "exact", "thermo", "writers"]
+    groups = sys.argv[1:] or ["replay", "replay_corr", "glazier", "rng", "normalize", "exact", "thermo", "cumulants",
+                              "writers"]
     for g in groups:
         globals()[f"gen_{g}"]()

@@ -13,7 +13,18 @@ import pytest
 
 from conftest import GOLDEN
 
-REPLAY = sorted(p.name for p in GOLDEN.glob("replay_*.npz") if not p.name.startswith("replay_corr_"))
+REPLAY = sorted(p.name for p in GOLDEN.glob("replay_*.npz"))
+
+
+def _assert_obs_close(got, ref, corr, msg="", rtol=1e-12):
+    """Moments to FP64 rounding of the running means; the G(q_min) columns (every fourth with
+    correlators) to the rounding of a transform summed in another order: the reference adds
+    it site by site, the kernels from row and column sums."""
+    g = np.zeros(got.shape[1], bool)
+    if corr:
+        g[3::4] = True
+    np.testing.assert_allclose(got[:, ~g], ref[:, ~g], rtol=rtol, atol=1e-15, err_msg=msg)
+    np.testing.assert_allclose(got[:, g], ref[:, g], rtol=1e-10, atol=1e-14, err_msg=msg + " G(q_min)")
 
 
 def _engine_layout(dofs_ref: np.ndarray, model: int) -> np.ndarray:
@@ -27,13 +38,14 @@ def _engine_layout(dofs_ref: np.ndarray, model: int) -> np.ndarray:
 def test_replay_matches_reference(engine_lib, oracle_lib, name):
     rg, po = engine_lib, oracle_lib
     z = np.load(GOLDEN / name)
+    corr = name.startswith("replay_corr_")     # the reference's CORRELATION_LENGTHS build
     model = int(z["model"])
     fields = z["fields"] if z["fields"].size else None
     ins = rg.Instance(model=model, L=int(z["L"]), J=1.0, K=float(z["K"]) if model else 0.0, fields=fields,
                       energy_min=float(z["wmin"]), energy_max=float(z["wmax"]), bin_width=float(z["bw"]),
                       num_windows=1, replicas_per_window=1, init_mode=1, seed=1)
     b = rg.Batch(instances=[ins], rng_mode=rg.RNG_REPLAY, lnf_initial=float(z["lnf1"]), lnf_final=1e-9,
-                 observables=1)
+                 observables=2 if corr else 1)
     with rg.Engine(b) as eng:
         which = int(z["state0"][4]) if model else 0
         eng.import_dofs(0, _engine_layout(z["dofs0"], model), which)
@@ -56,7 +68,7 @@ def test_replay_matches_reference(engine_lib, oracle_lib, name):
             # per-bin observables: the reference's running means, to FP64 rounding
             obs, ref = eng.export_observables(0), z[f"obs{stage}"]
             np.testing.assert_array_equal(obs[:, -1], ref[:, -1])
-            np.testing.assert_allclose(obs[:, :-1], ref[:, :-1], rtol=1e-12, atol=1e-15)
+            _assert_obs_close(obs[:, :-1], ref[:, :-1], corr, f"stage {stage}")
 
 
 def _pair(rg, po, model, L, emin, emax, bw, nwin, R, se, sc, seed, K=0.5, fields=None, flat=0.8,
@@ -172,11 +184,18 @@ def test_ising_L8_converges_to_exact(engine_lib):
 
 
 OBS_CASES = [
-    # name, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles, walkers_per_warp, sigma_h, mask
-    ("ising_L8_bins", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 3, 0, 0.0, 0),
-    ("ising_L16_bins_2perwarp", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 3, 2, 0.0, 0),
-    ("ising_L12_bw8_general", 0, 12, -288.0, 296.0, 8.0, 4, 2, 10, 20, 3, 3, 0, 0.0, 0),
-    ("at_L4_rf", 1, 4, -(2.5) * 2 * 16, 0.0, 0.05, 2, 2, 20, 40, 7, 3, 0, 0.5, 1),
+    # name, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles, walkers_per_warp, sigma_h, mask, observables
+    ("ising_L8_bins", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 3, 0, 0.0, 0, 1),
+    ("ising_L16_bins_2perwarp", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 3, 2, 0.0, 0, 1),
+    ("ising_L12_bw8_general", 0, 12, -288.0, 296.0, 8.0, 4, 2, 10, 20, 3, 3, 0, 0.0, 0, 1),
+    ("at_L4_rf", 1, 4, -(2.5) * 2 * 16, 0.0, 0.05, 2, 2, 20, 40, 7, 3, 0, 0.5, 1, 1),
+    # with the G(q_min) correlators: general Ising kernel (chunk = row, and chunks within a row)
+    # and the Ashkin-Teller kernel; exchanges add transforms through the exchange touch
+    ("ising_L8_corr", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 4, 0, 0.0, 0, 2),
+    ("ising_L16_corr", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 3, 0, 0.0, 0, 2),
+    ("ising_L64_corr_chunks", 0, 64, -8192.0, -7000.0, 4.0, 2, 2, 4, 8, 29, 2, 0, 0.0, 0, 2),
+    ("at_L4_rf_corr", 1, 4, -(2.5) * 2 * 16, 0.0, 0.05, 2, 2, 20, 40, 7, 3, 0, 0.5, 1, 2),
+    ("at_L8_rf_corr", 1, 8, -(2.5) * 2 * 64, -40.0, 0.05, 2, 2, 10, 20, 9, 3, 0, 0.5, 1, 2),
 ]
 
 
@@ -185,12 +204,12 @@ OBS_CASES = [
 def test_engine_observables_match_oracle(engine_lib, oracle_lib, case):
     """Per-bin observables of every walker, and their count-weighted window average, against
     the oracle's running means after every check interval (all three sweep kernels)."""
-    _, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles, wpw, sig, mask = case
+    _, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles, wpw, sig, mask, obs_mode = case
     fields = None
     if sig > 0:
         fields = np.round(np.random.default_rng(seed).normal(0, sig, L * L) * 2**20) / 2**20
     eng, orc = _pair(engine_lib, oracle_lib, model, L, emin, emax, bw, nwin, R, se, sc, seed, fields=fields,
-                     mask=mask, walkers_per_warp=wpw, observables=1)
+                     mask=mask, walkers_per_warp=wpw, observables=obs_mode)
     try:
         for k in range(cycles):
             eng.run_cycles(1)
@@ -202,14 +221,13 @@ def test_engine_observables_match_oracle(engine_lib, oracle_lib, case):
                     s = w * R + r
                     got, ref = eng.export_observables(s), orc.obs(s)
                     np.testing.assert_array_equal(got[:, -1], ref[:, -1], err_msg=f"cycle {k} walker {s} counts")
-                    np.testing.assert_allclose(got[:, :-1], ref[:, :-1], rtol=1e-12, atol=1e-15,
-                                               err_msg=f"cycle {k} walker {s}")
+                    _assert_obs_close(got[:, :-1], ref[:, :-1], obs_mode == 2, f"cycle {k} walker {s}")
                     ws.append(ref)
                 cnt = sum(o[:, -1] for o in ws)
                 avg = sum(o[:, :-1] * o[:, -1:] for o in ws) / np.maximum(cnt, 1)[:, None]
                 got = eng.window_observables(0, w)
                 np.testing.assert_array_equal(got[:, -1], cnt)
-                np.testing.assert_allclose(got[:, :-1], avg, rtol=1e-11, atol=1e-15, err_msg=f"cycle {k} window {w}")
+                _assert_obs_close(got[:, :-1], avg, obs_mode == 2, f"cycle {k} window {w}", rtol=1e-11)
     finally:
         eng.close()
         orc.close()

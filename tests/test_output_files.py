@@ -55,3 +55,47 @@ def test_write_outputs_end_to_end(engine_lib, tmp_path):
     np.testing.assert_allclose(sa[:, 1:], rows, rtol=1e-13, atol=1e-300)
     nl = np.loadtxt(files[2], delimiter=",", comments="#")
     np.testing.assert_allclose(nl[:, 1:], thermo.nonlinear(0, T, rows, 64), rtol=1e-13)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model", [0, 1])
+def test_write_outputs_with_correlators(engine_lib, tmp_path, model):
+    """observables = 2, the reference's default CORRELATION_LENGTHS build: the microcanonical and
+    self-averaged files carry the G(q_min) columns named as the reference names them, and the
+    nonlinear file the correlation lengths over L."""
+    rg = engine_lib
+    from rewl_simulator_gb300 import output, thermo
+    if model == 0:
+        ins = rg.Instance(model=0, L=8, energy_min=-128.0, energy_max=132.0, bin_width=4.0, num_windows=3,
+                          replicas_per_window=2, seed=5)
+        N, K = 64, 4
+    else:
+        h = np.round(np.random.default_rng(3).normal(0, 0.5, 16) * 2**20) / 2**20
+        ins = rg.Instance(model=1, L=4, K=0.5, fields=h, energy_min=-80.0, energy_max=0.0, bin_width=0.05,
+                          num_windows=2, replicas_per_window=2, seed=5)
+        N, K = 16, 16
+    # with random fields many bins are unreachable: flatness over the visited bins
+    b = rg.Batch(instances=[ins], sweeps_per_exchange=50, sweeps_per_check=100, lnf_final=1e-3, observables=2,
+                 mask_mode=0 if model == 0 else rg.MASK_VISITED)
+    with rg.Engine(b) as eng:
+        eng.simulate(max_cycles=400)
+        files = output.write_outputs(eng, 0, tmp_path, "corr", header="# test\n", num_T=300)
+        E, lng = eng.global_logdos(0, half_spectrum=model == 1)
+        obs = output.global_observables(eng, 0)
+    assert obs.shape[1] == K + 1
+    micro_text = files[0].read_text()
+    assert ("G(qmin)" in micro_text) if model == 0 else all(
+        f"{x} G(qmin)" in micro_text for x in ("Sigma", "Tau", "Phi", "Baxter"))
+    micro = np.loadtxt(files[0], delimiter=",", comments="#")
+    np.testing.assert_allclose(micro[:, 2:], obs, rtol=1e-14)
+    g_cols = [3] if model == 0 else [3, 7, 11, 15]
+    assert np.all(obs[:, g_cols] >= 0) and np.any(obs[:, g_cols] > 0)
+    if model == 1:
+        # tau's correlator is computed from sigma, as the reference does; phi's is the sum
+        np.testing.assert_array_equal(obs[:, 7], obs[:, 3])
+        np.testing.assert_allclose(obs[:, 11], 2 * obs[:, 3], rtol=1e-15)
+    T, rows = thermo.thermodynamics(E, lng, N, obs=obs, counts_col=K, num_T=300)
+    nl = np.loadtxt(files[2], delimiter=",", comments="#")
+    assert nl.shape[1] == 1 + (3 if model == 0 else 12)
+    np.testing.assert_allclose(nl[:, 1:], thermo.nonlinear(model, T, rows, N, correlators=True), rtol=1e-13)
+    assert "Correlation Length over L" in files[2].read_text()

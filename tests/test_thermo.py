@@ -91,3 +91,41 @@ def test_gpu_thermodynamics_reference_ladder_on_exact_L64(engine_lib):
     _check(T[pick], out[pick], {"N": 4096, "out": ref[pick], "temperatures": T2[pick]})
     # the specific-heat peak sits near the critical temperature 2 / ln(1 + sqrt 2) = 2.269
     assert abs(T[np.argmax(out[:, 4])] - 2.269) < 0.05
+
+
+def test_cumulants_pinned_to_reference():
+    """The restatement's susceptibility, Binder cumulants and correlation length over L against
+    the reference's order_parameter_cumulants.hpp (tests/golden/cumulants.npz), including the
+    DBL_MAX / L of a vanishing G and the NaN of G above <m^2>."""
+    z = np.load(GOLDEN / "cumulants.npz")
+    N = int(z["N"])
+    got = np.stack([thermo_ref.susceptibility(z["m2"], z["m"], z["T"], float(N)),
+                    thermo_ref.binder(z["m4"], z["m2"]), thermo_ref.binder_two_component(z["m4"], z["m2"]),
+                    thermo_ref.correlation_length_over_L(z["m2"], z["G"], N)], axis=1)
+    np.testing.assert_array_equal(got, z["out"])
+
+
+def _rows_with_correlators(model, nT, seed):
+    rng = np.random.default_rng(seed)
+    groups = 1 if model == 0 else 4
+    cols = []
+    for _ in range(groups):
+        m = rng.uniform(0.05, 0.95, nT)
+        m2 = m * m + rng.uniform(0.0, 0.05, nT)
+        cols += [m, m2, m2 * m2 + rng.uniform(0.0, 0.05, nT), m2 * rng.uniform(0.01, 0.9, nT)]
+    thermal = rng.uniform(-2, 2, (nT, 5))
+    counts = rng.integers(1, 100, (nT, 1)).astype(np.float64)
+    return np.ascontiguousarray(np.concatenate([thermal, np.stack(cols, 1), counts], axis=1))
+
+
+def test_nonlinear_observables_with_correlators_host(engine_lib):
+    """The C ABI's correlation lengths (observables = 2 layout) against the restatement."""
+    from rewl_simulator_gb300 import thermo
+    for model in (0, 1):
+        rows = _rows_with_correlators(model, 300, 5 + model)
+        rows[0, 5 + 3] = 0.0                      # a vanishing G: DBL_MAX / L
+        T = np.linspace(0.1, 5.0, 300)
+        got = thermo.nonlinear(model, T, rows, 256, correlators=True)
+        ref = thermo_ref.nonlinear(model, rows, T, 256.0, correlators=True)
+        assert got.shape == (300, 3 if model == 0 else 12)
+        np.testing.assert_allclose(got, ref, rtol=1e-14, atol=0)
