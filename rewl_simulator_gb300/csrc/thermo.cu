@@ -37,7 +37,7 @@ int tfail(int code, const char* fmt, ...)
 }
 
 constexpr int kThreads = 256;
-constexpr int kMaxObs = 16;
+constexpr int kMaxObs = 20;            // Ashkin-Teller with correlators: 16 averages + the count
 
 __device__ double block_sum(double v, double* sh)
 {
