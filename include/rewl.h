@@ -93,6 +93,9 @@ typedef struct rewl_batch_desc {
                                      2: also the G(q_min) Fourier correlators of the reference's default
                                      CORRELATION_LENGTHS build (src/Hamiltonians/Correlations/
                                      fourier_correlator.hpp), one transform at every 1000th count of a bin */
+    int32_t graphs;               /* 1: rewl_run_cycles replays each check interval (sweeps, exchanges,
+                                     flatness step) as one captured CUDA graph */
+    int32_t autotune;             /* 1: the first rewl_run_cycles call runs rewl_autotune first */
     const rewl_instance_desc* instances;
 } rewl_batch_desc;
 
@@ -178,6 +181,15 @@ int rewl_reset_histograms(rewl_engine* eng, int32_t instance, int32_t window, in
  * stopping early once every window is done or `timeout_ms` (> 0) has passed.
  * The main loop of REWL_simulation::simulate (src/Simulation/rewl_simulation.hpp:473-691). */
 int rewl_run_cycles(rewl_engine* eng, int64_t num_cycles, int64_t timeout_ms, rewl_status* status);
+/* Time each launch group's admissible kernel shapes (walkers per warp, warps per block) on a
+ * few sweeps each (sweeps = 0: about 2e7 attempted flips per trial) and keep the fastest; the
+ * engine's state is saved before and restored after, so the simulation is unchanged.  Launch
+ * groups (model x kernel x lattice size) of a heterogeneous batch run concurrently on their
+ * own streams in every sweep phase. */
+int rewl_autotune(rewl_engine* eng, int32_t sweeps);
+/* The launch groups' shapes: count rows of [model, bin-tracking kernel, walkers per warp,
+ * warps per block]; with shapes NULL or *count too small only *count is set. */
+int rewl_launch_shapes(rewl_engine* eng, int32_t* shapes, int32_t* count);
 
 /* Counters; synchronises the engine's stream. */
 int rewl_get_status(rewl_engine* eng, rewl_status* status);

@@ -100,6 +100,8 @@ def _declare(L: C.CDLL) -> None:
         "rewl_export_walker": [vp, i32, vp, vp, vp, vp, vp],
         "rewl_export_observables": [vp, i32, vp],
         "rewl_thermodynamics": [vp, vp, vp, i32, i32, i32, C.c_double, C.c_double, C.c_double, i32, i32, i32, vp, vp],
+        "rewl_autotune": [vp, i32],
+        "rewl_launch_shapes": [vp, vp, vp],
         "rewl_nonlinear_observables": [i32, i32, vp, i32, i32, vp, C.c_double, vp],
         "rewl_global_observables": [vp, i32, vp, vp],
         "rewl_write_microcanonical": [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, i32, i32, C.c_double, vp, vp, vp],

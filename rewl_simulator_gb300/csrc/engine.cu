@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cfloat>
 #include <cstdarg>
 #include <cstdlib>
 #include <cstdio>
@@ -130,6 +131,7 @@ struct DevPtrs {
     uint64_t* win_sweepctr;
     int32_t* pairs;          // exchange pair lists: (instance, lower window) for dir 0 then dir 1
     int32_t* counters;       // [0] error word, [1] flat events (this call)
+    unsigned long long* xround;  // [0] exchange round (its parity is the pairing direction), [1] blocks done
     unsigned long long* stats;  // [0] exch attempted, [1] exch accepted
     double* obs;             // per-bin observable sums (obs_stride per bin), or null when off
     int obs_stride;          // 3 (Ising) or 12 (a batch with Ashkin-Teller instances); 4 or 16 with correlators
@@ -1363,10 +1365,8 @@ __device__ inline void touch(const DevPtrs& P, const InstDev& I, int slot)
     }
 }
 
-__global__ void k_exchange(DevPtrs P, const int32_t* pairs, int npairs, uint64_t round)
+__device__ void exchange_pair(const DevPtrs& P, const int32_t* pairs, int k, uint64_t round)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= npairs) return;
     const int ii = pairs[2 * k], lw = pairs[2 * k + 1];
     const InstDev I = P.inst[ii];
     const int R = I.R;
@@ -1410,6 +1410,28 @@ __global__ void k_exchange(DevPtrs P, const int32_t* pairs, int npairs, uint64_t
     }
     atomicAdd(&P.stats[0], att);
     atomicAdd(&P.stats[1], accn);
+}
+
+// One exchange round: one thread per (instance, lower window) pair of the round's direction.
+// The round counter lives on the device (so that a captured cycle replays correctly): every
+// thread reads it first, and the last block to finish advances it.
+__global__ void k_exchange(DevPtrs P, const int32_t* pairs0, int n0, const int32_t* pairs1, int n1)
+{
+    __shared__ bool last;
+    const uint64_t round = *(volatile unsigned long long*)P.xround;
+    const int dir = (int)(round & 1u);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < (dir ? n1 : n0)) exchange_pair(P, dir ? pairs1 : pairs0, k, round);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&P.xround[1], 1ull) == (unsigned long long)(gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        P.xround[1] = 0;
+        P.xround[0] = round + 1;
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -1645,6 +1667,14 @@ struct rewl_engine {
     std::vector<Launch> launches;
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
+    // one check interval captured as a CUDA graph (rewl_batch_desc.graphs): the host counters it
+    // advances per replay, and the timing events recorded inside it
+    cudaGraphExec_t cycle_exec = nullptr;
+    bool capturing = false;
+    int64_t g_sweeps = 0, g_flips = 0, g_launches = 0, g_kernel_launches = 0, g_rounds = 0;
+    std::vector<cudaEvent_t> g_events;
+    double graph_sweep_ms = 0;          // sweep-phase time of replayed graphs since the last timing read
+    bool tuned = false;
     int64_t kernel_launches = 0;        // sweep-kernel launches since the last timing read
     int64_t launches_total = 0;         // every engine kernel since creation
     int sweep_variant = 3;              // Ising resolver: 3 all-lane (default), 2 lane-0 (REWL_SWEEP_VARIANT=2)
@@ -1663,6 +1693,10 @@ struct rewl_engine {
     DBuf<double> obs;           // per-bin observable sums (observables on)
     DBuf<int64_t> gsnap;        // Ashkin-Teller engines: logDoS copy taken by each sweep launch
     DBuf<double> qtab;          // correlator kernels (observables == 2)
+    DBuf<unsigned long long> xround;   // exchange round and the exchange kernel's done-block count
+    std::vector<cudaStream_t> gstreams; // one per launch group when there are several (they run concurrently)
+    cudaEvent_t fork_ev = nullptr;
+    std::vector<cudaEvent_t> join_ev;
     int obs_stride = 0;
     std::vector<int64_t> h_thr_off, h_thr_n;
     std::vector<int64_t> h_fields;
@@ -1680,9 +1714,18 @@ struct rewl_engine {
         P.g = g.p; P.gsnap = gsnap.p; P.H = H.p; P.visits = visits.p; P.mask = mask.p;
         P.win_lnf = win_lnf.p; P.win_done = win_done.p; P.win_oot = win_oot.p; P.win_iter = win_iter.p;
         P.win_sweepctr = win_sweepctr.p; P.pairs = nullptr; P.counters = counters.p; P.stats = stats.p;
+        P.xround = xround.p;
         P.obs = obs.p; P.obs_stride = obs_stride;
         P.corr = desc.observables == 2 ? 1 : 0; P.qtab = qtab.p;
         return P;
+    }
+
+    void drop_graph()
+    {
+        if (cycle_exec) cudaGraphExecDestroy(cycle_exec);
+        cycle_exec = nullptr;
+        for (auto ev : g_events) cudaEventDestroy(ev);
+        g_events.clear();
     }
 
     void release()
@@ -1690,7 +1733,12 @@ struct rewl_engine {
         d_inst.free_(); d_win.free_();
         slot_inst.free_(); slot_win.free_(); slot_cfg.free_(); slot_nb.free_(); slot_flavour.free_();
         pairs[0].free_(); pairs[1].free_();
-        obs.free_(); gsnap.free_(); qtab.free_();
+        obs.free_(); gsnap.free_(); qtab.free_(); xround.free_();
+        for (cudaStream_t st : gstreams) cudaStreamDestroy(st);
+        gstreams.clear();
+        for (cudaEvent_t ev : join_ev) cudaEventDestroy(ev);
+        join_ev.clear();
+        if (fork_ev) { cudaEventDestroy(fork_ev); fork_ev = nullptr; }
         slot_tab.free_(); slot_draws.free_(); slot_thr_off.free_(); slot_thr_n.free_(); cfg_off.free_();
         cfg_E.free_(); fields.free_(); g.free_(); win_lnf.free_(); slot_sweeps.free_(); visits.free_();
         win_iter.free_(); win_sweepctr.free_(); spins.free_(); cfg_M.free_(); win_done.free_(); win_oot.free_();
@@ -1698,6 +1746,7 @@ struct rewl_engine {
         for (auto& l : launches) l.d_slots.free_();
         for (auto e : ev_pool) cudaEventDestroy(e);
         ev_pool.clear();
+        drop_graph();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -1942,7 +1991,8 @@ int upload_all(rewl_engine* e)
         (rc = e->cfg_M.alloc(3 * (size_t)slot)) || (rc = e->spins.alloc(spin)) || (rc = e->g.alloc(tab)) ||
         (rc = e->H.alloc(tab)) || (rc = e->visits.alloc(tab)) || (rc = e->win_lnf.alloc(win)) ||
         (rc = e->win_done.alloc(win)) || (rc = e->win_oot.alloc(win)) || (rc = e->win_iter.alloc(win)) ||
-        (rc = e->win_sweepctr.alloc(win)) || (rc = e->counters.alloc(4)) || (rc = e->stats.alloc(2)))
+        (rc = e->win_sweepctr.alloc(win)) || (rc = e->counters.alloc(4)) || (rc = e->stats.alloc(2)) ||
+        (rc = e->xround.alloc(2)))
         return rc;
     CUDA_TRY(cudaMemsetAsync(e->slot_sweeps.p, 0, slot * sizeof(uint64_t), s));
     CUDA_TRY(cudaMemsetAsync(e->slot_draws.p, 0, slot * sizeof(int64_t), s));
@@ -1970,6 +2020,7 @@ int upload_all(rewl_engine* e)
     CUDA_TRY(cudaMemsetAsync(e->win_sweepctr.p, 0, win * sizeof(uint64_t), s));
     CUDA_TRY(cudaMemsetAsync(e->counters.p, 0, 4 * sizeof(int32_t), s));
     CUDA_TRY(cudaMemsetAsync(e->stats.p, 0, 2 * sizeof(unsigned long long), s));
+    CUDA_TRY(cudaMemsetAsync(e->xround.p, 0, 2 * sizeof(unsigned long long), s));
     return REWL_OK;
 }
 
@@ -1988,6 +2039,34 @@ bool bins_eligible(const InstDev& I, const rewl_batch_desc& D)
     const long long maxbins = (8 * std::llabs(I.J_u)) >> I.bin_shift;
     if (2 * maxbins > kGuard) return false;
     return true;
+}
+
+// The logDoS tables of the Ashkin-Teller kernel live in global memory and are read through L1,
+// so its shared-memory carveout is the smallest that still holds the blocks resident on an SM
+// (the driver's default leaves L1 far less).
+int at_carveout(rewl_engine* e, Launch& l)
+{
+    if (l.bins || l.model == REWL_MODEL_ISING2D) return REWL_OK;
+    const int nsm = 152;
+    const SweepKernel fn = at_kernel(e->desc.rng_mode == REWL_RNG_REPLAY, e->desc.observables != 0);
+    const int threads = 32 * l.wpb;
+    const size_t smem = (size_t)l.wpb * l.smem_per_warp;
+    int occ = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem));
+    const int blocks = ((int)l.slots.size() + l.wpb - 1) / l.wpb;
+    const int per_sm = std::max(1, std::min(occ, (blocks + nsm - 1) / nsm));
+    int smem_sm = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->desc.device));
+    const size_t need = (size_t)per_sm * (smem + 1024);
+    l.carveout = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / (size_t)smem_sm);
+    return REWL_OK;
+}
+
+// A launch group's shape: walkers per warp (bin-tracking kernel) and warps per block, if the
+// block's shared memory fits.
+bool shape_fits(const Launch& l, int G, int wpb)
+{
+    return (size_t)wpb * (l.bins ? G : 1) * l.smem_per_warp <= 200 * 1024;
 }
 
 int plan_launches(rewl_engine* e)
@@ -2068,26 +2147,22 @@ int plan_launches(rewl_engine* e)
     for (int r = 0; r < 2; ++r)
         for (int o = 0; o < 2; ++o)
             CUDA_TRY(cudaFuncSetAttribute(at_kernel(r, o), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-    for (auto& l : e->launches) {
-        if (l.bins || l.model == REWL_MODEL_ISING2D) continue;
-        // The logDoS tables of this kernel live in global memory and are read through
-        // L1, so the shared-memory carveout is the smallest that still holds the
-        // blocks resident on an SM; the driver's default leaves L1 far less.
-        const SweepKernel fn = at_kernel(e->desc.rng_mode == REWL_RNG_REPLAY, e->desc.observables != 0);
-        const int threads = 32 * l.wpb;
-        const size_t smem = (size_t)l.wpb * l.smem_per_warp;
-        int occ = 0;
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem));
-        const int blocks = ((int)l.slots.size() + l.wpb - 1) / l.wpb;
-        const int per_sm = std::max(1, std::min(occ, (blocks + nsm - 1) / nsm));
-        int smem_sm = 0;
-        CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->desc.device));
-        const size_t need = (size_t)per_sm * (smem + 1024);
-        l.carveout = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / (size_t)smem_sm);
-    }
+    for (auto& l : e->launches)
+        if (int rc = at_carveout(e, l)) return rc;
     CUDA_TRY(allow_bins_smem<1>());
     CUDA_TRY(allow_bins_smem<2>());
     CUDA_TRY(allow_bins_smem<4>());
+    if (e->launches.size() > 1) {
+        CUDA_TRY(cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming));
+        for (size_t gi = 0; gi < e->launches.size(); ++gi) {
+            cudaStream_t st;
+            cudaEvent_t ev;
+            CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            e->gstreams.push_back(st);
+            CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            e->join_ev.push_back(ev);
+        }
+    }
     return REWL_OK;
 }
 
@@ -2107,6 +2182,12 @@ int check_device_error(rewl_engine* e)
 
 cudaEvent_t next_event(rewl_engine* e)
 {
+    if (e->capturing) {                // a timing event owned by the captured graph
+        cudaEvent_t ev;
+        cudaEventCreate(&ev);
+        e->g_events.push_back(ev);
+        return ev;
+    }
     if (e->ev_used == e->ev_pool.size()) {
         cudaEvent_t ev;
         cudaEventCreate(&ev);
@@ -2115,44 +2196,60 @@ cudaEvent_t next_event(rewl_engine* e)
     return e->ev_pool[e->ev_used++];
 }
 
-int launch_sweeps(rewl_engine* e, int nsweeps)
+// One launch group's sweeps on a stream (its kernel and shape fixed by plan_launches or the
+// autotuner).
+int launch_group(rewl_engine* e, Launch& l, cudaStream_t stream, int nsweeps, const DevPtrs& P)
 {
-    const DevPtrs P = e->ptrs();
     const bool replay = e->desc.rng_mode == REWL_RNG_REPLAY;
-    cudaEventRecord(next_event(e), e->stream);
-    for (auto& l : e->launches) {
-        SweepParams sp;
-        sp.P = P; sp.slots = l.d_slots.p; sp.nslots = (int)l.slots.size(); sp.nsweeps = nsweeps;
-        sp.smem_per_warp = l.smem_per_warp; sp.nbcap = l.nbcap;
-        if (l.bins) {
-            const int G = l.walkers_per_warp;
-            const int warps = (sp.nslots + G - 1) / G;
-            const int blocks = (warps + l.wpb - 1) / l.wpb;
-            const size_t smem = (size_t)l.wpb * G * l.smem_per_warp;
-            if (G == 1) launch_bins<1>(l.chunk, blocks, 32 * l.wpb, smem, e->stream, sp);
-            else if (G == 2) launch_bins<2>(l.chunk, blocks, 32 * l.wpb, smem, e->stream, sp);
-            else launch_bins<4>(l.chunk, blocks, 32 * l.wpb, smem, e->stream, sp);
-            CUDA_TRY(cudaGetLastError());
-            e->kernel_launches++;
-            e->launches_total++;
-            continue;
-        }
+    SweepParams sp;
+    sp.P = P; sp.slots = l.d_slots.p; sp.nslots = (int)l.slots.size(); sp.nsweeps = nsweeps;
+    sp.smem_per_warp = l.smem_per_warp; sp.nbcap = l.nbcap;
+    if (l.bins) {
+        const int G = l.walkers_per_warp;
+        const int warps = (sp.nslots + G - 1) / G;
+        const int blocks = (warps + l.wpb - 1) / l.wpb;
+        const size_t smem = (size_t)l.wpb * G * l.smem_per_warp;
+        if (G == 1) launch_bins<1>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp);
+        else if (G == 2) launch_bins<2>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp);
+        else launch_bins<4>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp);
+    } else {
         const int blocks = (sp.nslots + l.wpb - 1) / l.wpb;
         const size_t smem = (size_t)l.wpb * l.smem_per_warp;
         if (l.model == REWL_MODEL_ISING2D) {
-            if (replay) k_sweep_ising<true, 2><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
-            else if (e->sweep_variant == 2) k_sweep_ising<false, 2><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
-            else k_sweep_ising<false, 3><<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+            if (replay) k_sweep_ising<true, 2><<<blocks, 32 * l.wpb, smem, stream>>>(sp);
+            else if (e->sweep_variant == 2) k_sweep_ising<false, 2><<<blocks, 32 * l.wpb, smem, stream>>>(sp);
+            else k_sweep_ising<false, 3><<<blocks, 32 * l.wpb, smem, stream>>>(sp);
         } else {
             const SweepKernel fn = at_kernel(replay, e->desc.observables != 0);
             if (l.carveout >= 0) CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, l.carveout));
-            fn<<<blocks, 32 * l.wpb, smem, e->stream>>>(sp);
+            fn<<<blocks, 32 * l.wpb, smem, stream>>>(sp);
         }
-        CUDA_TRY(cudaGetLastError());
-        e->kernel_launches++;
-        e->launches_total++;
     }
-    cudaEventRecord(next_event(e), e->stream);
+    CUDA_TRY(cudaGetLastError());
+    e->kernel_launches++;
+    e->launches_total++;
+    return REWL_OK;
+}
+
+int launch_sweeps(rewl_engine* e, int nsweeps)
+{
+    const DevPtrs P = e->ptrs();
+    CUDA_TRY(cudaEventRecord(next_event(e), e->stream));
+    // several launch groups (models, lattice sizes, kernel shapes) run concurrently, each on
+    // its own stream forked from and joined back into the engine stream; they touch disjoint
+    // walkers
+    const bool fork = e->gstreams.size() == e->launches.size() && e->launches.size() > 1;
+    if (fork) CUDA_TRY(cudaEventRecord(e->fork_ev, e->stream));
+    for (size_t gi = 0; gi < e->launches.size(); ++gi) {
+        const cudaStream_t stream = fork ? e->gstreams[gi] : e->stream;
+        if (fork) CUDA_TRY(cudaStreamWaitEvent(stream, e->fork_ev, 0));
+        if (int rc = launch_group(e, e->launches[gi], stream, nsweeps, P)) return rc;
+        if (fork) {
+            CUDA_TRY(cudaEventRecord(e->join_ev[gi], stream));
+            CUDA_TRY(cudaStreamWaitEvent(e->stream, e->join_ev[gi], 0));
+        }
+    }
+    CUDA_TRY(cudaEventRecord(next_event(e), e->stream));
     e->sweeps_total += nsweeps;
     e->sweeps_since_check += nsweeps;
     e->flips_total += (int64_t)nsweeps * e->flips_per_sweep;
@@ -2161,13 +2258,13 @@ int launch_sweeps(rewl_engine* e, int nsweeps)
 
 int launch_exchange(rewl_engine* e)
 {
-    const int dir = e->direction;
-    const int npairs = (int)e->pairs_dir[dir].size() / 2;
-    if (npairs > 0) {
-        k_exchange<<<(npairs + 127) / 128, 128, 0, e->stream>>>(e->ptrs(), e->pairs[dir].p, npairs, e->exch_round);
-        CUDA_TRY(cudaGetLastError());
-        e->launches_total++;
-    }
+    // the kernel reads the round (and from its parity the direction) on the device and
+    // advances it; the host keeps a mirror for snapshots
+    const int n0 = (int)e->pairs_dir[0].size() / 2, n1 = (int)e->pairs_dir[1].size() / 2;
+    const int blocks = std::max(1, (std::max(n0, n1) + 127) / 128);
+    k_exchange<<<blocks, 128, 0, e->stream>>>(e->ptrs(), e->pairs[0].p, n0, e->pairs[1].p, n1);
+    CUDA_TRY(cudaGetLastError());
+    e->launches_total++;
     e->direction ^= 1;
     e->exch_round++;
     return REWL_OK;
@@ -2473,13 +2570,10 @@ int rewl_exchange(rewl_engine* e)
     return check_device_error(e);
 }
 
-int rewl_check_flat(rewl_engine* e, int32_t* num_flat)
+namespace {
+// After k_flat: the number of windows that went flat, and the device error word.
+int finish_check(rewl_engine* e, int32_t* num_flat)
 {
-    if (!e) return fail(REWL_EINVAL, "null engine");
-    cudaSetDevice(e->desc.device);
-    CUDA_TRY(cudaMemsetAsync(e->counters.p + 1, 0, 4, e->stream));
-    int rc = launch_flat(e);
-    if (rc) return rc;
     int32_t h[2];
     CUDA_TRY(cudaMemcpyAsync(h, e->counters.p, sizeof h, cudaMemcpyDeviceToHost, e->stream));
     CUDA_TRY(cudaStreamSynchronize(e->stream));
@@ -2487,6 +2581,74 @@ int rewl_check_flat(rewl_engine* e, int32_t* num_flat)
     e->cycles++;
     if (num_flat) *num_flat = h[1];
     return check_device_error(e);
+}
+
+// Capture one check interval (rounds x (sweeps + exchange), then the flatness step) as a CUDA
+// graph.  Nothing runs during capture, so the host counters the launches advance are put back
+// and applied per replay instead.
+int capture_cycle(rewl_engine* e)
+{
+    const int se = e->desc.sweeps_per_exchange, rounds = e->desc.sweeps_per_check / se;
+    const int64_t s0 = e->sweeps_total, f0 = e->flips_total, l0 = e->launches_total, k0 = e->kernel_launches;
+    const uint64_t r0 = e->exch_round;
+    const int d0 = e->direction;
+    const size_t ev0 = e->ev_used;
+    e->drop_graph();
+    CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeRelaxed));
+    e->capturing = true;
+    int rc = REWL_OK;
+    for (int r = 0; r < rounds && rc == REWL_OK; ++r) {
+        rc = launch_sweeps(e, se);
+        if (rc == REWL_OK) rc = launch_exchange(e);
+    }
+    if (rc == REWL_OK && cudaMemsetAsync(e->counters.p + 1, 0, 4, e->stream) != cudaSuccess)
+        rc = fail(REWL_EDEVICE, "memset during capture failed");
+    if (rc == REWL_OK) rc = launch_flat(e);
+    e->capturing = false;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(e->stream, &graph);
+    if (rc == REWL_OK && ce != cudaSuccess) rc = fail(REWL_EDEVICE, "stream capture: %s", cudaGetErrorString(ce));
+    if (rc == REWL_OK && cudaGraphInstantiate(&e->cycle_exec, graph, 0) != cudaSuccess) {
+        e->cycle_exec = nullptr;
+        rc = fail(REWL_EDEVICE, "graph instantiation failed");
+    }
+    if (graph) cudaGraphDestroy(graph);
+    e->g_sweeps = e->sweeps_total - s0; e->g_flips = e->flips_total - f0;
+    e->g_launches = e->launches_total - l0; e->g_kernel_launches = e->kernel_launches - k0; e->g_rounds = rounds;
+    e->sweeps_total = s0; e->flips_total = f0; e->launches_total = l0; e->kernel_launches = k0;
+    e->exch_round = r0; e->direction = d0; e->sweeps_since_check = 0; e->ev_used = ev0;
+    if (rc) e->drop_graph();
+    return rc;
+}
+
+// One check interval by replaying the captured graph.
+int replay_cycle(rewl_engine* e, int32_t* num_flat)
+{
+    if (!e->cycle_exec)
+        if (int rc = capture_cycle(e)) return rc;
+    CUDA_TRY(cudaGraphLaunch(e->cycle_exec, e->stream));
+    e->sweeps_total += e->g_sweeps; e->flips_total += e->g_flips;
+    e->launches_total += e->g_launches; e->kernel_launches += e->g_kernel_launches;
+    e->exch_round += (uint64_t)e->g_rounds;
+    e->direction ^= (int)(e->g_rounds & 1);
+    int rc = finish_check(e, num_flat);     // synchronises the stream
+    for (size_t k = 0; k + 1 < e->g_events.size(); k += 2) {
+        float t = 0;
+        CUDA_TRY(cudaEventElapsedTime(&t, e->g_events[k], e->g_events[k + 1]));
+        e->graph_sweep_ms += t;
+    }
+    return rc;
+}
+} // namespace
+
+int rewl_check_flat(rewl_engine* e, int32_t* num_flat)
+{
+    if (!e) return fail(REWL_EINVAL, "null engine");
+    cudaSetDevice(e->desc.device);
+    CUDA_TRY(cudaMemsetAsync(e->counters.p + 1, 0, 4, e->stream));
+    int rc = launch_flat(e);
+    if (rc) return rc;
+    return finish_check(e, num_flat);
 }
 
 int rewl_reset_histograms(rewl_engine* e, int32_t ii, int32_t w, int32_t reduce)
@@ -2533,13 +2695,21 @@ int rewl_run_cycles(rewl_engine* e, int64_t ncycles, int64_t timeout_ms, rewl_st
     const auto t0 = std::chrono::steady_clock::now();
     const int se = e->desc.sweeps_per_exchange, rounds = e->desc.sweeps_per_check / se;
     int rc = REWL_OK;
+    if (e->desc.autotune && !e->tuned && (rc = rewl_autotune(e, 0))) return rc;
     for (int64_t c = 0; c < ncycles; ++c) {
-        for (int r = 0; r < rounds; ++r) {
-            if ((rc = launch_sweeps(e, se))) return rc;
-            if ((rc = launch_exchange(e))) return rc;
-        }
         int32_t nflat = 0;
-        if ((rc = rewl_check_flat(e, &nflat))) return rc;
+        // a whole check interval replays as one graph unless sweeps were run by hand since the
+        // last check (the captured flatness step assumes exactly one interval of sweeps)
+        const bool graph = e->desc.graphs && e->desc.rng_mode != REWL_RNG_REPLAY && e->sweeps_since_check == 0;
+        if (graph) {
+            if ((rc = replay_cycle(e, &nflat))) return rc;
+        } else {
+            for (int r = 0; r < rounds; ++r) {
+                if ((rc = launch_sweeps(e, se))) return rc;
+                if ((rc = launch_exchange(e))) return rc;
+            }
+            if ((rc = rewl_check_flat(e, &nflat))) return rc;
+        }
         rewl_status s;
         if ((rc = rewl_get_status(e, &s))) return rc;
         if (st) *st = s;
@@ -2937,10 +3107,11 @@ int rewl_sweep_kernel_time(rewl_engine* e, double* ms, int64_t* launches)
         CUDA_TRY(cudaEventElapsedTime(&t, e->ev_pool[k], e->ev_pool[k + 1]));
         total += t;
     }
-    if (ms) *ms = total;
+    if (ms) *ms = total + e->graph_sweep_ms;
     if (launches) *launches = e->kernel_launches;
     e->ev_used = 0;
     e->kernel_launches = 0;
+    e->graph_sweep_ms = 0;
     return REWL_OK;
 }
 
@@ -3005,9 +3176,95 @@ int rewl_restore(rewl_engine* e, const void* buffer, size_t bytes)
         if (p.bytes) CUDA_TRY(cudaMemcpyAsync(p.dev, src, p.bytes, cudaMemcpyHostToDevice, e->stream));
         src += (p.bytes + 15) & ~size_t(15);
     }
+    const unsigned long long xr[2] = {h.exch_round, 0};
+    CUDA_TRY(cudaMemcpyAsync(e->xround.p, xr, sizeof xr, cudaMemcpyHostToDevice, e->stream));
     CUDA_TRY(cudaStreamSynchronize(e->stream));
     e->exch_round = h.exch_round; e->sweeps_since_check = h.sweeps_since_check; e->sweeps_total = h.sweeps_total;
     e->cycles = h.cycles; e->flat_events = h.flat_events; e->flips_total = h.flips_total; e->direction = h.direction;
+    return REWL_OK;
+}
+
+// Autotuner: for every launch group with more than one admissible shape (walkers per warp 1, 2
+// or 4 for the bin-tracking kernel, warps per block 1, 2, 4 or 8, within what the descriptor
+// fixes), time sweeps of that group alone in each shape and keep the fastest.  The trials run
+// on the live state, which is saved before and restored after, so tuning leaves the simulation
+// exactly where it was; a walker's trajectory does not depend on the shape.
+int rewl_autotune(rewl_engine* e, int32_t sweeps)
+{
+    if (!e || sweeps < 0) return fail(REWL_EINVAL, "bad arguments");
+    cudaSetDevice(e->desc.device);
+    size_t bytes = 0;
+    if (int rc = rewl_snapshot_size(e, &bytes)) return rc;
+    std::vector<char> snap(bytes);
+    if (int rc = rewl_snapshot(e, snap.data(), bytes)) return rc;
+    const int64_t l0 = e->launches_total, k0 = e->kernel_launches;
+    cudaEvent_t a = nullptr, b = nullptr;
+    int rc = REWL_OK;
+    auto ck = [&](cudaError_t ce) {
+        if (ce != cudaSuccess && rc == REWL_OK) rc = fail(REWL_EDEVICE, "autotune: %s", cudaGetErrorString(ce));
+        return rc == REWL_OK;
+    };
+    ck(cudaEventCreate(&a));
+    ck(cudaEventCreate(&b));
+    const DevPtrs P = e->ptrs();
+    for (auto& l : e->launches) {
+        if (rc) break;
+        int64_t dof = 0;
+        for (int s : l.slots) dof += e->inst[e->h_slot_inst[s]].dev.ndof;
+        // about 2e7 attempted flips of the group per trial, at least one sweep
+        const int ts = sweeps > 0 ? sweeps
+                                  : (int)std::max<int64_t>(1, std::min<int64_t>(e->desc.sweeps_per_exchange,
+                                                                                 20000000 / std::max<int64_t>(1, dof)));
+        std::vector<std::pair<int, int>> cand;
+        for (int G : {1, 2, 4}) {
+            if ((!l.bins && G > 1) || (l.bins && G > (int)l.slots.size())) continue;
+            if (e->desc.walkers_per_warp && l.bins && G != e->desc.walkers_per_warp) continue;
+            for (int W : {1, 2, 4, 8}) {
+                if (e->desc.warps_per_block && W != e->desc.warps_per_block) continue;
+                if (shape_fits(l, G, W)) cand.push_back({G, W});
+            }
+        }
+        if (cand.size() < 2) continue;
+        float best = FLT_MAX;
+        std::pair<int, int> pick{l.walkers_per_warp, l.wpb};
+        for (const auto& c : cand) {
+            l.walkers_per_warp = c.first;
+            l.wpb = c.second;
+            if ((rc = at_carveout(e, l))) break;
+            if ((rc = launch_group(e, l, e->stream, ts, P))) break;         // warm-up
+            if (!ck(cudaEventRecord(a, e->stream))) break;
+            if ((rc = launch_group(e, l, e->stream, ts, P))) break;
+            if (!ck(cudaEventRecord(b, e->stream)) || !ck(cudaEventSynchronize(b))) break;
+            float ms = 0;
+            if (!ck(cudaEventElapsedTime(&ms, a, b))) break;
+            if (ms < best) { best = ms; pick = c; }
+        }
+        l.walkers_per_warp = pick.first;
+        l.wpb = pick.second;
+        if (int r2 = at_carveout(e, l)) if (rc == REWL_OK) rc = r2;
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (rc == REWL_OK) rc = check_device_error(e);
+    const int rr = rewl_restore(e, snap.data(), bytes);
+    e->launches_total = l0;
+    e->kernel_launches = k0;
+    e->drop_graph();
+    e->tuned = true;
+    return rc ? rc : rr;
+}
+
+int rewl_launch_shapes(rewl_engine* e, int32_t* shapes, int32_t* count)
+{
+    if (!e || !count) return fail(REWL_EINVAL, "bad arguments");
+    const int n = (int)e->launches.size();
+    if (shapes && *count >= n)
+        for (int i = 0; i < n; ++i) {
+            const Launch& l = e->launches[i];
+            shapes[4 * i] = l.model; shapes[4 * i + 1] = l.bins ? 1 : 0;
+            shapes[4 * i + 2] = l.bins ? l.walkers_per_warp : 1; shapes[4 * i + 3] = l.wpb;
+        }
+    *count = n;
     return REWL_OK;
 }
 

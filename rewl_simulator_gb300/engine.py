@@ -54,7 +54,8 @@ class _BatchDesc(C.Structure):
                 ("lnf_initial", C.c_double), ("lnf_final", C.c_double), ("mask_mode", C.c_int32),
                 ("one_over_t", C.c_int32), ("reduce_logdos", C.c_int32), ("rng_mode", C.c_int32),
                 ("device", C.c_int32), ("warps_per_block", C.c_int32), ("walkers_per_warp", C.c_int32),
-                ("observables", C.c_int32), ("instances", C.c_void_p)]
+                ("observables", C.c_int32), ("graphs", C.c_int32), ("autotune", C.c_int32),
+                ("instances", C.c_void_p)]
 
 
 class _Status(C.Structure):
@@ -108,6 +109,8 @@ class Batch:
     warps_per_block: int = 0
     walkers_per_warp: int = 0
     observables: int = 0            # 1: per-bin moments; 2: also the G(q_min) correlators
+    graphs: int = 0                 # 1: replay each check interval as one captured CUDA graph
+    autotune: int = 0               # 1: time the launch groups' kernel shapes before the first cycle
 
 
 @dataclass
@@ -163,7 +166,7 @@ class Engine:
         b.num_instances = n
         for name in ("sweeps_per_exchange", "sweeps_per_check", "flatness_mode", "flatness_param", "lnf_initial",
                      "lnf_final", "mask_mode", "one_over_t", "reduce_logdos", "rng_mode", "device",
-                     "warps_per_block", "walkers_per_warp", "observables"):
+                     "warps_per_block", "walkers_per_warp", "observables", "graphs", "autotune"):
             setattr(b, name, getattr(batch, name))
         b.instances = C.cast(self._inst, C.c_void_p)
         self._desc = b
@@ -263,6 +266,18 @@ class Engine:
     def simulate(self, max_cycles: int = 1 << 40, timeout_ms: int = 0) -> Status:
         """Run until every window is done (REWL_simulation::simulate)."""
         return self.run_cycles(max_cycles, timeout_ms)
+
+    def autotune(self, sweeps: int = 0) -> None:
+        """Time each launch group's kernel shapes and keep the fastest (state unchanged)."""
+        self._check(self.lib.rewl_autotune(self.h, sweeps))
+
+    def launch_shapes(self) -> np.ndarray:
+        """Rows of [model, bin-tracking kernel, walkers per warp, warps per block] per launch group."""
+        n = C.c_int32(0)
+        self._check(self.lib.rewl_launch_shapes(self.h, None, C.byref(n)))
+        out = np.zeros((n.value, 4), dtype=np.int32)
+        self._check(self.lib.rewl_launch_shapes(self.h, _p(out), C.byref(n)))
+        return out
 
     def status(self) -> Status:
         st = _Status()

@@ -22,7 +22,11 @@ INSTANCES = [
 
 
 @pytest.mark.gpu
-def test_mixed_batch_instances_match_their_oracles(engine_lib, oracle_lib):
+@pytest.mark.parametrize("graphs,autotune", [(0, 0), (1, 0), (1, 1)], ids=["eager", "graphs", "graphs_autotuned"])
+def test_mixed_batch_instances_match_their_oracles(engine_lib, oracle_lib, graphs, autotune):
+    """The launch groups (two bin-tracking shapes, the general Ising kernel, Ashkin-Teller) run
+    concurrently on their own streams; with graphs each check interval replays as one captured
+    graph; the autotuner times the groups' shapes first.  None of it may change a trajectory."""
     rg, po = engine_lib, oracle_lib
     inss, orcs = [], []
     for name, model, L, K, sig, emin, emax, bw, nwin, R, seed in INSTANCES:
@@ -38,7 +42,7 @@ def test_mixed_batch_instances_match_their_oracles(engine_lib, oracle_lib):
                         semantics=po.SEM_ENGINE, seed=seed)
         orcs.append(po.Oracle(cfg, fields=fields))
     b = rg.Batch(instances=inss, sweeps_per_exchange=SE, sweeps_per_check=SC, flatness_param=0.8,
-                 lnf_initial=1.0, lnf_final=LNF_FINAL, mask_mode=rg.MASK_VISITED)
+                 lnf_initial=1.0, lnf_final=LNF_FINAL, mask_mode=rg.MASK_VISITED, graphs=graphs, autotune=autotune)
     eng = rg.Engine(b)
     try:
         def compare(tag):
@@ -71,3 +75,31 @@ def test_mixed_batch_instances_match_their_oracles(engine_lib, oracle_lib):
         eng.close()
         for o in orcs:
             o.close()
+
+
+@pytest.mark.gpu
+def test_autotune_leaves_the_state_unchanged(engine_lib):
+    """rewl_autotune runs trial sweeps on the live state and restores it: every walker's tables,
+    configuration and the engine's counters are as before, and the shapes it keeps are admissible."""
+    rg = engine_lib
+    inss = [rg.Instance(model=0, L=16, energy_min=-512.0, energy_max=516.0, bin_width=4.0, num_windows=4,
+                        replicas_per_window=4, seed=3),
+            rg.Instance(model=0, L=8, energy_min=-128.0, energy_max=132.0, bin_width=4.0, num_windows=3,
+                        replicas_per_window=2, seed=4)]
+    b = rg.Batch(instances=inss, sweeps_per_exchange=20, sweeps_per_check=40, lnf_final=1e-6)
+    with rg.Engine(b) as eng:
+        eng.run_cycles(2)
+        before = [eng.export_walker(s) for s in range(eng.num_walkers)]
+        st0 = eng.status()
+        eng.autotune(sweeps=5)
+        after = [eng.export_walker(s) for s in range(eng.num_walkers)]
+        st1 = eng.status()
+        for x, y in zip(before, after):
+            for k in x:
+                np.testing.assert_array_equal(x[k], y[k])
+        assert (st0.sweeps, st0.attempted_flips, st0.cycles, st0.exchanges_attempted) == \
+               (st1.sweeps, st1.attempted_flips, st1.cycles, st1.exchanges_attempted)
+        shapes = eng.launch_shapes()
+        assert len(shapes) == 2
+        for model, bins, g, wpb in shapes:
+            assert g in (1, 2, 4) and wpb in (1, 2, 4, 8)
