@@ -2120,6 +2120,7 @@ int plan_launches(rewl_engine* e)
                 const int warps = (n + G - 1) / G;
                 wpb = warps <= nsm * 2 ? 1 : warps <= nsm * 8 ? 2 : 4;
             }
+            wpb = std::min(wpb, 4);                                // the kernel's launch bounds: 128 threads
             while (wpb > 1 && (size_t)wpb * G * l.smem_per_warp > 200 * 1024) wpb >>= 1;
             l.wpb = wpb;
         } else if (l.model == REWL_MODEL_ISING2D) {
@@ -2231,10 +2232,18 @@ int launch_group(rewl_engine* e, Launch& l, cudaStream_t stream, int nsweeps, co
     return REWL_OK;
 }
 
+// A timing event on the engine stream; inside a stream capture it must become an event node of
+// the graph (a plain record there only marks a dependency).
+cudaError_t record_timing(rewl_engine* e)
+{
+    cudaEvent_t ev = next_event(e);
+    return e->capturing ? cudaEventRecordWithFlags(ev, e->stream, cudaEventRecordExternal) : cudaEventRecord(ev, e->stream);
+}
+
 int launch_sweeps(rewl_engine* e, int nsweeps)
 {
     const DevPtrs P = e->ptrs();
-    CUDA_TRY(cudaEventRecord(next_event(e), e->stream));
+    CUDA_TRY(record_timing(e));
     // several launch groups (models, lattice sizes, kernel shapes) run concurrently, each on
     // its own stream forked from and joined back into the engine stream; they touch disjoint
     // walkers
@@ -2249,7 +2258,7 @@ int launch_sweeps(rewl_engine* e, int nsweeps)
             CUDA_TRY(cudaStreamWaitEvent(e->stream, e->join_ev[gi], 0));
         }
     }
-    CUDA_TRY(cudaEventRecord(next_event(e), e->stream));
+    CUDA_TRY(record_timing(e));
     e->sweeps_total += nsweeps;
     e->sweeps_since_check += nsweeps;
     e->flips_total += (int64_t)nsweeps * e->flips_per_sweep;
@@ -2633,9 +2642,9 @@ int replay_cycle(rewl_engine* e, int32_t* num_flat)
     e->direction ^= (int)(e->g_rounds & 1);
     int rc = finish_check(e, num_flat);     // synchronises the stream
     for (size_t k = 0; k + 1 < e->g_events.size(); k += 2) {
-        float t = 0;
-        CUDA_TRY(cudaEventElapsedTime(&t, e->g_events[k], e->g_events[k + 1]));
-        e->graph_sweep_ms += t;
+        float t = 0;                        // timing only: a failed read leaves it out
+        if (cudaEventElapsedTime(&t, e->g_events[k], e->g_events[k + 1]) == cudaSuccess) e->graph_sweep_ms += t;
+        else (void)cudaGetLastError();
     }
     return rc;
 }
@@ -3216,11 +3225,14 @@ int rewl_autotune(rewl_engine* e, int32_t sweeps)
                                   : (int)std::max<int64_t>(1, std::min<int64_t>(e->desc.sweeps_per_exchange,
                                                                                  20000000 / std::max<int64_t>(1, dof)));
         std::vector<std::pair<int, int>> cand;
-        for (int G : {1, 2, 4}) {
+        // the bin-tracking kernel takes at most 4 warps per block (its launch bounds); 4 walkers
+        // per warp is left to the planner's rule for very large batches
+        for (int G : {1, 2}) {
             if ((!l.bins && G > 1) || (l.bins && G > (int)l.slots.size())) continue;
             if (e->desc.walkers_per_warp && l.bins && G != e->desc.walkers_per_warp) continue;
             for (int W : {1, 2, 4, 8}) {
-                if (e->desc.warps_per_block && W != e->desc.warps_per_block) continue;
+                if (l.bins && W > 4) continue;
+                if (e->desc.warps_per_block && W != std::min(e->desc.warps_per_block, l.bins ? 4 : 8)) continue;
                 if (shape_fits(l, G, W)) cand.push_back({G, W});
             }
         }
