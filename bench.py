@@ -60,6 +60,33 @@ WORKLOADS = {
                flatness="min >= 0.8 mean over visited bins", realizations=64,
                bytes_per_flip=51, kernel="k_sweep_at", profile="sweep_at_L32_64real_rewl.md"),
 }
+
+
+def _mixed_components():
+    """The uneven batch: 2D Ising at L = 16, 24, 32, 48 (16 windows x 4 walkers each) and 2D
+    Ashkin-Teller at L = 24 with K = 0.25, 0.5, 0.75, Baxter fields h ~ N(0, 0.3^2), 32
+    realisations each (8 windows x 4 walkers, bins of 0.05)."""
+    comps = []
+    for L in (16, 24, 32, 48):
+        N = L * L
+        comps.append(dict(model="ising2d", L=L, energy_min=-2.0 * N, energy_max=2.0 * N + 4, bin_width=4.0,
+                          num_windows=16, replicas_per_window=4, window_overlap=0.75, realizations=1))
+    for K in (0.25, 0.5, 0.75):
+        N = 24 * 24
+        comps.append(dict(model="ashkin_teller2d", L=24, K=K, sigma_h=0.3, energy_min=-(2.0 + K) * 2 * N,
+                          energy_max=0.0, bin_width=0.05, num_windows=8, replicas_per_window=4, window_overlap=0.75,
+                          realizations=32))
+    return comps
+
+
+WORKLOADS["mixed"] = dict(
+    name="mixed_ising_L16_24_32_48_x16win_x4_at_L24_K0.25_0.5_0.75_x32real_x8win_x4_rewl", model="mixed",
+    components=_mixed_components(), sweeps_per_exchange=100, sweeps_per_check=200, lnf_initial=1.0,
+    lnf_final=1e-8, flatness="min >= 0.8 mean over visited bins", realizations=1,
+    kernel="k_sweep_at + k_sweep_ising_bins (launch groups on concurrent streams)", profile="",
+    graphs=1, autotune=1)
+for _c in WORKLOADS["mixed"]["components"]:
+    _c["bytes_per_flip"] = 46 if _c["model"] == "ising2d" else 51
 WORKLOAD = WORKLOADS["ising"]
 
 
@@ -79,7 +106,16 @@ def ndof(w) -> int:
 
 
 def flips_per_sweep(w) -> int:
+    if w["model"] == "mixed":
+        return sum(flips_per_sweep(c) for c in w["components"])
     return w["realizations"] * w["num_windows"] * w["replicas_per_window"] * ndof(w)
+
+
+def bytes_per_flip(w) -> float:
+    """Algorithmic bytes per attempted flip (46 Ising, 51 Ashkin-Teller), flip-weighted for a mix."""
+    if w["model"] == "mixed":
+        return sum(c["bytes_per_flip"] * flips_per_sweep(c) for c in w["components"]) / flips_per_sweep(w)
+    return w["bytes_per_flip"]
 
 
 def at_fields(w, k: int) -> np.ndarray:
@@ -102,6 +138,8 @@ def peaks():
 
 def traffic_per_launch():
     """dram bytes per sweep-kernel launch from the committed ncu summary, if any."""
+    if not WORKLOAD["profile"]:
+        return None
     p = ROOT / "profiles" / WORKLOAD["profile"]
     if not p.exists():
         return None
@@ -171,6 +209,21 @@ class ClockSampler:
 
 def make_batch(rg, seed: int, device: int):
     w = WORKLOAD
+    if w["model"] == "mixed":
+        inss = []
+        for ci, c in enumerate(w["components"]):
+            for k in range(c["realizations"]):
+                at = c["model"] != "ising2d"
+                inss.append(rg.Instance(model=rg.MODEL_ASHKIN_TELLER2D if at else rg.MODEL_ISING2D, L=c["L"],
+                                        K=c.get("K", 0.0), fields=at_fields(c, 1000 * ci + k) if at else None,
+                                        energy_min=c["energy_min"], energy_max=c["energy_max"],
+                                        bin_width=c["bin_width"], num_windows=c["num_windows"],
+                                        replicas_per_window=c["replicas_per_window"],
+                                        window_overlap=c["window_overlap"], seed=seed * 1000 + 100 * ci + k))
+        return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
+                        sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
+                        lnf_final=w["lnf_final"], device=device, mask_mode=rg.MASK_VISITED,
+                        graphs=w["graphs"], autotune=w["autotune"])
     if w["model"] == "ising2d":
         inss = [rg.Instance(model=rg.MODEL_ISING2D, L=w["L"], energy_min=w["energy_min"], energy_max=w["energy_max"],
                             bin_width=w["bin_width"], num_windows=w["num_windows"],
@@ -192,9 +245,31 @@ def make_batch(rg, seed: int, device: int):
 # --------------------------------------------------------------------------- CPU leg
 def cpu_port_rate(target_seconds: float, threads: int, steps: int | None = None, warmup: int = 0):
     """Flips/s of the oracle port (reference semantics) on `threads` host threads (one instance:
-    the port drives one instance at a time, so for a batch of realisations it times one of them)."""
+    the port drives one instance at a time, so for a batch of realisations it times one of them).
+    For the uneven batch, one instance of every component is timed and the rate is the batch's
+    flips over the time the CPU needs for all of them."""
+    if WORKLOAD["model"] == "mixed":
+        return _cpu_port_rate_mixed(target_seconds, threads, steps, warmup)
+    return _cpu_port_rate_one(WORKLOAD, target_seconds, threads, steps, warmup)
+
+
+def _cpu_port_rate_mixed(target_seconds, threads, steps, warmup):
+    comps = WORKLOAD["components"]
+    cpu_s, n_total, t_total, times = 0.0, 0, 0.0, []
+    for c in comps:
+        w = dict(c, sweeps_per_exchange=WORKLOAD["sweeps_per_exchange"], sweeps_per_check=WORKLOAD["sweeps_per_check"],
+                 lnf_initial=WORKLOAD["lnf_initial"], lnf_final=WORKLOAD["lnf_final"])
+        rate, n, total, ts = _cpu_port_rate_one(w, target_seconds / len(comps), threads,
+                                                None if steps is None else max(1, steps // len(comps)), 0)
+        cpu_s += flips_per_sweep(c) * WORKLOAD["sweeps_per_check"] / rate     # one check interval of component c
+        n_total += n
+        t_total += total
+        times += ts
+    return flips_per_sweep(WORKLOAD) * WORKLOAD["sweeps_per_check"] / cpu_s, n_total, t_total, times
+
+
+def _cpu_port_rate_one(w, target_seconds, threads, steps, warmup):
     from oracle import pyoracle as po
-    w = WORKLOAD
     at = w["model"] != "ising2d"
     cfg = po.Config(model=po.MODEL_AT if at else po.MODEL_ISING, L=w["L"], K=w.get("K", 0.0),
                     escale_bits=20 if at else 0, nwin=w["num_windows"], R=w["replicas_per_window"],
@@ -203,7 +278,8 @@ def cpu_port_rate(target_seconds: float, threads: int, steps: int | None = None,
                     lnf0=w["lnf_initial"], lnf_final=w["lnf_final"], semantics=po.SEM_REFERENCE, nthreads=threads,
                     mask_mode=po.MASK_VISITED if at else po.MASK_STATIC, seed=2024)
     orc = po.Oracle(cfg, fields=at_fields(w, 0) if at else None)
-    flips_per_sweep = w["num_windows"] * w["replicas_per_window"] * ndof(w)
+    w = dict(w, realizations=1)
+    fps = w["num_windows"] * w["replicas_per_window"] * ndof(w)
     for _ in range(warmup):
         orc.run_sweeps(w["sweeps_per_exchange"])
     times = []
@@ -221,7 +297,7 @@ def cpu_port_rate(target_seconds: float, threads: int, steps: int | None = None,
             break
     orc.close()
     total = sum(times)
-    rate = done_steps * w["sweeps_per_check"] * flips_per_sweep / total
+    rate = done_steps * w["sweeps_per_check"] * fps / total
     return rate, done_steps, total, times
 
 
@@ -239,8 +315,10 @@ def run_reference(args):
         "config": {"workload": WORKLOAD["name"], **{k: v for k, v in WORKLOAD.items() if k != "name"},
                    "step": step_text()},
         "cpu_baseline": {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} check intervals of one instance of the workload "
-                                   f"({w['num_windows'] * w['replicas_per_window']} walkers, {w['sweeps_per_check']} sweeps each)"},
+                         "sample": (f"{n} check intervals of one instance of each of the {len(w['components'])} components"
+                                    if w["model"] == "mixed" else
+                                    f"{n} check intervals of one instance of the workload "
+                                    f"({w['num_windows'] * w['replicas_per_window']} walkers, {w['sweeps_per_check']} sweeps each)")},
         "e2e": {"value": rate, "unit": "flips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -409,6 +487,7 @@ def run_gpu(args):
         step_ms = [a.elapsed_time(b) for a, b in evs]
         st1 = eng.status()
         kern_ms, kern_launches = eng.sweep_kernel_time()
+        groups = max(1, len(eng.launch_shapes()))
     total_ms = sum(step_ms)
     flips = st1.attempted_flips - st0.attempted_flips
     launches = st1.kernel_launches - st0.kernel_launches
@@ -449,9 +528,10 @@ def run_gpu(args):
         return 0
 
     peak, peak_kind = peaks()
-    avg_launch_ms = kern_ms / max(kern_launches, 1)
+    # one sweep phase = one launch per launch group, concurrent; its span is what the events time
+    avg_launch_ms = kern_ms / max(kern_launches / groups, 1)
     flips_per_launch = WORKLOAD["sweeps_per_exchange"] * flips_per_sweep(WORKLOAD)
-    achieved = WORKLOAD["bytes_per_flip"] * flips_per_launch / (avg_launch_ms * 1e-3) / 1e9
+    achieved = bytes_per_flip(WORKLOAD) * flips_per_launch / (avg_launch_ms * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "flips/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -461,7 +541,7 @@ def run_gpu(args):
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"instances x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic_per_launch(),
-                     "kernel": WORKLOAD["kernel"], "bytes_per_flip": WORKLOAD["bytes_per_flip"],
+                     "kernel": WORKLOAD["kernel"], "bytes_per_flip": bytes_per_flip(WORKLOAD),
                      "avg_launch_ms": avg_launch_ms, "flips_per_launch": flips_per_launch},
         "e2e": {"value": e2e_rate, "unit": "flips/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps},
@@ -471,8 +551,10 @@ def run_gpu(args):
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, n, total, _ = cpu_port_rate(args.cpu_seconds, threads)
-        line["cpu_baseline"] = {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
-                                "sample": f"{n} check intervals of the same workload ({total:.1f} s)"}
+        sample = (f"{n} check intervals of one instance of each of the {len(WORKLOAD['components'])} components "
+                  f"({total:.1f} s)" if WORKLOAD["model"] == "mixed"
+                  else f"{n} check intervals of the same workload ({total:.1f} s)")
+        line["cpu_baseline"] = {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port", "sample": sample}
     if args.tta and world == 1:
         line["time_to_accuracy"] = warm_start_tta(rg, device, args.tta_seconds,
                                                   line.get("cpu_baseline", {}).get("value"))
@@ -495,7 +577,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="ising",
-                    help="ising: the headline configuration (default); at: 2D Ashkin-Teller, 64 realisations")
+                    help="ising: the headline configuration (default); at: 2D Ashkin-Teller, 64 realisations; "
+                         "mixed: the uneven batch (Ising L = 16..48 and Ashkin-Teller L = 24, K = 0.25..0.75)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
