@@ -128,6 +128,25 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def rank_seed(rank: int) -> int:
+    """Each rank runs its own copy of the workload (weak scaling) with its own seed: the ranks'
+    instances are independent and exchange nothing."""
+    return 1000 + rank
+
+
+def reduce_over_ranks(times, counts, device: str = "cpu"):
+    """Job-wide figures from per-rank ones: the maximum over ranks of each time (the slowest rank
+    ends the job) and the sum of each count.  One all-reduce each over the default group (NCCL
+    tensors on the GPU, gloo on CPU)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x) for x in times], dtype=torch.float64, device=device)
+    c = torch.tensor([float(x) for x in counts], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return t.tolist(), c.tolist()
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -463,7 +482,7 @@ def run_gpu(args):
             import torch.distributed as dist
             dist.barrier()
 
-    batch = make_batch(rg, seed=1000 + rank, device=device)
+    batch = make_batch(rg, seed=rank_seed(rank), device=device)
     eng = rg.Engine(batch)
     stream = torch.cuda.ExternalStream(eng.stream_handle(), device=torch.device("cuda", device))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")
@@ -510,15 +529,8 @@ def run_gpu(args):
     eng.close()
 
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms, float(flips), e2e_s, float(e2e_steps * flips_per_step)], device=f"cuda:{device}",
-                         dtype=torch.float64)
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        tsum = t.clone()
-        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
-        total_ms, e2e_s = float(tmax[0]), float(tmax[2])
-        flips, e2e_flips = float(tsum[1]), float(tsum[3])
+        (total_ms, e2e_s), (flips, e2e_flips) = reduce_over_ranks([total_ms, e2e_s], [flips, e2e_steps * flips_per_step],
+                                                                  device=f"cuda:{device}")
         e2e_rate = e2e_flips / e2e_s
     value = flips / (total_ms * 1e-3)
     if rank != 0:
