@@ -2041,13 +2041,21 @@ bool bins_eligible(const InstDev& I, const rewl_batch_desc& D)
     return true;
 }
 
+// Streaming multiprocessors of the engine's device (152 on a GB300).
+int sm_count(const rewl_engine* e)
+{
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, e->desc.device) != cudaSuccess || n < 1) n = 152;
+    return n;
+}
+
 // The logDoS tables of the Ashkin-Teller kernel live in global memory and are read through L1,
 // so its shared-memory carveout is the smallest that still holds the blocks resident on an SM
 // (the driver's default leaves L1 far less).
 int at_carveout(rewl_engine* e, Launch& l)
 {
     if (l.bins || l.model == REWL_MODEL_ISING2D) return REWL_OK;
-    const int nsm = 152;
+    const int nsm = sm_count(e);
     const SweepKernel fn = at_kernel(e->desc.rng_mode == REWL_RNG_REPLAY, e->desc.observables != 0);
     const int threads = 32 * l.wpb;
     const size_t smem = (size_t)l.wpb * l.smem_per_warp;
@@ -2071,7 +2079,7 @@ bool shape_fits(const Launch& l, int G, int wpb)
 
 int plan_launches(rewl_engine* e)
 {
-    const int nsm = 152;
+    const int nsm = sm_count(e);
     // group walkers by (model, bin-tracking kernel, chunk, sites) so each launch has one
     // kernel shape and the walkers sharing a warp run the same number of chunks
     struct Key { int model, bins, chunk, sites; };
