@@ -258,7 +258,7 @@ def make_batch(rg, seed: int, device: int):
         mask = rg.MASK_VISITED
     return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
                     sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
-                    lnf_final=w["lnf_final"], device=device, mask_mode=mask)
+                    lnf_final=w["lnf_final"], device=device, mask_mode=mask, observables=w.get("observables", 0))
 
 
 # --------------------------------------------------------------------------- CPU leg
@@ -588,6 +588,9 @@ def main():
     ap.add_argument("--tta-seconds", type=float, default=90.0, help="wall-time limit of each time-to-accuracy arm")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--observables", type=int, choices=[0, 1, 2], default=0,
+                    help="1: keep the per-bin observables during the sweeps; 2: also the G(q_min) correlators "
+                         "(the reference's default build)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="ising",
                     help="ising: the headline configuration (default); at: 2D Ashkin-Teller, 64 realisations; "
                          "mixed: the uneven batch (Ising L = 16..48 and Ashkin-Teller L = 24, K = 0.25..0.75)")
@@ -595,6 +598,9 @@ def main():
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     select_workload(args.workload)
+    if args.observables:
+        WORKLOADS[args.workload]["observables"] = args.observables
+        select_workload(args.workload)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

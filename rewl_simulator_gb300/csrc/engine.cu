@@ -386,11 +386,11 @@ __device__ double full_corr(const int8_t* a, const int8_t* b, const double* q, i
     return 0.5 * ((rx * rx + ix * ix) + (ry * ry + iy * iy));
 }
 
-// Row and column sums of a plane (value(i) for site i) into rs, cs, by the warp's lanes.
+// Row and column sums of a plane (value(i) for site i) into rs, cs, by `stride` lanes.
 template <class V>
-__device__ void plane_sums(int* rs, int* cs, int L, int lane, V value)
+__device__ void plane_sums(int* rs, int* cs, int L, int lane, V value, int stride = 32)
 {
-    for (int t = lane; t < L; t += 32) {
+    for (int t = lane; t < L; t += stride) {
         int r = 0, c = 0;
         for (int u = 0; u < L; ++u) { r += value(t * L + u); c += value(u * L + t); }
         rs[t] = r;
@@ -751,6 +751,8 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     long long* Tb = reinterpret_cast<long long*>(base + gs_bytes + ((N + 15) & ~15));   // 2 x 4C thresholds
     int2* Db = reinterpret_cast<int2*>(Tb + 8 * C);                                   // 2 x C offset pairs
     int* seqb = reinterpret_cast<int*>(Db + 2 * C);                                   // C bins (observables)
+    int* rsum = seqb + C;                                                             // correlators: row sums,
+    int* csum = rsum + L;                                                             // column sums
     // table positions are byte offsets from the start of shared memory, so that the
     // accesses need no address arithmetic
     char* const sm = reinterpret_cast<char*>(smem);
@@ -763,6 +765,11 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     for (int k = q; k < nb; k += P) gs[k] = gg[k];
     for (int k = q; k < kGuard; k += P) { gs[-1 - k] = kGuardValue; gs[nb + k] = kGuardValue; }
     __syncwarp();
+    const bool corr = OBS && P_.corr;
+    if (corr) {
+        plane_sums(rsum, csum, L, q, [&](int i) { return (int)lat[i]; }, P);
+        __syncwarp();
+    }
 
     const int J = (int)I.J_u;
     const int sh = I.bin_shift;                        // energy change -> bin change (x8: byte offset)
@@ -963,6 +970,40 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                         obs_add_ising(ob + (size_t)((seqb[jj] - gsoff) >> 3) * P_.obs_stride, M + chunk_dm(acc, plus, jj),
                                       1.0 / (double)N);
                 }
+            }
+            if (corr) {
+                // G(q_min) at the steps whose bin count before the visit is a multiple of 1000:
+                // the count is the launch-start visits plus the change of g over ln f, less this
+                // chunk's visits to the bin from that step on.  The lattice already holds the
+                // chunk's flips: an accepted site's value before the chunk is minus its value now.
+                if (valid) {
+                    const double invN = 1.0 / (double)N;
+                    double* ob = P_.obs + (size_t)P_.slot_tab[s] * P_.obs_stride;
+#pragma unroll
+                    for (int k = 0; k < SPL; ++k) {
+                        const int jj = q + k * P;
+                        if (jj >= C) continue;
+                        const int off = seqb[jj], b = (off - gsoff) >> 3;
+                        int later = 0;
+                        for (int j2 = jj; j2 < C; ++j2) later += seqb[j2] == off;
+                        const unsigned long long after =
+                            P_.visits[P_.slot_tab[s] + b] + (unsigned long long)((gs[b] - gg[b]) / lnf);
+                        if ((after - (unsigned long long)later) % kCountsPerTransform == 0) {
+                            const double Gq = plane_corr(rsum, csum, P_.qtab + I.qtab_off, L, y, chunk_dm(acc, plus, jj), x0,
+                                                         jj, acc, [&](int kk) { return -(int)lat[c0 + kk]; });
+                            atomicAdd(ob + (size_t)b * P_.obs_stride + 3, invN * invN * Gq);
+                        }
+                    }
+                }
+                __syncwarp();
+                // the chunk's flips into the row and column sums
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) {
+                    const int jj = q + k * P;
+                    if (valid && jj < C && ((acc >> jj) & 1u)) csum[x0 + jj] += 2 * (int)lat[c0 + jj];
+                }
+                if (valid && q == 0) rsum[y] += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus & full));
+                __syncwarp();
             }
             M += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus & full));
         }
@@ -2027,7 +2068,6 @@ int upload_all(rewl_engine* e)
 bool bins_eligible(const InstDev& I, const rewl_batch_desc& D)
 {
     if (I.model != REWL_MODEL_ISING2D || D.rng_mode != REWL_RNG_PHILOX) return false;
-    if (D.observables == 2) return false;   // the correlators are kept by the general kernel
     const int C = I.chunk;
     if (!(C == 32 || C == 24 || C == 16 || C == 8 || C == 4)) return false;
     const long long step = 4 * std::llabs(I.J_u);            // every energy change is a multiple of 4|J|
@@ -2120,7 +2160,8 @@ int plan_launches(rewl_engine* e)
             }
             l.walkers_per_warp = G;
             l.nbcap = (maxnb + 1) & ~1;
-            int raw = (((l.nbcap + 2 * kGuard) * 8 + 15) & ~15) + ((maxN + 15) & ~15) + 8 * l.chunk * 8 + 2 * l.chunk * 8 + l.chunk * 4;
+            int raw = (((l.nbcap + 2 * kGuard) * 8 + 15) & ~15) + ((maxN + 15) & ~15) + 8 * l.chunk * 8 + 2 * l.chunk * 8 + l.chunk * 4
+                      + (corr ? 8 * maxL : 0);
             l.smem_per_warp = ((raw + 127) & ~127) + 16;           // per walker; +16 skews the walkers' banks
             if ((size_t)l.smem_per_warp * G > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory", l.smem_per_warp);
             int wpb = e->desc.warps_per_block;

@@ -189,11 +189,14 @@ OBS_CASES = [
     ("ising_L16_bins_2perwarp", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 3, 2, 0.0, 0, 1),
     ("ising_L12_bw8_general", 0, 12, -288.0, 296.0, 8.0, 4, 2, 10, 20, 3, 3, 0, 0.0, 0, 1),
     ("at_L4_rf", 1, 4, -(2.5) * 2 * 16, 0.0, 0.05, 2, 2, 20, 40, 7, 3, 0, 0.5, 1, 1),
-    # with the G(q_min) correlators: general Ising kernel (chunk = row, and chunks within a row)
-    # and the Ashkin-Teller kernel; exchanges add transforms through the exchange touch
+    # with the G(q_min) correlators: the bin-tracking kernel (chunk = row, chunks within a row, two
+    # walkers per warp), the general Ising kernel (bin width 8) and the Ashkin-Teller kernel;
+    # exchanges add transforms through the exchange touch
     ("ising_L8_corr", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 4, 0, 0.0, 0, 2),
     ("ising_L16_corr", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 3, 0, 0.0, 0, 2),
     ("ising_L64_corr_chunks", 0, 64, -8192.0, -7000.0, 4.0, 2, 2, 4, 8, 29, 2, 0, 0.0, 0, 2),
+    ("ising_L16_corr_2perwarp", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 3, 2, 0.0, 0, 2),
+    ("ising_L12_bw8_corr_general", 0, 12, -288.0, 296.0, 8.0, 4, 2, 10, 20, 3, 3, 0, 0.0, 0, 2),
     ("at_L4_rf_corr", 1, 4, -(2.5) * 2 * 16, 0.0, 0.05, 2, 2, 20, 40, 7, 3, 0, 0.5, 1, 2),
     ("at_L8_rf_corr", 1, 8, -(2.5) * 2 * 64, -40.0, 0.05, 2, 2, 10, 20, 9, 3, 0, 0.5, 1, 2),
 ]
