@@ -752,7 +752,8 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     int2* Db = reinterpret_cast<int2*>(Tb + 8 * C);                                   // 2 x C offset pairs
     int* seqb = reinterpret_cast<int*>(Db + 2 * C);                                   // C bins (observables)
     int* rsum = seqb + C;                                                             // correlators: row sums,
-    int* csum = rsum + L;                                                             // column sums
+    int* csum = rsum + L;                                                             // column sums,
+    int* bcnt = csum + L;                                                             // bin counts mod 1000
     // table positions are byte offsets from the start of shared memory, so that the
     // accesses need no address arithmetic
     char* const sm = reinterpret_cast<char*>(smem);
@@ -768,6 +769,8 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     const bool corr = OBS && P_.corr;
     if (corr) {
         plane_sums(rsum, csum, L, q, [&](int i) { return (int)lat[i]; }, P);
+        const uint64_t* gv0 = P_.visits + P_.slot_tab[s];
+        for (int k = q; k < nb; k += P) bcnt[k] = (int)(gv0[k] % kCountsPerTransform);
         __syncwarp();
     }
 
@@ -973,9 +976,9 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             }
             if (corr) {
                 // G(q_min) at the steps whose bin count before the visit is a multiple of 1000:
-                // the count is the launch-start visits plus the change of g over ln f, less this
-                // chunk's visits to the bin from that step on.  The lattice already holds the
-                // chunk's flips: an accepted site's value before the chunk is minus its value now.
+                // bcnt holds every bin's count before this chunk (mod 1000), to which the chunk's
+                // earlier visits to the bin are added.  The lattice already holds the chunk's
+                // flips: an accepted site's value before the chunk is minus its value now.
                 if (valid) {
                     const double invN = 1.0 / (double)N;
                     double* ob = P_.obs + (size_t)P_.slot_tab[s] * P_.obs_stride;
@@ -984,11 +987,9 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                         const int jj = q + k * P;
                         if (jj >= C) continue;
                         const int off = seqb[jj], b = (off - gsoff) >> 3;
-                        int later = 0;
-                        for (int j2 = jj; j2 < C; ++j2) later += seqb[j2] == off;
-                        const unsigned long long after =
-                            P_.visits[P_.slot_tab[s] + b] + (unsigned long long)((gs[b] - gg[b]) / lnf);
-                        if ((after - (unsigned long long)later) % kCountsPerTransform == 0) {
+                        int earlier = 0;
+                        for (int j2 = 0; j2 < jj; ++j2) earlier += seqb[j2] == off;
+                        if ((bcnt[b] + earlier) % (int)kCountsPerTransform == 0) {
                             const double Gq = plane_corr(rsum, csum, P_.qtab + I.qtab_off, L, y, chunk_dm(acc, plus, jj), x0,
                                                          jj, acc, [&](int kk) { return -(int)lat[c0 + kk]; });
                             atomicAdd(ob + (size_t)b * P_.obs_stride + 3, invN * invN * Gq);
@@ -996,11 +997,12 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                     }
                 }
                 __syncwarp();
-                // the chunk's flips into the row and column sums
+                // the chunk's flips into the row and column sums, its visits into the counts
 #pragma unroll
                 for (int k = 0; k < SPL; ++k) {
                     const int jj = q + k * P;
                     if (valid && jj < C && ((acc >> jj) & 1u)) csum[x0 + jj] += 2 * (int)lat[c0 + jj];
+                    if (valid && jj < C) atomicAdd(&bcnt[(seqb[jj] - gsoff) >> 3], 1);
                 }
                 if (valid && q == 0) rsum[y] += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus & full));
                 __syncwarp();
@@ -2161,7 +2163,7 @@ int plan_launches(rewl_engine* e)
             l.walkers_per_warp = G;
             l.nbcap = (maxnb + 1) & ~1;
             int raw = (((l.nbcap + 2 * kGuard) * 8 + 15) & ~15) + ((maxN + 15) & ~15) + 8 * l.chunk * 8 + 2 * l.chunk * 8 + l.chunk * 4
-                      + (corr ? 8 * maxL : 0);
+                      + (corr ? 8 * maxL + 4 * l.nbcap : 0);
             l.smem_per_warp = ((raw + 127) & ~127) + 16;           // per walker; +16 skews the walkers' banks
             if ((size_t)l.smem_per_warp * G > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory", l.smem_per_warp);
             int wpb = e->desc.warps_per_block;
