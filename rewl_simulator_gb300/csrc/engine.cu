@@ -977,9 +977,19 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
             if (corr) {
                 // G(q_min) at the steps whose bin count before the visit is a multiple of 1000:
                 // bcnt holds every bin's count before this chunk (mod 1000), to which the chunk's
-                // earlier visits to the bin are added.  The lattice already holds the chunk's
-                // flips: an accepted site's value before the chunk is minus its value now.
+                // earlier visits to the bin are added.  The chunk's bins are read once into
+                // registers (broadcast loads) and compared there.  The lattice already holds the
+                // chunk's flips: an accepted site's value before the chunk is minus its value now.
+                int first[SPL], total[SPL];
+#pragma unroll
+                for (int k = 0; k < SPL; ++k) { first[k] = 0; total[k] = 0; }
                 if (valid) {
+                    int sq[C];
+#pragma unroll
+                    for (int j2 = 0; j2 < C; j2 += 4) {
+                        const int4 v = reinterpret_cast<const int4*>(seqb)[j2 >> 2];
+                        sq[j2] = v.x; sq[j2 + 1] = v.y; sq[j2 + 2] = v.z; sq[j2 + 3] = v.w;
+                    }
                     const double invN = 1.0 / (double)N;
                     double* ob = P_.obs + (size_t)P_.slot_tab[s] * P_.obs_stride;
 #pragma unroll
@@ -987,8 +997,15 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                         const int jj = q + k * P;
                         if (jj >= C) continue;
                         const int off = seqb[jj], b = (off - gsoff) >> 3;
-                        int earlier = 0;
-                        for (int j2 = 0; j2 < jj; ++j2) earlier += seqb[j2] == off;
+                        int earlier = 0, all = 0;
+#pragma unroll
+                        for (int j2 = 0; j2 < C; ++j2) {
+                            const int eq = sq[j2] == off ? 1 : 0;
+                            earlier += j2 < jj ? eq : 0;
+                            all += eq;
+                        }
+                        first[k] = earlier == 0;
+                        total[k] = all;
                         if ((bcnt[b] + earlier) % (int)kCountsPerTransform == 0) {
                             const double Gq = plane_corr(rsum, csum, P_.qtab + I.qtab_off, L, y, chunk_dm(acc, plus, jj), x0,
                                                          jj, acc, [&](int kk) { return -(int)lat[c0 + kk]; });
@@ -997,12 +1014,13 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                     }
                 }
                 __syncwarp();
-                // the chunk's flips into the row and column sums, its visits into the counts
+                // the chunk's flips into the row and column sums, its visits into the counts (by
+                // the first step at each bin)
 #pragma unroll
                 for (int k = 0; k < SPL; ++k) {
                     const int jj = q + k * P;
                     if (valid && jj < C && ((acc >> jj) & 1u)) csum[x0 + jj] += 2 * (int)lat[c0 + jj];
-                    if (valid && jj < C) atomicAdd(&bcnt[(seqb[jj] - gsoff) >> 3], 1);
+                    if (valid && jj < C && first[k]) bcnt[(seqb[jj] - gsoff) >> 3] += total[k];
                 }
                 if (valid && q == 0) rsum[y] += -2 * ((int)__popc(acc & plus) - (int)__popc(acc & ~plus & full));
                 __syncwarp();
