@@ -103,3 +103,43 @@ def test_autotune_leaves_the_state_unchanged(engine_lib):
         assert len(shapes) == 2
         for model, bins, g, wpb in shapes:
             assert g in (1, 2, 4) and wpb in (1, 2, 4, 8)
+
+
+@pytest.mark.gpu
+def test_graph_replay_with_manual_steps_and_restore(engine_lib):
+    """Graph replay interleaved with hand-run sweeps and exchanges (the next interval then runs
+    eagerly), a snapshot, more cycles, and a restore of the snapshot followed by the same cycles:
+    a graph engine and an eager engine end in identical states."""
+    rg = engine_lib
+    ins = [rg.Instance(model=0, L=8, energy_min=-128.0, energy_max=132.0, bin_width=4.0, num_windows=3,
+                       replicas_per_window=2, seed=21),
+           rg.Instance(model=1, L=4, K=0.5, energy_min=-80.0, energy_max=0.0, bin_width=0.05, num_windows=2,
+                       replicas_per_window=2, seed=22,
+                       fields=np.round(np.random.default_rng(22).normal(0, 0.5, 16) * 2**20) / 2**20)]
+
+    def run(graphs):
+        b = rg.Batch(instances=ins, sweeps_per_exchange=10, sweeps_per_check=30, lnf_final=1e-6,
+                     mask_mode=rg.MASK_VISITED, graphs=graphs)
+        with rg.Engine(b) as eng:
+            eng.run_cycles(2)
+            eng.wang_landau_walk(7)
+            eng.replica_exchange_update()
+            eng.run_cycles(2)
+            snap = eng.snapshot()
+            eng.run_cycles(3)
+            first = [eng.export_walker(s) for s in range(eng.num_walkers)]
+            eng.restore(snap)
+            eng.run_cycles(3)
+            again = [eng.export_walker(s) for s in range(eng.num_walkers)]
+            st = eng.status()
+        return first, again, st
+
+    g_first, g_again, g_st = run(1)
+    e_first, e_again, e_st = run(0)
+    for a, b, c, d in zip(g_first, e_first, g_again, e_again):
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k])     # graph == eager
+            np.testing.assert_array_equal(a[k], c[k])     # restore + the same cycles == first pass
+            np.testing.assert_array_equal(c[k], d[k])
+    assert (g_st.sweeps, g_st.exchanges_attempted, g_st.exchanges_accepted, g_st.flat_events) == \
+           (e_st.sweeps, e_st.exchanges_attempted, e_st.exchanges_accepted, e_st.flat_events)
