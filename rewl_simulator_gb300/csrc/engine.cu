@@ -40,6 +40,7 @@
 #include <fstream>
 #include <iomanip>
 #include <limits>
+#include <new>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -3273,7 +3274,12 @@ int rewl_autotune(rewl_engine* e, int32_t sweeps)
     cudaSetDevice(e->desc.device);
     size_t bytes = 0;
     if (int rc = rewl_snapshot_size(e, &bytes)) return rc;
-    std::vector<char> snap(bytes);
+    std::vector<char> snap;
+    try {
+        snap.resize(bytes);
+    } catch (const std::bad_alloc&) {
+        return fail(REWL_ENOMEM, "autotune: no host memory for the %zu-byte state copy", bytes);
+    }
     if (int rc = rewl_snapshot(e, snap.data(), bytes)) return rc;
     const int64_t l0 = e->launches_total, k0 = e->kernel_launches;
     cudaEvent_t a = nullptr, b = nullptr;
