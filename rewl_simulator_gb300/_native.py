@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 LIB = PKG / "librewl_gb300.so"
 SOURCES = [CSRC / "engine.cu", CSRC / "mlp.cu", CSRC / "thermo.cu"]
-DEPS = SOURCES + [CSRC / "rng.cuh", INCLUDE / "rewl.h"]
+DEPS = SOURCES + [CSRC / "rng.cuh", CSRC / "models.cuh", INCLUDE / "rewl.h"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

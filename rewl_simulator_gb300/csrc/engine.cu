@@ -47,6 +47,7 @@
 
 #include "../../include/rewl.h"
 #include "rng.cuh"
+#include "models.cuh"
 
 using namespace rewl;
 
@@ -141,55 +142,8 @@ struct DevPtrs {
 };
 
 // --------------------------------------------------------------------------
-// Energies in integer units
+// Energies in integer units: the model types of models.cuh
 // --------------------------------------------------------------------------
-__host__ __device__ inline int nb_up(int i, int L) { int x = i % L, y = i / L; return (y == 0 ? L - 1 : y - 1) * L + x; }
-__host__ __device__ inline int nb_left(int i, int L) { int x = i % L, y = i / L; return y * L + (x == 0 ? L - 1 : x - 1); }
-__host__ __device__ inline int nb_right(int i, int L) { int x = i % L, y = i / L; return y * L + (x == L - 1 ? 0 : x + 1); }
-__host__ __device__ inline int nb_down(int i, int L) { int x = i % L, y = i / L; return (y == L - 1 ? 0 : y + 1) * L + x; }
-
-// Ising: E = -J sum_<ij> s_i s_j, recomputed as sum_i -1/2 s_i J sum_nb s_nb
-// (ising2d_hamiltonian.hpp:191-210); integer arithmetic, so exact.
-__host__ __device__ inline void ising_recalc(const int8_t* s, int L, int64_t J, int64_t& E, int32_t& M)
-{
-    const int N = L * L;
-    int64_t twiceE = 0; int32_t m = 0;
-    for (int i = 0; i < N; ++i) {
-        const int sum = s[nb_up(i, L)] + s[nb_left(i, L)] + s[nb_right(i, L)] + s[nb_down(i, L)];
-        twiceE -= (int64_t)s[i] * J * sum;
-        m += s[i];
-    }
-    E = twiceE / 2; M = m;
-}
-
-// Energy change of flipping spin a_i of plane `a` (other plane b) for the
-// Ashkin-Teller model H = -sum[J(s s' + t t') + K s t s' t'] - sum h s t
-// (ashkin_teller2d_hamiltonian.hpp:169-191,224-250).
-__host__ __device__ inline int64_t at_dE(const int8_t* a, const int8_t* b, int i, int L, int64_t J, int64_t K, int64_t h)
-{
-    const int u = nb_up(i, L), l = nb_left(i, L), r = nb_right(i, L), d = nb_down(i, L);
-    const int sa = a[u] + a[l] + a[r] + a[d];
-    const int sab = a[u] * b[u] + a[l] * b[l] + a[r] * b[r] + a[d] * b[d];
-    return 2 * (int64_t)a[i] * (h * b[i] + J * sa + K * (int64_t)b[i] * sab);
-}
-
-__host__ __device__ inline void at_recalc(const int8_t* s, const int8_t* t, int L, int64_t J, int64_t K,
-                                          const int64_t* h, int64_t& E, int32_t* M)
-{
-    const int N = L * L;
-    int64_t twiceE = 0; int32_t sm = 0, tm = 0, bx = 0;
-    for (int i = 0; i < N; ++i) {
-        const int u = nb_up(i, L), l = nb_left(i, L), r = nb_right(i, L), d = nb_down(i, L);
-        const int ss = s[u] + s[l] + s[r] + s[d];
-        const int tt = t[u] + t[l] + t[r] + t[d];
-        const int st = s[u] * t[u] + s[l] * t[l] + s[r] * t[r] + s[d] * t[d];
-        twiceE -= (int64_t)s[i] * J * ss + (int64_t)t[i] * J * tt + (int64_t)s[i] * t[i] * K * st;
-        if (h) twiceE -= 2 * h[i] * s[i] * t[i];
-        sm += s[i]; tm += t[i]; bx += s[i] * t[i];
-    }
-    E = twiceE / 2; M[0] = sm; M[1] = tm; M[2] = bx;
-}
-
 __host__ __device__ inline int64_t global_bin(const InstDev& I, int64_t E)
 {
     return ((E - I.eglo_u) * I.bin_mul) >> I.bin_shift;
@@ -198,10 +152,16 @@ __host__ __device__ inline int64_t global_bin(const InstDev& I, int64_t E)
 // --------------------------------------------------------------------------
 // k_init: initial configuration and the deterministic walk into the window
 // --------------------------------------------------------------------------
+// REWL_Walker::adjust_state_to_range (src/REWL/rewl_walker.hpp:79-115): visit the sites in
+// typewriter order from `start`, flipping a spin whenever that moves the energy towards the
+// window, until the energy is inside it.  Ashkin-Teller alternates the flipped plane at the
+// end of every pass (change_state toggles at the last site).
+template <class Model>
 __device__ bool adjust_walk(const InstDev& I, const WinDev& W, int8_t* sp, int64_t& E, int32_t* M, int32_t& flavour,
                             const int64_t* h, uint32_t start, int64_t max_steps)
 {
     const int L = I.L, N = I.N;
+    const Couplings cp{I.J_u, I.K_u};
     auto in_range = [&](int64_t e) { const int64_t b = global_bin(I, e) - W.gblo; return b >= 0 && b < W.nb; };
     bool in = in_range(E);
     int site = (int)start;
@@ -211,37 +171,48 @@ __device__ bool adjust_walk(const InstDev& I, const WinDev& W, int8_t* sp, int64
         if (++steps > max_steps || ++idle > 2 * (int64_t)N) return false;
         ++site;
         if (site == N) { site = 0; flavour ^= 1; }
-        int64_t dE;
-        int8_t* a;
-        if (I.model == REWL_MODEL_ISING2D) {
-            a = sp;
-            const int sum = sp[nb_up(site, L)] + sp[nb_left(site, L)] + sp[nb_right(site, L)] + sp[nb_down(site, L)];
-            dE = 2 * (int64_t)sp[site] * I.J_u * sum;
-        } else {
-            int8_t* s = sp; int8_t* t = sp + N;
-            a = flavour == 0 ? s : t;
-            int8_t* b = flavour == 0 ? t : s;
-            dE = at_dE(a, b, site, L, I.J_u, I.K_u, h ? h[site] : 0);
-            if (site == N - 1) flavour ^= 1;     // change_state toggles at the last site
-        }
+        const int plane = Model::kPlanes == 1 ? 0 : flavour;
+        const int8_t* a = sp + plane * N;
+        const int8_t* b = sp + (plane ^ 1) * N;
+        const int64_t dE = Model::delta_energy(a, b, site, L, cp, h ? h[site] : 0);
+        if (Model::kPlanes == 2 && site == N - 1) flavour ^= 1;     // change_state toggles at the last site
         const int64_t gb = global_bin(I, E) - W.gblo;
         const bool too_low = gb < 0, too_high = gb >= W.nb;
         const int64_t En = E + dE;
         if ((too_low && En > E) || (too_high && En <= E)) {
             E = En;
             idle = 0;
-            if (I.model == REWL_MODEL_ISING2D) { M[0] -= 2 * a[site]; a[site] = (int8_t)-a[site]; }
-            else {
-                // flavour was possibly toggled above; the flipped plane is the one chosen before the toggle
-                int8_t* s = sp; int8_t* t = sp + N;
-                const bool flipped_sigma = (a == s);
-                if (flipped_sigma) { M[0] -= 2 * s[site]; M[2] -= 2 * s[site] * t[site]; s[site] = (int8_t)-s[site]; }
-                else { M[1] -= 2 * t[site]; M[2] -= 2 * s[site] * t[site]; t[site] = (int8_t)-t[site]; }
-            }
+            Model::flip(sp, N, site, plane, M);      // the plane chosen before a toggle
         }
         in = in_range(E);
     }
     return true;
+}
+
+template <class Model>
+__device__ void init_walker(const InstDev& I, const WinDev& W, int8_t* sp, const int64_t* h, uint32_t uid,
+                            int64_t& E, int32_t* M, int32_t& flavour, bool& ok)
+{
+    const Couplings cp{I.J_u, I.K_u};
+    const int init_random = (int)(I.init_mode == 0);
+    for (int i = 0; i < I.ndof; ++i)
+        sp[i] = init_random ? ((philox_word(I.seed, uid, (uint64_t)i, kStreamInit) >> 31) ? -1 : 1) : 1;
+    Model::recalculate(sp, I.L, cp, h, E, M);
+    flavour = 0;
+    const uint32_t start = mulhi32(philox_word(I.seed, uid, 0, kStreamAdjust), (uint32_t)I.N);
+    const int64_t cap = 4000LL * I.ndof;
+    ok = adjust_walk<Model>(I, W, sp, E, M, flavour, h, start, cap);
+    // a greedy walk can stick in a local extremum: retry from all +1 (walks up
+    // from the ground state) and then from the checkerboard (walks down from the top)
+    for (int attempt = 1; attempt <= 2 && !ok; ++attempt) {
+        for (int i = 0; i < I.ndof; ++i) {
+            const int site = i % I.N, x = site % I.L, y = site / I.L;
+            sp[i] = (attempt == 1 || ((x + y) & 1) == 0) ? 1 : -1;
+        }
+        Model::recalculate(sp, I.L, cp, h, E, M);
+        flavour = 0;
+        ok = adjust_walk<Model>(I, W, sp, E, M, flavour, h, start, cap);
+    }
 }
 
 __global__ void k_init(DevPtrs P, int nslots, int init_mode_mask_unused)
@@ -255,28 +226,10 @@ __global__ void k_init(DevPtrs P, int nslots, int init_mode_mask_unused)
     int8_t* sp = P.spins + P.cfg_off[c];
     const uint32_t uid = (uint32_t)(s - I.first_slot);
     const int64_t* h = I.field_off >= 0 ? P.fields + I.field_off : nullptr;
-    const int init_random = (int)(I.init_mode == 0);
-    for (int i = 0; i < I.ndof; ++i)
-        sp[i] = init_random ? ((philox_word(I.seed, uid, (uint64_t)i, kStreamInit) >> 31) ? -1 : 1) : 1;
-    int64_t E; int32_t M[3] = {0, 0, 0};
-    if (I.model == REWL_MODEL_ISING2D) ising_recalc(sp, I.L, I.J_u, E, M[0]);
-    else at_recalc(sp, sp + I.N, I.L, I.J_u, I.K_u, h, E, M);
-    int32_t flavour = 0;
-    const uint32_t start = mulhi32(philox_word(I.seed, uid, 0, kStreamAdjust), (uint32_t)I.N);
-    const int64_t cap = 4000LL * I.ndof;
-    bool ok = adjust_walk(I, W, sp, E, M, flavour, h, start, cap);
-    // a greedy walk can stick in a local extremum: retry from all +1 (walks up
-    // from the ground state) and then from the checkerboard (walks down from the top)
-    for (int attempt = 1; attempt <= 2 && !ok; ++attempt) {
-        for (int i = 0; i < I.ndof; ++i) {
-            const int site = i % I.N, x = site % I.L, y = site / I.L;
-            sp[i] = (attempt == 1 || ((x + y) & 1) == 0) ? 1 : -1;
-        }
-        if (I.model == REWL_MODEL_ISING2D) ising_recalc(sp, I.L, I.J_u, E, M[0]);
-        else at_recalc(sp, sp + I.N, I.L, I.J_u, I.K_u, h, E, M);
-        flavour = 0;
-        ok = adjust_walk(I, W, sp, E, M, flavour, h, start, cap);
-    }
+    int64_t E = 0; int32_t M[3] = {0, 0, 0}; int32_t flavour = 0;
+    bool ok = false;
+    if (I.model == REWL_MODEL_ISING2D) init_walker<Ising2dModel>(I, W, sp, h, uid, E, M, flavour, ok);
+    else init_walker<AshkinTeller2dModel>(I, W, sp, h, uid, E, M, flavour, ok);
     if (!ok) atomicOr(&P.counters[0], ERR_ADJUST);
     P.cfg_E[c] = E;
     P.cfg_M[3 * c] = M[0]; P.cfg_M[3 * c + 1] = M[1]; P.cfg_M[3 * c + 2] = M[2];
@@ -293,8 +246,9 @@ __global__ void k_recalc(DevPtrs P, const int32_t* cfgs, const int32_t* insts, i
     const int8_t* sp = P.spins + P.cfg_off[c];
     const int64_t* h = I.field_off >= 0 ? P.fields + I.field_off : nullptr;
     int64_t E; int32_t M[3] = {0, 0, 0};
-    if (I.model == REWL_MODEL_ISING2D) ising_recalc(sp, I.L, I.J_u, E, M[0]);
-    else at_recalc(sp, sp + I.N, I.L, I.J_u, I.K_u, h, E, M);
+    const Couplings cp{I.J_u, I.K_u};
+    if (I.model == REWL_MODEL_ISING2D) Ising2dModel::recalculate(sp, I.L, cp, h, E, M);
+    else AshkinTeller2dModel::recalculate(sp, I.L, cp, h, E, M);
     P.cfg_E[c] = E;
     P.cfg_M[3 * c] = M[0]; P.cfg_M[3 * c + 1] = M[1]; P.cfg_M[3 * c + 2] = M[2];
 }
@@ -309,30 +263,6 @@ __global__ void k_recalc(DevPtrs P, const int32_t* cfgs, const int32_t* insts, i
 // moments of Ashkin_Teller2d::update_observables (ashkin_teller2d_hamiltonian.hpp:267-318).
 // The reference keeps running means (v + c avg) / (c + 1) (ising2d_observables.hpp:134-145);
 // the export divides these sums by the visits instead, equal up to FP64 rounding.
-__device__ inline void obs_add_ising(double* o, int M, double invN)
-{
-    const double m = invN * fabs((double)M);
-    atomicAdd(o, m);
-    atomicAdd(o + 1, m * m);
-    atomicAdd(o + 2, m * m * m * m);
-}
-
-// With correlators each Ashkin-Teller group of three moments is followed by its
-// G(q_min) column (sigma, tau, phi, Baxter: ashkin_teller2d_observables.hpp:36-41).
-__device__ inline void obs_add_at(double* o, int sm, int tm, int bx, double invN, int corr)
-{
-    const double a = invN * fabs((double)sm), t = invN * fabs((double)tm), b = invN * fabs((double)bx);
-    const double p2 = a * a + t * t;
-    const int g = corr ? 1 : 0;
-    atomicAdd(o + 0, a); atomicAdd(o + 1, a * a); atomicAdd(o + 2, a * a * a * a);
-    o += g;
-    atomicAdd(o + 3, t); atomicAdd(o + 4, t * t); atomicAdd(o + 5, t * t * t * t);
-    o += g;
-    atomicAdd(o + 6, sqrt(p2)); atomicAdd(o + 7, p2); atomicAdd(o + 8, p2 * p2);
-    o += g;
-    atomicAdd(o + 9, b); atomicAdd(o + 10, b * b); atomicAdd(o + 11, b * b * b * b);
-}
-
 // G(q_min) correlators (CORRELATION_LENGTHS, on in the reference's default build).  At
 // every visit of a bin whose count before the visit is a multiple of counts_per_transform
 // = 1000 (src/Hamiltonians/Correlations/fourier_correlator.hpp:11), the walker's G is added
@@ -364,25 +294,6 @@ __device__ double plane_corr(const int* rs, const int* cs, const double* q, int 
         ix += r * sn;
         ry += (double)cl * c;
         iy += (double)cl * sn;
-    }
-    return 0.5 * ((rx * rx + ix * ix) + (ry * ry + iy * iy));
-}
-
-// The same from a whole configuration, in the reference's order (one thread): plane a,
-// or the product plane a * b.
-__device__ double full_corr(const int8_t* a, const int8_t* b, const double* q, int L)
-{
-    double rx = 0.0, ix = 0.0, ry = 0.0, iy = 0.0;
-    for (int y = 0; y < L; ++y) {
-        int rsum = 0;
-        for (int x = 0; x < L; ++x) {
-            const int v = b ? a[y * L + x] * b[y * L + x] : a[y * L + x];
-            rsum += v;
-            ry += (double)v * q[x];
-            iy += (double)v * q[L + x];
-        }
-        rx += (double)rsum * q[y];
-        ix += (double)rsum * q[L + y];
     }
     return 0.5 * ((rx * rx + ix * ix) + (ry * ry + iy * iy));
 }
@@ -545,17 +456,15 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
             // chunk = sites c0 .. c0+C-1 of one row (C divides L)
             const int y = c0 / L, x0 = c0 - y * L, x = x0 + lane;
             const int row = y * L;
-            const int up = (y == 0 ? L - 1 : y - 1) * L, down = (y == L - 1 ? 0 : y + 1) * L;
             int si = 0, d0 = 0, d1 = 0, wc = 0;
             long long T = 0;
             if (lane < C) {
                 si = lat[row + x];
-                const int left = lat[row + (x == 0 ? L - 1 : x - 1)];
-                const int right = lat[row + (x == L - 1 ? 0 : x + 1)];
-                const int sum = lat[up + x] + left + right + lat[down + x];
-                d0 = 2 * J * si * sum;
-                d1 = lane > 0 ? d0 - 4 * J * si * left : d0;
-                wc = (C == L && lane == L - 1) ? -4 * J * si * right : 0;
+                const Couplings cp{J, 0};
+                const int i = row + x;
+                d0 = (int)Ising2dModel::delta_energy(lat, nullptr, i, L, cp, 0);
+                d1 = lane > 0 ? (int)Ising2dModel::left_flipped(lat, nullptr, i, L, cp, d0) : d0;
+                wc = (C == L && lane == L - 1) ? (int)Ising2dModel::right_flipped(lat, nullptr, i, L, cp) : 0;
                 if (!REPLAY) {
                     const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)(c0 + lane), kStreamWL);
                     T = accept_threshold(neglog_u32(word));
@@ -626,8 +535,11 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
             if (obs_on) {
                 __syncwarp();
                 if (lane < C)
-                    obs_add_ising(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
-                                  M + chunk_dm(acc, plus, lane), invN);
+                {
+                    const int32_t Mv[1] = {M + chunk_dm(acc, plus, lane)};
+                    Ising2dModel::add_observables(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride, Mv,
+                                                  invN, P.corr);
+                }
                 if (corr) {
                     const int bin = lane < C ? st->seq[lane] : -1 - lane;
                     const unsigned grp = __match_any_sync(kFull, bin);
@@ -971,8 +883,11 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
                 for (int k = 0; k < SPL; ++k) {
                     const int jj = q + k * P;
                     if (jj < C)
-                        obs_add_ising(ob + (size_t)((seqb[jj] - gsoff) >> 3) * P_.obs_stride, M + chunk_dm(acc, plus, jj),
-                                      1.0 / (double)N);
+                    {
+                        const int32_t Mv[1] = {M + chunk_dm(acc, plus, jj)};
+                        Ising2dModel::add_observables(ob + (size_t)((seqb[jj] - gsoff) >> 3) * P_.obs_stride, Mv,
+                                                      1.0 / (double)N, P_.corr);
+                    }
                 }
             }
             if (corr) {
@@ -1268,11 +1183,11 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
                 if (lane < C) {
                     const int i = c0 + lane;
                     ai = A[i]; bi = B[i];
-                    const int l = nb_left(i, L), r = nb_right(i, L);
-                    const long long d0 = at_dE(A, B, i, L, J, K, hf ? hf[i] : 0);
-                    const long long d1 = lane > 0 ? d0 - 4 * (long long)ai * A[l] * (J + K * (long long)bi * B[l]) : d0;
+                    const Couplings cp{J, K};
+                    const long long d0 = AshkinTeller2dModel::delta_energy(A, B, i, L, cp, hf ? hf[i] : 0);
+                    const long long d1 = lane > 0 ? AshkinTeller2dModel::left_flipped(A, B, i, L, cp, d0) : d0;
                     st->du[lane] = make_longlong2(d0 * mul, d1 * mul);
-                    if (wraps && lane == C - 1) st->wcu = -4 * (long long)ai * A[r] * (J + K * (long long)bi * B[r]) * mul;
+                    if (wraps && lane == C - 1) st->wcu = AshkinTeller2dModel::right_flipped(A, B, i, L, cp) * mul;
                     if (!REPLAY) {
                         const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)i, kStreamWL);
                         st->T[lane] = accept_threshold(neglog_u32(word));
@@ -1309,9 +1224,9 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
                     __syncwarp();
                     if (lane < C) {
                         const int da = chunk_dm(acc, aplus, lane), db = chunk_dm(acc, abplus, lane);
-                        obs_add_at(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
-                                   flavour == 0 ? sm0 + da : sm0, flavour == 0 ? tm0 : tm0 + da, bx0 + db,
-                                   invN, P.corr);
+                        const int32_t Mv[3] = {flavour == 0 ? sm0 + da : sm0, flavour == 0 ? tm0 : tm0 + da, bx0 + db};
+                        AshkinTeller2dModel::add_observables(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
+                                                             Mv, invN, P.corr);
                     }
                     if (corr) {
                         const int y = c0 / L, x0 = c0 - y * L, row = y * L;
@@ -1408,21 +1323,16 @@ __device__ inline void touch(const DevPtrs& P, const InstDev& I, int slot)
     if (P.obs) {
         double* ob = P.obs + (size_t)o * P.obs_stride;
         const double invN = 1.0 / (double)I.N;
-        if (I.model == REWL_MODEL_ISING2D) obs_add_ising(ob, P.cfg_M[3 * c], invN);
-        else obs_add_at(ob, P.cfg_M[3 * c], P.cfg_M[3 * c + 1], P.cfg_M[3 * c + 2], invN, P.corr);
-        if (P.corr && seen % kCountsPerTransform == 0) {
-            const double* q = P.qtab + I.qtab_off;
-            const int8_t* sp = P.spins + P.cfg_off[c];
-            const double in2 = invN * invN;
-            if (I.model == REWL_MODEL_ISING2D) {
-                atomicAdd(ob + 3, in2 * full_corr(sp, nullptr, q, I.L));
-            } else {
-                // the tau correlator is computed from sigma, as the reference does
-                // (ashkin_teller2d_hamiltonian.hpp:298-299); phi's is the sum of the two
-                const double gs = in2 * full_corr(sp, nullptr, q, I.L);
-                const double gb = in2 * full_corr(sp, sp + I.N, q, I.L);
-                atomicAdd(ob + 3, gs); atomicAdd(ob + 7, gs); atomicAdd(ob + 11, gs + gs); atomicAdd(ob + 15, gb);
-            }
+        const int32_t* Mc = P.cfg_M + 3 * c;
+        const bool due = P.corr && seen % kCountsPerTransform == 0;
+        const double* q = P.qtab + I.qtab_off;
+        const int8_t* sp = P.spins + P.cfg_off[c];
+        if (I.model == REWL_MODEL_ISING2D) {
+            Ising2dModel::add_observables(ob, Mc, invN, P.corr);
+            if (due) Ising2dModel::add_correlators(ob, sp, I.N, I.L, q, invN * invN);
+        } else {
+            AshkinTeller2dModel::add_observables(ob, Mc, invN, P.corr);
+            if (due) AshkinTeller2dModel::add_correlators(ob, sp, I.N, I.L, q, invN * invN);
         }
     }
 }
