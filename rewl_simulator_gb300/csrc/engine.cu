@@ -21,8 +21,9 @@
 //                   (energy change with and without the left neighbour flipped,
 //                   integer acceptance threshold), lane 0 resolves the serial
 //                   Wang-Landau chain in integer arithmetic only
-//   k_sweep_at      the same for Ashkin-Teller (one plane per pass, tables in
-//                   global memory)
+//   k_sweep_tables  the same for any model type of models.cuh with the tables in
+//                   global memory (Ashkin-Teller: one plane per pass; Ising windows
+//                   too large for shared memory)
 //   k_exchange      one thread per window pair (rewl_simulation.hpp:228-346)
 //   k_flat          one block per window: flatness vote, FP64 count-weighted
 //                   averaging, histogram reset, REDUCE_LOGDOS, ln f schedule
@@ -1022,7 +1023,7 @@ cudaError_t allow_bins_smem()
 // derived at its end from the change of g against a copy taken at its start
 // (every visit adds the same ln f), and the chain loads both possible proposals
 // of the next step one step ahead, so a load's latency overlaps a decision.
-struct StageAT {
+struct TableStage {
     longlong2 du[32];        // per site: {proposal, proposal after its left neighbour flipped in this chunk}
     long long T[32];         // acceptance thresholds of the chunk's sites
     long long wcu;           // row-wrap correction of the last site when the chunk is a whole row
@@ -1033,7 +1034,7 @@ struct StageAT {
 // position v = (E - E_lo) * bin_mul - gblo << bin_shift, in units of the bin
 // numerator within the window, so that a proposal's bin is (v + dv) >> bin_shift:
 // one add and one shift instead of a multiply per candidate.
-struct ChainAT {
+struct TableChain {
     long long v, vn, gc, draws;
     long long G0, G1;        // logDoS loaded for step j's proposal if step j-1 was rejected / accepted
     long long T;             // step j's threshold
@@ -1053,7 +1054,7 @@ struct ChainAT {
 // WRAPFIX: step j+1 is the last site of a whole-row chunk, whose right neighbour
 // is the row's first site, flipped in this chunk iff bit 0 of acc.
 template <bool REPLAY, bool OBS, bool PREFETCH, bool LOADQ, bool WRAPFIX>
-__device__ __forceinline__ void at_step(ChainAT& c, const int j, StageAT* st, long long* gg, const int nb,
+__device__ __forceinline__ void table_step(TableChain& c, const int j, TableStage* st, long long* gg, const int nb,
                                         const int sh, const long long lnf, const DevPtrs& P,
                                         const long long thr_off, const long long thr_n)
 {
@@ -1103,9 +1104,14 @@ __device__ __forceinline__ void at_step(ChainAT& c, const int j, StageAT* st, lo
     }
 }
 
-template <bool REPLAY, bool OBS>
-__global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
+// Sweeps of any model type of models.cuh with the window tables in global memory (the
+// Ashkin-Teller instances, whose windows hold tens of thousands of bins, and Ising windows too
+// large for shared memory).  One warp per walker; the planes sweep in turn (sigma then tau for
+// Ashkin-Teller, wang_landau.hpp:109-119), the flipped plane toggling after each pass.
+template <class Model, bool REPLAY, bool OBS>
+__global__ void __launch_bounds__(256, 2) k_sweep_tables(const SweepParams p)
 {
+    constexpr int NP = Model::kPlanes, NM = Model::kMags, NC = Model::kCorrPlanes;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int li = blockIdx.x * (blockDim.x >> 5) + wib;
@@ -1117,32 +1123,29 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
     const WinDev W = P.win[w];
     const int L = I.L, N = I.N, C = I.chunk, nb = W.nb;
     unsigned char* base = smem + (size_t)wib * p.smem_per_warp;
-    StageAT* st = reinterpret_cast<StageAT*>(base);
-    int8_t* sig = reinterpret_cast<int8_t*>(st + 1);
-    int8_t* tau = sig + N;
+    TableStage* st = reinterpret_cast<TableStage*>(base);
+    int8_t* sp = reinterpret_cast<int8_t*>(st + 1);       // NP planes of N spins
     const int64_t* hf = I.field_off >= 0 ? P.fields + I.field_off : nullptr;
 
     const int cfg = P.slot_cfg[s];
     int8_t* gl = P.spins + P.cfg_off[cfg];
-    for (int i = lane; i < 2 * N; i += 32) sig[i] = gl[i];
+    for (int i = lane; i < NP * N; i += 32) sp[i] = gl[i];
     long long* gg = reinterpret_cast<long long*>(P.g + P.slot_tab[s]);
     long long* g0 = reinterpret_cast<long long*>(P.gsnap + P.slot_tab[s]);
     for (int k = lane; k < nb; k += 32) g0[k] = gg[k];
     __syncwarp();
-    // correlators: row and column sums of the sigma plane and of the Baxter plane sigma * tau
-    int* rs_s = reinterpret_cast<int*>(sig + ((2 * N + 15) & ~15));
-    int* cs_s = rs_s + L;
-    int* rs_b = cs_s + L;
-    int* cs_b = rs_b + L;
+    // correlators: row sums rs[p] and column sums cs[p] of every correlator plane
+    int* sums = reinterpret_cast<int*>(sp + ((NP * N + 15) & ~15));
     const bool corr = OBS && P.corr;
     const double invN = 1.0 / (double)N;
     if (corr) {
-        plane_sums(rs_s, cs_s, L, lane, [&](int i) { return (int)sig[i]; });
-        plane_sums(rs_b, cs_b, L, lane, [&](int i) { return (int)sig[i] * (int)tau[i]; });
+        for (int cp = 0; cp < NC; ++cp)
+            plane_sums(sums + 2 * L * cp, sums + 2 * L * cp + L, L, lane,
+                       [&](int i) { return Model::corr_site(sp, N, i, cp); });
         __syncwarp();
     }
 
-    const long long J = I.J_u, K = I.K_u;
+    const Couplings cpl{I.J_u, I.K_u};
     const long long lnf = P.win_lnf[w];
     const uint64_t sweeps0 = P.slot_sweeps[s];
     const uint32_t uid = (uint32_t)(s - I.first_slot);
@@ -1151,15 +1154,15 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
     const int sh = I.bin_shift;
     const long long vlo = (long long)W.gblo << sh;     // window start in bin-numerator units
     const bool wraps = C == L;
-    int flavour = P.slot_flavour[s];
+    int flavour = NP == 1 ? 0 : P.slot_flavour[s];
 
-    ChainAT c{};
-    int sm = 0, tm = 0, bx = 0;
+    TableChain c{};
+    int32_t M[3] = {0, 0, 0};                          // lane 0: the magnetisations
     long long thr_off = 0, thr_n = 0;
     int err = 0;
     if (lane == 0) {
         const long long E = P.cfg_E[cfg];
-        sm = P.cfg_M[3 * cfg]; tm = P.cfg_M[3 * cfg + 1]; bx = P.cfg_M[3 * cfg + 2];
+        for (int m = 0; m < NM; ++m) M[m] = P.cfg_M[3 * cfg + m];
         c.v = (E - eglo) * mul - vlo;
         const long long gb = c.v >> sh;
         if (gb < 0 || gb >= nb) err = ERR_BOUNDS;
@@ -1174,20 +1177,22 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
     }
 
     for (int sw = 0; sw < p.nsweeps; ++sw) {
-        for (int pass = 0; pass < 2; ++pass) {
-            int8_t* A = flavour == 0 ? sig : tau;
-            int8_t* B = flavour == 0 ? tau : sig;
-            const uint64_t A0 = ((sweeps0 + (uint64_t)sw) * 2u + (uint64_t)pass) * (uint64_t)N;
+        for (int pass = 0; pass < NP; ++pass) {
+            const int plane = NP == 1 ? 0 : flavour;
+            int8_t* A = sp + plane * N;
+            const int8_t* B = NP == 1 ? A : sp + (plane ^ 1) * N;
+            const uint64_t A0 = ((sweeps0 + (uint64_t)sw) * (uint64_t)NP + (uint64_t)pass) * (uint64_t)N;
             for (int c0 = 0; c0 < N; c0 += C) {
-                int ai = 0, bi = 0;
+                int ai = 0, sg[NM];
+                for (int m = 0; m < NM; ++m) sg[m] = 0;
                 if (lane < C) {
                     const int i = c0 + lane;
-                    ai = A[i]; bi = B[i];
-                    const Couplings cp{J, K};
-                    const long long d0 = AshkinTeller2dModel::delta_energy(A, B, i, L, cp, hf ? hf[i] : 0);
-                    const long long d1 = lane > 0 ? AshkinTeller2dModel::left_flipped(A, B, i, L, cp, d0) : d0;
+                    ai = A[i];
+                    Model::flip_signs(ai, B[i], plane, sg);
+                    const long long d0 = Model::delta_energy(A, B, i, L, cpl, hf ? hf[i] : 0);
+                    const long long d1 = lane > 0 ? Model::left_flipped(A, B, i, L, cpl, d0) : d0;
                     st->du[lane] = make_longlong2(d0 * mul, d1 * mul);
-                    if (wraps && lane == C - 1) st->wcu = AshkinTeller2dModel::right_flipped(A, B, i, L, cp) * mul;
+                    if (wraps && lane == C - 1) st->wcu = Model::right_flipped(A, B, i, L, cpl) * mul;
                     if (!REPLAY) {
                         const uint32_t word = philox_word(seed, uid, A0 + (uint64_t)i, kStreamWL);
                         st->T[lane] = accept_threshold(neglog_u32(word));
@@ -1203,80 +1208,80 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
                     c.ap = false;
                     if (!REPLAY) c.T = st->T[0];
                     if (C == 1) {
-                        at_step<REPLAY, OBS, false, false, false>(c, 0, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        table_step<REPLAY, OBS, false, false, false>(c, 0, st, gg, nb, sh, lnf, P, thr_off, thr_n);
                     } else {
                         c.q = st->du[1];
 #pragma unroll 4
                         for (int j = 0; j < C - 2; ++j)
-                            at_step<REPLAY, OBS, true, true, false>(c, j, st, gg, nb, sh, lnf, P, thr_off, thr_n);
-                        if (wraps) at_step<REPLAY, OBS, true, false, true>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
-                        else at_step<REPLAY, OBS, true, false, false>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
-                        at_step<REPLAY, OBS, false, false, false>(c, C - 1, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                            table_step<REPLAY, OBS, true, true, false>(c, j, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        if (wraps) table_step<REPLAY, OBS, true, false, true>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        else table_step<REPLAY, OBS, true, false, false>(c, C - 2, st, gg, nb, sh, lnf, P, thr_off, thr_n);
+                        table_step<REPLAY, OBS, false, false, false>(c, C - 1, st, gg, nb, sh, lnf, P, thr_off, thr_n);
                     }
                 }
                 const unsigned acc = __shfl_sync(kFull, c.acc, 0);
-                const unsigned aplus = __ballot_sync(kFull, lane < C && ai > 0);
-                const unsigned abplus = __ballot_sync(kFull, lane < C && ai * bi > 0);
+                // per magnetisation: the steps whose accepted flip lowers it (its term was +1)
+                // and raises it; the change after step j is -2 (lowered - raised) up to j
+                unsigned plus[NM], minus[NM];
+                for (int m = 0; m < NM; ++m) {
+                    plus[m] = __ballot_sync(kFull, lane < C && sg[m] > 0);
+                    minus[m] = __ballot_sync(kFull, lane < C && sg[m] < 0);
+                }
+                auto dm = [&](int m, int j) {
+                    const unsigned le = j >= 31 ? 0xFFFFFFFFu : ((2u << j) - 1u);
+                    return -2 * ((int)__popc(acc & plus[m] & le) - (int)__popc(acc & minus[m] & le));
+                };
                 if (OBS) {
-                    // magnetisations after each step of the chunk, from lane 0's values before it
-                    const int sm0 = __shfl_sync(kFull, sm, 0), tm0 = __shfl_sync(kFull, tm, 0);
-                    const int bx0 = __shfl_sync(kFull, bx, 0);
+                    int32_t M0[3] = {0, 0, 0};
+                    for (int m = 0; m < NM; ++m) M0[m] = __shfl_sync(kFull, M[m], 0);
                     __syncwarp();
                     if (lane < C) {
-                        const int da = chunk_dm(acc, aplus, lane), db = chunk_dm(acc, abplus, lane);
-                        const int32_t Mv[3] = {flavour == 0 ? sm0 + da : sm0, flavour == 0 ? tm0 : tm0 + da, bx0 + db};
-                        AshkinTeller2dModel::add_observables(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride,
-                                                             Mv, invN, P.corr);
+                        int32_t Mv[3] = {0, 0, 0};
+                        for (int m = 0; m < NM; ++m) Mv[m] = M0[m] + dm(m, lane);
+                        Model::add_observables(P.obs + (size_t)(P.slot_tab[s] + st->seq[lane]) * P.obs_stride, Mv, invN,
+                                               P.corr);
                     }
                     if (corr) {
                         const int y = c0 / L, x0 = c0 - y * L, row = y * L;
                         const int bin = lane < C ? st->seq[lane] : -1 - lane;
                         const unsigned grp = __match_any_sync(kFull, bin);
                         if (lane < C) {
-                            // the bin's count before step `lane` (see the Ising kernel)
+                            // the bin's count before step `lane`: its visits at the launch's start
+                            // plus the change of g over ln f, less the chunk's visits from this step on
                             const unsigned long long after =
                                 P.visits[P.slot_tab[s] + bin] + (unsigned long long)((gg[bin] - g0[bin]) / lnf);
                             const unsigned long long seen = after - (unsigned long long)__popc(grp >> lane);
                             if (seen % kCountsPerTransform == 0) {
                                 const double* q = P.qtab + I.qtab_off;
-                                // sigma changes in the sigma pass only, the Baxter product in both
-                                const double gsig = plane_corr(rs_s, cs_s, q, L, y, flavour == 0 ? chunk_dm(acc, aplus, lane) : 0,
-                                                               x0, lane, flavour == 0 ? acc : 0u,
-                                                               [&](int k) { return (int)sig[row + x0 + k]; });
-                                const double gbax = plane_corr(rs_b, cs_b, q, L, y, chunk_dm(acc, abplus, lane), x0, lane, acc,
-                                                               [&](int k) { return (int)sig[row + x0 + k] * (int)tau[row + x0 + k]; });
-                                const double gs = invN * invN * gsig, gb = invN * invN * gbax;
-                                // the tau correlator is computed from sigma, as the reference does
-                                // (ashkin_teller2d_hamiltonian.hpp:298-299); phi's is the sum of the two
-                                double* o = P.obs + (size_t)(P.slot_tab[s] + bin) * P.obs_stride;
-                                atomicAdd(o + 3, gs); atomicAdd(o + 7, gs); atomicAdd(o + 11, gs + gs); atomicAdd(o + 15, gb);
+                                double G[NC];
+                                for (int cp = 0; cp < NC; ++cp) {
+                                    const int m = Model::corr_mag(cp);
+                                    // a correlator plane changes where its magnetisation's terms do
+                                    G[cp] = plane_corr(sums + 2 * L * cp, sums + 2 * L * cp + L, q, L, y, dm(m, lane), x0, lane,
+                                                       acc & (plus[m] | minus[m]),
+                                                       [&](int k) { return Model::corr_site(sp, N, row + x0 + k, cp); });
+                                }
+                                Model::add_transforms(P.obs + (size_t)(P.slot_tab[s] + bin) * P.obs_stride, G, invN * invN);
                             }
                         }
                         __syncwarp();
                         // the chunk's flips into the sums
-                        if (lane < C && ((acc >> lane) & 1u)) {
-                            if (flavour == 0) cs_s[x0 + lane] -= 2 * ai;
-                            cs_b[x0 + lane] -= 2 * ai * bi;
-                        }
-                        if (lane == 0) {
-                            if (flavour == 0) rs_s[y] += -2 * ((int)__popc(acc & aplus) - (int)__popc(acc & ~aplus));
-                            rs_b[y] += -2 * ((int)__popc(acc & abplus) - (int)__popc(acc & ~abplus));
+                        for (int cp = 0; cp < NC; ++cp) {
+                            const int m = Model::corr_mag(cp);
+                            if (lane < C && ((acc >> lane) & 1u)) sums[2 * L * cp + L + x0 + lane] -= 2 * sg[m];
+                            if (lane == 0) sums[2 * L * cp + y] += dm(m, 31);
                         }
                     }
                 }
                 if (lane < C && ((acc >> lane) & 1u)) A[c0 + lane] = (int8_t)(-ai);
-                if (lane == 0) {
-                    const int da = -2 * ((int)__popc(acc & aplus) - (int)__popc(acc & ~aplus));
-                    const int db = -2 * ((int)__popc(acc & abplus) - (int)__popc(acc & ~abplus));
-                    if (flavour == 0) sm += da; else tm += da;
-                    bx += db;
-                }
+                if (lane == 0)
+                    for (int m = 0; m < NM; ++m) M[m] += dm(m, 31);
                 __syncwarp();
             }
-            flavour ^= 1;
+            if (NP == 2) flavour ^= 1;
         }
     }
-    for (int i = lane; i < 2 * N; i += 32) gl[i] = sig[i];
+    for (int i = lane; i < NP * N; i += 32) gl[i] = sp[i];
     // counts and visits from the logDoS change (lane 0's stores to g are ordered
     // before the other lanes' loads by the barrier)
     __syncwarp();
@@ -1292,9 +1297,9 @@ __global__ void __launch_bounds__(256, 2) k_sweep_at(const SweepParams p)
     }
     if (lane == 0) {
         P.cfg_E[cfg] = eglo + (c.v + vlo) / mul;
-        P.cfg_M[3 * cfg] = sm; P.cfg_M[3 * cfg + 1] = tm; P.cfg_M[3 * cfg + 2] = bx;
+        for (int m = 0; m < NM; ++m) P.cfg_M[3 * cfg + m] = M[m];
         P.slot_sweeps[s] = sweeps0 + (uint64_t)p.nsweeps;
-        P.slot_flavour[s] = flavour;
+        if (NP == 2) P.slot_flavour[s] = flavour;
         if (REPLAY) P.slot_draws[s] = c.draws;
         if (c.err) atomicOr(&P.counters[0], c.err);
     }
@@ -1606,16 +1611,24 @@ struct Launch {
     int bins = 0;           // Ising bin-tracking kernel with `walkers_per_warp` walkers per warp and chunk `chunk`
     int walkers_per_warp = 1;
     int chunk = 32;
-    int carveout = -1;      // Ashkin-Teller: shared-memory carveout (percent) that leaves the rest to L1
+    int tables = 0;         // the global-table kernel (k_sweep_tables)
+    int carveout = -1;      // global-table kernel: shared-memory carveout (percent) that leaves the rest to L1
     DBuf<int32_t> d_slots;
 };
 
 using SweepKernel = void (*)(const SweepParams);
 
-SweepKernel at_kernel(bool replay, bool obs)
+template <class Model>
+SweepKernel table_kernel_t(bool replay, bool obs)
 {
-    if (replay) return obs ? k_sweep_at<true, true> : k_sweep_at<true, false>;
-    return obs ? k_sweep_at<false, true> : k_sweep_at<false, false>;
+    if (replay) return obs ? k_sweep_tables<Model, true, true> : k_sweep_tables<Model, true, false>;
+    return obs ? k_sweep_tables<Model, false, true> : k_sweep_tables<Model, false, false>;
+}
+
+SweepKernel table_kernel(int model, bool replay, bool obs)
+{
+    return model == REWL_MODEL_ISING2D ? table_kernel_t<Ising2dModel>(replay, obs)
+                                       : table_kernel_t<AshkinTeller2dModel>(replay, obs);
 }
 
 } // namespace
@@ -1649,7 +1662,7 @@ struct rewl_engine {
     bool tuned = false;
     int64_t kernel_launches = 0;        // sweep-kernel launches since the last timing read
     int64_t launches_total = 0;         // every engine kernel since creation
-    int sweep_variant = 3;              // Ising resolver: 3 all-lane (default), 2 lane-0 (REWL_SWEEP_VARIANT=2)
+    int sweep_variant = 3;              // REWL_SWEEP_VARIANT: 3 all-lane Ising resolver (default), 2 lane-0, 4 global tables
 
     DBuf<InstDev> d_inst;
     DBuf<WinDev> d_win;
@@ -2025,9 +2038,9 @@ int sm_count(const rewl_engine* e)
 // (the driver's default leaves L1 far less).
 int at_carveout(rewl_engine* e, Launch& l)
 {
-    if (l.bins || l.model == REWL_MODEL_ISING2D) return REWL_OK;
+    if (!l.tables) return REWL_OK;
     const int nsm = sm_count(e);
-    const SweepKernel fn = at_kernel(e->desc.rng_mode == REWL_RNG_REPLAY, e->desc.observables != 0);
+    const SweepKernel fn = table_kernel(l.model, e->desc.rng_mode == REWL_RNG_REPLAY, e->desc.observables != 0);
     const int threads = 32 * l.wpb;
     const size_t smem = (size_t)l.wpb * l.smem_per_warp;
     int occ = 0;
@@ -2103,12 +2116,19 @@ int plan_launches(rewl_engine* e)
             wpb = std::min(wpb, 4);                                // the kernel's launch bounds: 128 threads
             while (wpb > 1 && (size_t)wpb * G * l.smem_per_warp > 200 * 1024) wpb >>= 1;
             l.wpb = wpb;
-        } else if (l.model == REWL_MODEL_ISING2D) {
-            l.nbcap = (maxnb + 1) & ~1;
-            l.smem_per_warp = (int)(l.nbcap * 8 + sizeof(Stage) + ((maxN + 15) & ~15) + (corr ? 8 * maxL : 0));
         } else {
-            l.nbcap = 0;
-            l.smem_per_warp = (int)(sizeof(StageAT) + ((2 * maxN + 15) & ~15) + (corr ? 16 * maxL : 0));
+            const size_t ising_smem = (size_t)(((maxnb + 1) & ~1) * 8 + sizeof(Stage) + ((maxN + 15) & ~15) + (corr ? 8 * maxL : 0));
+            // Ising windows live in shared memory unless they do not fit there (or the
+            // global-table kernel is asked for)
+            l.tables = l.model != REWL_MODEL_ISING2D || e->sweep_variant == 4 || ising_smem > 200 * 1024;
+            if (!l.tables) {
+                l.nbcap = (maxnb + 1) & ~1;
+                l.smem_per_warp = (int)ising_smem;
+            } else {
+                const int planes = l.model == REWL_MODEL_ISING2D ? 1 : 2;
+                l.nbcap = 0;
+                l.smem_per_warp = (int)(sizeof(TableStage) + ((planes * maxN + 15) & ~15) + (corr ? 8 * planes * maxL : 0));
+            }
         }
         if (!l.bins) {
             l.smem_per_warp = (l.smem_per_warp + 15) & ~15;
@@ -2127,9 +2147,14 @@ int plan_launches(rewl_engine* e)
     CUDA_TRY(cudaFuncSetAttribute(k_sweep_ising<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     for (int r = 0; r < 2; ++r)
         for (int o = 0; o < 2; ++o)
-            CUDA_TRY(cudaFuncSetAttribute(at_kernel(r, o), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-    for (auto& l : e->launches)
+            for (int m : {REWL_MODEL_ISING2D, REWL_MODEL_ASHKIN_TELLER2D})
+                CUDA_TRY(cudaFuncSetAttribute(table_kernel(m, r, o), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    for (auto& l : e->launches) {
         if (int rc = at_carveout(e, l)) return rc;
+        // the global-table kernel copies each walker's logDoS at the start of a launch
+        if (l.tables && !e->gsnap.p && e->table_total > 0)
+            if (int rc = e->gsnap.alloc(e->table_total)) return rc;
+    }
     CUDA_TRY(allow_bins_smem<1>());
     CUDA_TRY(allow_bins_smem<2>());
     CUDA_TRY(allow_bins_smem<4>());
@@ -2196,14 +2221,14 @@ int launch_group(rewl_engine* e, Launch& l, cudaStream_t stream, int nsweeps, co
     } else {
         const int blocks = (sp.nslots + l.wpb - 1) / l.wpb;
         const size_t smem = (size_t)l.wpb * l.smem_per_warp;
-        if (l.model == REWL_MODEL_ISING2D) {
+        if (l.tables) {
+            const SweepKernel fn = table_kernel(l.model, replay, e->desc.observables != 0);
+            if (l.carveout >= 0) CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, l.carveout));
+            fn<<<blocks, 32 * l.wpb, smem, stream>>>(sp);
+        } else {
             if (replay) k_sweep_ising<true, 2><<<blocks, 32 * l.wpb, smem, stream>>>(sp);
             else if (e->sweep_variant == 2) k_sweep_ising<false, 2><<<blocks, 32 * l.wpb, smem, stream>>>(sp);
             else k_sweep_ising<false, 3><<<blocks, 32 * l.wpb, smem, stream>>>(sp);
-        } else {
-            const SweepKernel fn = at_kernel(replay, e->desc.observables != 0);
-            if (l.carveout >= 0) CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, l.carveout));
-            fn<<<blocks, 32 * l.wpb, smem, stream>>>(sp);
         }
     }
     CUDA_TRY(cudaGetLastError());
@@ -2349,7 +2374,12 @@ int rewl_create(const rewl_batch_desc* desc, rewl_engine** out)
     *out = nullptr;
     rewl_engine* e = new rewl_engine();
     e->desc = *desc;
-    if (const char* v = std::getenv("REWL_SWEEP_VARIANT")) e->sweep_variant = std::atoi(v) == 2 ? 2 : 3;
+    // REWL_SWEEP_VARIANT: 2 the general Ising kernel's lane-0 resolver, 3 its all-lane resolver,
+    // 4 the global-table kernel for Ising too (any of them turns the bin-tracking kernel off)
+    if (const char* v = std::getenv("REWL_SWEEP_VARIANT")) {
+        const int k = std::atoi(v);
+        e->sweep_variant = (k == 2 || k == 4) ? k : 3;
+    }
     int rc = build_host(e);               // descriptor validation and layout: host only
     if (rc) { delete e; return rc; }
     int ndev = 0;

@@ -11,6 +11,13 @@
 //   flip              apply a flip and update the magnetisations
 //   add_observables   the per-bin moments of update_observables for the current magnetisations
 //   add_correlators   the per-bin G(q_min) transforms of the whole configuration
+// and, for the sweep kernels' per-chunk bookkeeping,
+//   flip_signs        for each magnetisation, the sign of the site's term before a flip of
+//                     plane a (the flip changes it by -2 sign; 0: unchanged)
+//   corr_site         a site's value in each correlator plane
+//   add_transforms    the G(q_min) of each correlator plane into the observable columns
+// kPlanes spin planes, kMags magnetisations, kCorrPlanes correlator planes, corr_mag[p]
+// the magnetisation whose terms are correlator plane p's values.
 // Energies are integers in the model's units (Ising: J; Ashkin-Teller: 2^-20, with the
 // Baxter fields quantised to that grid), so every sum is exact.  The sweep kernels and the
 // initial walk are written against these functions; the engine dispatches on the
@@ -54,6 +61,13 @@ __device__ inline double full_corr(const int8_t* a, const int8_t* b, const doubl
 struct Ising2dModel {
     static constexpr int kPlanes = 1;
     static constexpr int kMoments = 3;
+    static constexpr int kMags = 1;
+    static constexpr int kCorrPlanes = 1;
+    __host__ __device__ static constexpr int corr_mag(int) { return 0; }
+
+    __host__ __device__ static void flip_signs(int a, int, int, int* sg) { sg[0] = a; }
+    __host__ __device__ static int corr_site(const int8_t* sp, int, int i, int) { return sp[i]; }
+    __device__ static void add_transforms(double* o, const double* G, double in2) { atomicAdd(o + 3, in2 * G[0]); }
 
     __host__ __device__ static int64_t delta_energy(const int8_t* a, const int8_t*, int i, int L, Couplings c, int64_t)
     {
@@ -109,6 +123,28 @@ struct Ising2dModel {
 struct AshkinTeller2dModel {
     static constexpr int kPlanes = 2;
     static constexpr int kMoments = 12;
+    static constexpr int kMags = 3;          // sigma, tau, Baxter
+    static constexpr int kCorrPlanes = 2;    // sigma, sigma * tau
+    __host__ __device__ static constexpr int corr_mag(int p) { return p == 0 ? 0 : 2; }
+
+    // a: the flipped plane's spin, b: the other plane's
+    __host__ __device__ static void flip_signs(int a, int b, int plane, int* sg)
+    {
+        sg[0] = plane == 0 ? a : 0;
+        sg[1] = plane == 0 ? 0 : a;
+        sg[2] = a * b;
+    }
+    __host__ __device__ static int corr_site(const int8_t* sp, int N, int i, int p)
+    {
+        return p == 0 ? sp[i] : sp[i] * sp[N + i];
+    }
+    // the tau correlator is computed from sigma, as the reference does (ashkin_teller2d_hamiltonian.hpp:
+    // 298-299); phi's is the sum of the two
+    __device__ static void add_transforms(double* o, const double* G, double in2)
+    {
+        const double gs = in2 * G[0], gb = in2 * G[1];
+        atomicAdd(o + 3, gs); atomicAdd(o + 7, gs); atomicAdd(o + 11, gs + gs); atomicAdd(o + 15, gb);
+    }
 
     __host__ __device__ static int64_t delta_energy(const int8_t* a, const int8_t* b, int i, int L, Couplings c, int64_t h)
     {

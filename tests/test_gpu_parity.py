@@ -207,6 +207,26 @@ OBS_CASES = [
 def test_engine_observables_match_oracle(engine_lib, oracle_lib, case):
     """Per-bin observables of every walker, and their count-weighted window average, against
     the oracle's running means after every check interval (all three sweep kernels)."""
+    _run_observables_case(engine_lib, oracle_lib, case)
+
+
+TABLE_CASES = [
+    ("ising_L8_tables", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 3, 0, 0.0, 0, 1),
+    ("ising_L16_tables_corr", 0, 16, -512.0, 516.0, 4.0, 4, 3, 20, 40, 17, 3, 0, 0.0, 0, 2),
+    ("ising_L12_bw8_tables_corr", 0, 12, -288.0, 296.0, 8.0, 4, 2, 10, 20, 3, 3, 0, 0.0, 0, 2),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", TABLE_CASES, ids=[c[0] for c in TABLE_CASES])
+def test_ising_on_the_global_table_kernel(engine_lib, oracle_lib, monkeypatch, case):
+    """The model-generic global-table kernel (k_sweep_tables) instantiated for Ising -- the
+    kernel an Ising window too large for shared memory runs on -- against the oracle."""
+    monkeypatch.setenv("REWL_SWEEP_VARIANT", "4")
+    _run_observables_case(engine_lib, oracle_lib, case)
+
+
+def _run_observables_case(engine_lib, oracle_lib, case):
     _, model, L, emin, emax, bw, nwin, R, se, sc, seed, cycles, wpw, sig, mask, obs_mode = case
     fields = None
     if sig > 0:
