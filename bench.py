@@ -58,7 +58,7 @@ WORKLOADS = {
                sigma_h=0.5, energy_min=-5120.0, energy_max=0.0, bin_width=0.05, num_windows=8, replicas_per_window=4,
                window_overlap=0.75, sweeps_per_exchange=100, sweeps_per_check=200, lnf_initial=1.0, lnf_final=1e-7,
                flatness="min >= 0.8 mean over visited bins", realizations=64,
-               bytes_per_flip=51, kernel="k_sweep_at", profile="sweep_at_L32_64real_rewl.md"),
+               bytes_per_flip=51, kernel="k_sweep_tables<AshkinTeller2dModel>", profile="sweep_at_L32_64real_rewl.md"),
 }
 
 
@@ -83,7 +83,7 @@ WORKLOADS["mixed"] = dict(
     name="mixed_ising_L16_24_32_48_x16win_x4_at_L24_K0.25_0.5_0.75_x32real_x8win_x4_rewl", model="mixed",
     components=_mixed_components(), sweeps_per_exchange=100, sweeps_per_check=200, lnf_initial=1.0,
     lnf_final=1e-8, flatness="min >= 0.8 mean over visited bins", realizations=1,
-    kernel="k_sweep_at + k_sweep_ising_bins (launch groups on concurrent streams)", profile="",
+    kernel="k_sweep_tables<AshkinTeller2dModel> + k_sweep_ising_bins (launch groups on concurrent streams)", profile="",
     graphs=1, autotune=1)
 for _c in WORKLOADS["mixed"]["components"]:
     _c["bytes_per_flip"] = 46 if _c["model"] == "ising2d" else 51
