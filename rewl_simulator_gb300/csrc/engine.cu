@@ -2009,9 +2009,14 @@ int upload_all(rewl_engine* e)
     return REWL_OK;
 }
 
-bool bins_eligible(const InstDev& I, const rewl_batch_desc& D)
+bool bins_eligible(const InstDev& I, const rewl_batch_desc& D, int max_window_bins)
 {
     if (I.model != REWL_MODEL_ISING2D || D.rng_mode != REWL_RNG_PHILOX) return false;
+    // the window table, with its guard bins, and the lattice live in shared memory (with the
+    // correlators also the bin counts and the row and column sums)
+    const size_t need = (size_t)(max_window_bins + 2 + 2 * kGuard) * 8 + I.N + 4096 +
+                        (D.observables == 2 ? (size_t)4 * (max_window_bins + 2) + 8 * I.L : 0);
+    if (need > 200 * 1024) return false;
     const int C = I.chunk;
     if (!(C == 32 || C == 24 || C == 16 || C == 8 || C == 4)) return false;
     const long long step = 4 * std::llabs(I.J_u);            // every energy change is a multiple of 4|J|
@@ -2071,7 +2076,9 @@ int plan_launches(rewl_engine* e)
     std::vector<Launch> plans;
     for (int s = 0; s < e->nslots; ++s) {
         const HostInst& H = e->inst[e->h_slot_inst[s]];
-        const int bins = bins_eligible(H.dev, e->desc) && getenv("REWL_SWEEP_VARIANT") == nullptr ? 1 : 0;
+        int max_nb = 0;
+        for (const auto& wd : H.wins) max_nb = std::max(max_nb, wd.nb);
+        const int bins = bins_eligible(H.dev, e->desc, max_nb) && getenv("REWL_SWEEP_VARIANT") == nullptr ? 1 : 0;
         Key k{H.d.model, bins, bins ? H.dev.chunk : 0, bins ? H.dev.N : 0};
         size_t idx = 0;
         for (; idx < keys.size(); ++idx)

@@ -254,3 +254,23 @@ def _run_observables_case(engine_lib, oracle_lib, case):
     finally:
         eng.close()
         orc.close()
+
+
+@pytest.mark.gpu
+def test_ising_window_too_large_for_shared_memory(engine_lib, oracle_lib):
+    """An Ising window of 36,865 bins (L = 96, one window over the whole spectrum at bin width 1)
+    does not fit in shared memory: the engine runs it on the global-table kernel, bit for bit
+    with the oracle."""
+    rg, po = engine_lib, oracle_lib
+    L, N = 96, 96 * 96
+    eng, orc = _pair(rg, po, 0, L, -2.0 * N, 2.0 * N + 4, 1.0, 1, 2, 5, 10, 41)
+    try:
+        shapes = eng.launch_shapes()
+        assert len(shapes) == 1 and shapes[0][1] == 0          # not the bin-tracking kernel
+        for k in range(2):
+            eng.run_cycles(1)
+            orc.cycle()
+            _compare(eng, orc, f"cycle {k}")
+    finally:
+        eng.close()
+        orc.close()
