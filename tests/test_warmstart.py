@@ -154,7 +154,7 @@ def test_gpu_warm_start_gain_over_plain_wang_landau(engine_lib):
     (residual over the L=16 ln g/N) predicts the L=32 windows: its error at injection is compared
     with the zero start of plain Wang-Landau, and plain WL (ln f0 = 1) is run until it is as
     accurate as the prediction was before a single flip; the warm-started run (ln f0 = 1e-4,
-    burn-in and stall fallback) gets the same number of intervals and must keep its accuracy."""
+    burn-in) must keep its accuracy over the intervals before its stall fallback could act."""
     rg = engine_lib
     from rewl_simulator_gb300.mlp import MLP
     e16 = _exact(16)
@@ -185,8 +185,9 @@ def test_gpu_warm_start_gain_over_plain_wang_landau(engine_lib):
                 if _max_err(plain, exact) <= err_warm0:
                     need, flips = k, st.attempted_flips
                     break
-            # plain WL spends at least two check intervals (13 M flips) to get where the network starts
-            assert need is None or need >= 2, (need, err_warm0)
+            # plain WL spends many check intervals (6.6 M flips each) to get where the network
+            # starts: 124 on a GB300 with these seeds
+            assert need is None or need >= 20, (need, err_warm0)
 
             errs = []
 
@@ -194,8 +195,12 @@ def test_gpu_warm_start_gain_over_plain_wang_landau(engine_lib):
                 errs.append(_max_err(e, exact))
                 return False
 
-            ws.run(warm, need or cap, stall_checks=40, burn_in=8, on_cycle=track)
+            # before any window could fall back to plain WL (which zeroes its ln g), the small
+            # ln f keeps the network's estimate: the error stays near its value at injection
+            stall = 40
+            ws.run(warm, min(need or cap, stall - 1), stall_checks=stall, burn_in=8, on_cycle=track)
             assert max(errs) <= 2.0 * err_warm0 + 0.5, (err_warm0, errs[:5], max(errs))
+            assert errs[-1] < err_warm0, (err_warm0, errs[-1])          # and it improves on it
     mlp.close()
     print(f"\nwarm start L=32: max|dlng| {err_warm0:.3f} at injection (zero start {err_zero:.1f}); "
-          f"plain WL needs {need} intervals ({flips} flips) to reach it; warm run after as many: {errs[-1]:.3f}")
+          f"plain WL needs {need} intervals ({flips} flips) to reach it; warm run after {len(errs)}: {errs[-1]:.3f}")
