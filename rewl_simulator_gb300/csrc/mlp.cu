@@ -1,18 +1,20 @@
 // Learned warm start: an MLP surrogate ln g(E)/N = f(E/N, 1/L, J, K, sigma_h,
 // window lo/N, window hi/N), trained and evaluated on the GPU with hand-written
-// BF16 tensor-core GEMMs (mma.sync m16n8k16, FP32 accumulation), a fused
-// bias + GELU epilogue, split-K weight gradients, and Adam on FP32 master weights.
+// BF16 tensor-core GEMMs (tcgen05.mma with the FP32 accumulator in tensor memory;
+// an mma.sync m16n8k16 kernel is kept for comparison), a fused bias + GELU
+// epilogue, split-K weight gradients, and Adam on FP32 master weights.
 //
 // Shapes: 7 inputs (padded to 64) -> 4 x 256 (GELU) -> 1 output (padded to 64).
 // A batch of 4096 is 4096 x 256 x 256 per hidden GEMM, i.e. latency-bound work.
-// The tiles are therefore small (64 x 64 x 32, four warps) so that a layer spans
-// ~256 blocks, and every GEMM of a step runs on one stream.
+// The tiles are therefore small (128 x 64 on tcgen05, 64 x 64 on mma.sync) so
+// that a layer spans many blocks, and every GEMM of a step runs on one stream.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -191,6 +193,278 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g)
             }
 }
 
+// ---------------------------------------------------------------------------
+// The same GEMM on the 5th-generation tensor cores (tcgen05), the default.
+//
+// One CTA computes a 128 x 64 tile of C.  Per K block of 64, the four warps copy
+// the A (128 x 64) and B (64 x 64) tiles into shared memory in the canonical
+// K-major layout without swizzle: 8 x 8 bf16 "core matrices" of 128 contiguous
+// bytes (8 rows of 16 B), the 8 core matrices along K of an 8-row group side by
+// side (128 B apart), and 8-row groups 1024 B apart.  Transposed sources are
+// transposed by the copy.  One thread then issues four tcgen05.mma (M 128, N 64,
+// K 16 each) from shared-memory descriptors into an FP32 accumulator in tensor
+// memory (64 columns, allocated per CTA) and commits them to an mbarrier.  Two
+// shared stages let the copy of block t+1 overlap the MMAs of block t.  The
+// epilogue reads the accumulator back with tcgen05.ld (warp w owns rows
+// 32w..32w+31, one row per thread) and applies the same epilogues as above.
+//
+// Every wait on an mbarrier is bounded: on a timeout the block records
+// kTcTimeout in g_tc_error, waits once more (bounded) for its MMAs, frees its
+// tensor memory and skips the epilogue.  Rows of A beyond M and K beyond the
+// split's end are zero-filled, so M need only be a multiple of 64.
+// ---------------------------------------------------------------------------
+namespace tc {
+constexpr int BM = 128, BN = 64, BK = 64, STAGES = 2;
+constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 64;   // + mbarriers and the tensor-memory address
+constexpr uint32_t kTmemCols = 64;                     // FP32 accumulator: 128 lanes x 64 columns
+constexpr uint32_t kLBO = 128;                         // next core matrix along K
+constexpr uint32_t kSBO = 1024;                        // next 8-row group
+// instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1),
+// both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+constexpr int kSpinLimit = 1 << 18;
+constexpr int kTcTimeout = 1;
+static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256 && BM == 128, "tcgen05.mma cta_group::1 kind::f16 shape");
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+}  // namespace tc
+
+__device__ int g_tc_error;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start >> 4 (bits 0-13), LBO >> 4 (16-29), SBO >> 4 (32-45),
+// descriptor version 1 (bits 46-47), base offset 0, no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
+{
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(tc::kLBO >> 4) << 16) | ((uint64_t)(tc::kSBO >> 4) << 32) |
+           (1ull << 46);
+}
+
+// byte offset of element (r, k) of a tile in the canonical K-major layout
+__device__ __forceinline__ int core_off(int r, int k) { return (r >> 3) * tc::kSBO + (k >> 3) * tc::kLBO + (r & 7) * 16 + (k & 7) * 2; }
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < tc::kSpinLimit; ++i) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// R rows x BK columns of K starting at (r0, k0) of a matrix whose row r, column k sits at
+// src[r * ld + k] (KMAJ) or src[k * ld + r] (!KMAJ); rows >= rmax and k >= kmax read zero.
+template <int R, bool KMAJ>
+__device__ __forceinline__ void load_tile(unsigned char* dst, const bf16* src, int ld, int r0, int rmax, int k0, int kmax,
+                                          int tid)
+{
+    for (int c = tid; c < R * (tc::BK / 8); c += 128) {
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        int r, kq;
+        if (KMAJ) {
+            // a quarter-warp covers 8 rows of one 16-byte column: 128 contiguous shared bytes
+            r = (c & 7) | ((c >> 6) << 3);
+            kq = (c >> 3) & 7;
+            const int gr = r0 + r, gk = k0 + kq * 8;
+            if (gr < rmax && gk < kmax) v = *reinterpret_cast<const uint4*>(src + (size_t)gr * ld + gk);
+        } else {
+            // consecutive threads take consecutive rows: each of the 8 loads is coalesced
+            r = c % R;
+            kq = c / R;
+            const int gr = r0 + r, gk = k0 + kq * 8;
+            if (gr < rmax) {
+                unsigned short e[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    e[i] = gk + i < kmax ? reinterpret_cast<const unsigned short*>(src)[(size_t)(gk + i) * ld + gr] : 0;
+                v = make_uint4(e[0] | (uint32_t)e[1] << 16, e[2] | (uint32_t)e[3] << 16, e[4] | (uint32_t)e[5] << 16,
+                               e[6] | (uint32_t)e[7] << 16);
+            }
+        }
+        *reinterpret_cast<uint4*>(dst + core_off(r, kq * 8)) = v;
+    }
+}
+
+template <bool A_KM, bool B_NK, int EPI>
+__global__ void __launch_bounds__(128) k_gemm_tc(const GemmArgs g)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + tc::STAGES * tc::STAGE_BYTES);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + tc::STAGES);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * tc::BM, n0 = blockIdx.x * tc::BN;
+    const int kb = blockIdx.z * g.k_per_split, ke = min(kb + g.k_per_split, g.K);
+    const int nk = (ke - kb + tc::BK - 1) / tc::BK;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" :: "r"(smem_u32(tslot)), "r"(tc::kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < tc::STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(bar + s)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+
+    bool ok = true;
+    int issued = 0;                                     // K blocks whose MMAs were committed
+    for (int t = 0; t < nk; ++t) {
+        const int st = t & 1;
+        if (t >= tc::STAGES) {                          // the MMAs that read this stage are done
+            const bool mine = mbar_wait(smem_u32(bar + st), (uint32_t)(((t - tc::STAGES) >> 1) & 1));
+            ok = __syncthreads_and(mine);
+            if (!ok) break;
+        }
+        unsigned char* As = sm + st * tc::STAGE_BYTES;
+        unsigned char* Bs = As + tc::A_BYTES;
+        const int k0 = kb + t * tc::BK;
+        load_tile<tc::BM, !A_KM>(As, g.A, g.lda, m0, g.M, k0, ke, tid);
+        load_tile<tc::BN, B_NK>(Bs, g.B, g.ldb, n0, g.N, k0, ke, tid);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");   // the copies, seen by the tensor cores
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+            for (int kk = 0; kk < tc::BK / 16; ++kk) {
+                const uint64_t ad = smem_desc(smem_u32(As + kk * 2 * tc::kLBO));
+                const uint64_t bd = smem_desc(smem_u32(Bs + kk * 2 * tc::kLBO));
+                const uint32_t accumulate = (t > 0 || kk > 0) ? 1u : 0u;
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                             :: "r"(tmem), "l"(ad), "l"(bd), "r"(tc::kIdesc), "r"(accumulate) : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" :: "r"(smem_u32(bar + st)) : "memory");
+        }
+        issued = t + 1;
+    }
+    if (issued > 0) {                                   // the last commit covers every earlier MMA
+        const int t = issued - 1;
+        const bool mine = mbar_wait(smem_u32(bar + (t & 1)), (uint32_t)((t >> 1) & 1));
+        const bool all = __syncthreads_and(mine);
+        if (!all && ok && tid == 0) atomicOr(&g_tc_error, tc::kTcTimeout);
+        if (!ok && tid == 0) atomicOr(&g_tc_error, tc::kTcTimeout);
+        ok = ok && all;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+    if (ok && issued > 0) {
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll
+        for (int c0 = 0; c0 < tc::BN; c0 += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (row < g.M) {
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+                const int col = n0 + c0;
+                const size_t o = (size_t)row * g.ldc + col;
+                if (EPI == EPI_F32) {
+                    if (gridDim.z > 1) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) atomicAdd(g.Cf + o + j, v[j]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; j += 4) *reinterpret_cast<float4*>(g.Cf + o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                    }
+                } else if (EPI == EPI_BIAS_GELU || EPI == EPI_BIAS_F32) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] += g.bias[col + j];
+#pragma unroll
+                    for (int j = 0; j < 16; j += 4) *reinterpret_cast<float4*>(g.Cf + o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                    if (EPI == EPI_BIAS_GELU) {
+                        uint32_t h[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const __nv_bfloat162 b2 = __floats2bfloat162_rn(gelu_f(v[2 * j]), gelu_f(v[2 * j + 1]));
+                            h[j] = *reinterpret_cast<const uint32_t*>(&b2);
+                        }
+                        *reinterpret_cast<uint4*>(g.Cb + o) = make_uint4(h[0], h[1], h[2], h[3]);
+                        *reinterpret_cast<uint4*>(g.Cb + o + 8) = make_uint4(h[4], h[5], h[6], h[7]);
+                    }
+                } else {
+                    uint32_t h[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                        h[j] = *reinterpret_cast<const uint32_t*>(&b2);
+                    }
+                    *reinterpret_cast<uint4*>(g.Cb + o) = make_uint4(h[0], h[1], h[2], h[3]);
+                    *reinterpret_cast<uint4*>(g.Cb + o + 8) = make_uint4(h[4], h[5], h[6], h[7]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(tc::kTmemCols) : "memory");
+    }
+}
+
+// REWL_MLP_GEMM=mma_sync selects the mma.sync kernel (kept for comparison)
+bool use_tcgen05()
+{
+    static const bool tc5 = [] {
+        const char* v = std::getenv("REWL_MLP_GEMM");
+        return !(v && std::strcmp(v, "mma_sync") == 0);
+    }();
+    return tc5;
+}
+
+template <bool A_KM, bool B_NK, int EPI>
+cudaError_t launch_gemm(cudaStream_t st, const GemmArgs& g, int splits)
+{
+    if (use_tcgen05()) {
+        static_assert(tc::BN == kBN, "tile widths agree");
+        k_gemm_tc<A_KM, B_NK, EPI><<<dim3(g.N / tc::BN, (g.M + tc::BM - 1) / tc::BM, splits), 128, tc::SMEM_BYTES, st>>>(g);
+    } else {
+        k_gemm<A_KM, B_NK, EPI><<<dim3(g.N / kBN, g.M / kBM, splits), 128, 0, st>>>(g);
+    }
+    return cudaGetLastError();
+}
+
+// The tensor-core GEMMs need more than the default 48 KB of dynamic shared memory.  Set
+// once per device when a network is created, so that launches made while a stream is
+// being captured (rewl_mlp_predict_noalloc) need no attribute call.
+cudaError_t prepare_tc_kernels()
+{
+    const void* kernels[] = {
+        reinterpret_cast<const void*>(k_gemm_tc<false, true, EPI_BIAS_GELU>),
+        reinterpret_cast<const void*>(k_gemm_tc<false, true, EPI_BIAS_F32>),
+        reinterpret_cast<const void*>(k_gemm_tc<true, false, EPI_F32>),
+        reinterpret_cast<const void*>(k_gemm_tc<false, false, EPI_BF16>),
+    };
+    for (const void* k : kernels) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// a bounded wait in a tensor-core GEMM ran out since the last call: report it once
+int take_tc_error()
+{
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_tc_error, sizeof v) != cudaSuccess) return mfail(REWL_EDEVICE, "reading the GEMM status failed");
+    if (!v) return REWL_OK;
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_tc_error, &zero, sizeof zero);
+    return mfail(REWL_EDEVICE, "a tensor-core GEMM timed out waiting for its MMAs (results discarded)");
+}
+
 // G = dY * gelu'(Z) (bf16), dY given in bf16
 __global__ void k_gelu_back(const bf16* dY, const float* Z, bf16* G, size_t n)
 {
@@ -333,10 +607,8 @@ int gemm(rewl_mlp* m, const bf16* A, const bf16* B, int M, int N, int K, int lda
 {
     if (M % kBM || N % kBN || K % (kBK * splits)) return mfail(REWL_EINVAL, "gemm shape %d x %d x %d (split %d)", M, N, K, splits);
     GemmArgs g{A, B, M, N, K, lda, ldb, K / splits, Cf, Cb, ldc, bias};
-    dim3 grid(N / kBN, M / kBM, splits);
-    k_gemm<A_KM, B_NK, EPI><<<grid, 128, 0, m->stream>>>(g);
     m->launches++;
-    MCUDA(cudaGetLastError());
+    MCUDA((launch_gemm<A_KM, B_NK, EPI>(m->stream, g, splits)));
     return REWL_OK;
 }
 
@@ -425,6 +697,7 @@ int rewl_mlp_create(int32_t device, int32_t hidden, int32_t layers, uint64_t see
     rewl_mlp* m = new rewl_mlp();
     m->device = device; m->hidden = hidden; m->layers = layers; m->seed = seed;
     if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) { delete m; return mfail(REWL_EDEVICE, "stream"); }
+    if (prepare_tc_kernels() != cudaSuccess) { m->release(); delete m; return mfail(REWL_EDEVICE, "tensor-core GEMM setup failed"); }
     for (int l = 0; l <= layers; ++l) {
         m->din.push_back(l == 0 ? kIn : hidden);
         m->dout.push_back(l == layers ? kOut : hidden);
@@ -535,6 +808,7 @@ int rewl_mlp_predict(rewl_mlp* m, const float* X, int32_t n, int32_t in_dim, flo
     std::vector<float> o((size_t)Bp * kOut);
     MCUDA(cudaMemcpyAsync(o.data(), m->out.p, o.size() * 4, cudaMemcpyDeviceToHost, m->stream));
     MCUDA(cudaStreamSynchronize(m->stream));
+    if ((rc = take_tc_error())) return rc;
     for (int i = 0; i < n; ++i) y[i] = o[(size_t)i * kOut];
     return REWL_OK;
 }
@@ -552,7 +826,7 @@ int rewl_mlp_gradient(rewl_mlp* m, const float* X, const float* y, int32_t n, in
     if ((rc = forward(m, n)) || (rc = backward(m, n))) return rc;
     MCUDA(cudaMemcpyAsync(loss, m->loss.p, 4, cudaMemcpyDeviceToHost, m->stream));
     MCUDA(cudaStreamSynchronize(m->stream));
-    return REWL_OK;
+    return take_tc_error();
 }
 
 // Load a training set (features n x in_dim, targets n) into device memory.
@@ -594,6 +868,7 @@ int rewl_mlp_train(rewl_mlp* m, int32_t steps, int32_t batch, float lr, float* l
         if (losses) MCUDA(cudaMemcpyAsync(&lh[s], m->loss.p, 4, cudaMemcpyDeviceToHost, m->stream));
     }
     MCUDA(cudaStreamSynchronize(m->stream));
+    if ((rc = take_tc_error())) return rc;
     if (losses) std::memcpy(losses, lh.data(), lh.size() * 4);
     return REWL_OK;
 }
@@ -683,8 +958,7 @@ cudaError_t noalloc_layer(cudaStream_t st, const bf16* A, const bf16* W, int M, 
                           const float* bias)
 {
     const GemmArgs g{A, W, M, N, K, K, K, K, Cf, Cb, N, bias};
-    k_gemm<false, true, EPI><<<dim3(N / kBN, M / kBM, 1), 128, 0, st>>>(g);
-    return cudaGetLastError();
+    return launch_gemm<false, true, EPI>(st, g, 1);
 }
 
 } // namespace

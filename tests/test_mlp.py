@@ -93,3 +93,42 @@ def test_gpu_training_fits_exact_lng(engine_lib):
     pred = m.predict(X)
     assert np.abs(pred - y).max() < 0.05
     m.close()
+
+
+_GRAD_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+from rewl_simulator_gb300.mlp import MLP
+rng = np.random.default_rng(4)
+m = MLP(hidden=256, layers=4, seed=9)
+X = rng.uniform(-1, 1, (1024, 7)).astype(np.float32)
+y = rng.uniform(0, 0.7, 1024).astype(np.float32)
+loss = m.gradient(X, y)
+np.savez(sys.argv[2], loss=loss, grads=m.grads(), pred=m.predict(X[:200]))
+m.close()
+"""
+
+
+@pytest.mark.gpu
+def test_gpu_tcgen05_gemm_matches_mma_sync(engine_lib, tmp_path):
+    """The tcgen05 GEMMs (default) against the mma.sync ones on one forward + backward with a
+    split-K weight gradient (batch 1024) and a prediction on 200 rows (a partial 128-row tile):
+    same BF16 operands and FP32 accumulation, so only the summation order differs."""
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT
+    out = {}
+    for kind in ("tcgen05", "mma_sync"):
+        env = dict(os.environ)
+        env.pop("REWL_MLP_GEMM", None)
+        if kind == "mma_sync":
+            env["REWL_MLP_GEMM"] = "mma_sync"
+        f = tmp_path / f"{kind}.npz"
+        subprocess.run([sys.executable, "-c", _GRAD_SCRIPT, str(ROOT), str(f)], env=env, check=True, timeout=300)
+        out[kind] = np.load(f)
+    a, b = out["tcgen05"], out["mma_sync"]
+    assert abs(float(a["loss"]) - float(b["loss"])) <= 1e-3 * abs(float(b["loss"]))
+    ga, gb = a["grads"].astype(np.float64), b["grads"].astype(np.float64)
+    assert np.linalg.norm(ga - gb) <= 1e-2 * np.linalg.norm(gb), np.linalg.norm(ga - gb) / np.linalg.norm(gb)
+    np.testing.assert_allclose(a["pred"], b["pred"], rtol=0, atol=2e-3)
