@@ -196,17 +196,22 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g)
 // ---------------------------------------------------------------------------
 // The same GEMM on the 5th-generation tensor cores (tcgen05), the default.
 //
-// One CTA computes a 128 x 64 tile of C.  Per K block of 64, the four warps copy
-// the A (128 x 64) and B (64 x 64) tiles into shared memory in the canonical
-// K-major layout without swizzle: 8 x 8 bf16 "core matrices" of 128 contiguous
-// bytes (8 rows of 16 B), the 8 core matrices along K of an 8-row group side by
-// side (128 B apart), and 8-row groups 1024 B apart.  Transposed sources are
-// transposed by the copy.  One thread then issues four tcgen05.mma (M 128, N 64,
-// K 16 each) from shared-memory descriptors into an FP32 accumulator in tensor
-// memory (64 columns, allocated per CTA) and commits them to an mbarrier.  Two
-// shared stages let the copy of block t+1 overlap the MMAs of block t.  The
-// epilogue reads the accumulator back with tcgen05.ld (warp w owns rows
-// 32w..32w+31, one row per thread) and applies the same epilogues as above.
+// One CTA computes a 128 x 64 tile of C.  Its K range is cut into blocks of 64
+// that stream through a ring of four shared-memory stages by cp.async (16-byte
+// copies, zero-filled outside the matrix), three blocks ahead of the one being
+// multiplied.  Tiles are kept in tcgen05's canonical layouts without swizzle:
+// "core matrices" of 8 rows x 16 B (128 contiguous bytes), the 8 core matrices
+// along K of an 8-wide group of rows (M or N) side by side (LBO = 128 B), groups
+// 1024 B apart (SBO).  An operand stored with K contiguous uses the K-major form
+// (a core row = 8 consecutive k of one row); one stored transposed, with M or N
+// contiguous, uses the MN-major form (a core row = 8 consecutive rows at one k)
+// and the transpose bit of the instruction descriptor, so every 16-byte chunk is
+// copied as it lies in global memory.  One thread issues four tcgen05.mma
+// (M 128, N 64, K 16 each) per block from shared-memory descriptors into an
+// FP32 accumulator in tensor memory (64 columns, allocated per CTA) and commits
+// them to the stage's mbarrier, which releases the stage for the block four
+// ahead.  The epilogue reads the accumulator back with tcgen05.ld (warp w owns
+// rows 32w..32w+31, one row per thread) and applies the same epilogues as above.
 //
 // Every wait on an mbarrier is bounded: on a timeout the block records
 // kTcTimeout in g_tc_error, waits once more (bounded) for its MMAs, frees its
@@ -214,15 +219,19 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g)
 // split's end are zero-filled, so M need only be a multiple of 64.
 // ---------------------------------------------------------------------------
 namespace tc {
-constexpr int BM = 128, BN = 64, BK = 64, STAGES = 2;
+constexpr int BM = 128, BN = 64, BK = 64, STAGES = 4;
 constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 64;   // + mbarriers and the tensor-memory address
 constexpr uint32_t kTmemCols = 64;                     // FP32 accumulator: 128 lanes x 64 columns
 constexpr uint32_t kLBO = 128;                         // next core matrix along K
 constexpr uint32_t kSBO = 1024;                        // next 8-row group
 // instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1),
-// both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+// A / B MN-major (transposed) in bits 15 / 16, N >> 3 in bits 17-22, M >> 4 in bits 24-28
+__host__ __device__ constexpr uint32_t idesc(bool a_mn, bool b_mn)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)b_mn << 16) |
+           ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
 constexpr int kSpinLimit = 1 << 18;
 constexpr int kTcTimeout = 1;
 static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256 && BM == 128, "tcgen05.mma cta_group::1 kind::f16 shape");
@@ -255,36 +264,32 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
     return false;
 }
 
-// R rows x BK columns of K starting at (r0, k0) of a matrix whose row r, column k sits at
-// src[r * ld + k] (KMAJ) or src[k * ld + r] (!KMAJ); rows >= rmax and k >= kmax read zero.
-template <int R, bool KMAJ>
-__device__ __forceinline__ void load_tile(unsigned char* dst, const bf16* src, int ld, int r0, int rmax, int k0, int kmax,
-                                          int tid)
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool in)
 {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" :: "r"(dst), "l"(src), "r"(in ? 16 : 0) : "memory");
+}
+
+// Copy R rows x BK columns of K starting at (r0, k0) into a stage at shared address dst.
+// KMAJ: row r, column k at src[r * ld + k], K-major layout.  !KMAJ: at src[k * ld + r],
+// MN-major layout.  Chunks with rows >= rmax or k >= kmax are filled with zeros.
+template <int R, bool KMAJ>
+__device__ __forceinline__ void issue_tile(uint32_t dst, const bf16* src, int ld, int r0, int rmax, int k0, int kmax, int tid)
+{
+#pragma unroll
     for (int c = tid; c < R * (tc::BK / 8); c += 128) {
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        int r, kq;
         if (KMAJ) {
             // a quarter-warp covers 8 rows of one 16-byte column: 128 contiguous shared bytes
-            r = (c & 7) | ((c >> 6) << 3);
-            kq = (c >> 3) & 7;
+            const int r = (c & 7) | ((c >> 6) << 3), kq = (c >> 3) & 7;
             const int gr = r0 + r, gk = k0 + kq * 8;
-            if (gr < rmax && gk < kmax) v = *reinterpret_cast<const uint4*>(src + (size_t)gr * ld + gk);
+            const bool in = gr < rmax && gk < kmax;
+            cp_async16(dst + core_off(r, kq * 8), in ? src + (size_t)gr * ld + gk : src, in);
         } else {
-            // consecutive threads take consecutive rows: each of the 8 loads is coalesced
-            r = c % R;
-            kq = c / R;
-            const int gr = r0 + r, gk = k0 + kq * 8;
-            if (gr < rmax) {
-                unsigned short e[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    e[i] = gk + i < kmax ? reinterpret_cast<const unsigned short*>(src)[(size_t)(gk + i) * ld + gr] : 0;
-                v = make_uint4(e[0] | (uint32_t)e[1] << 16, e[2] | (uint32_t)e[3] << 16, e[4] | (uint32_t)e[5] << 16,
-                               e[6] | (uint32_t)e[7] << 16);
-            }
+            // consecutive threads take consecutive 8-row groups of one k: coalesced
+            const int mg = c % (R / 8), k = c / (R / 8);
+            const int gr = r0 + mg * 8, gk = k0 + k;
+            const bool in = gr < rmax && gk < kmax;
+            cp_async16(dst + mg * tc::kSBO + (k >> 3) * tc::kLBO + (k & 7) * 16, in ? src + (size_t)gk * ld + gr : src, in);
         }
-        *reinterpret_cast<uint4*>(dst + core_off(r, kq * 8)) = v;
     }
 }
 
@@ -312,43 +317,54 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const GemmArgs g)
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = *tslot;
 
+    constexpr int S = tc::STAGES;
+    constexpr uint32_t kId = tc::idesc(A_KM, !B_NK);
+    const uint32_t sbase = smem_u32(sm);
+    auto issue = [&](int t) {                           // block t into stage t % S (an empty group past the end)
+        if (t < nk) {
+            const uint32_t As = sbase + (t % S) * tc::STAGE_BYTES;
+            const int k0 = kb + t * tc::BK;
+            issue_tile<tc::BM, !A_KM>(As, g.A, g.lda, m0, g.M, k0, ke, tid);
+            issue_tile<tc::BN, B_NK>(As + tc::A_BYTES, g.B, g.ldb, n0, g.N, k0, ke, tid);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+#pragma unroll
+    for (int t = 0; t < S - 1; ++t) issue(t);
+
     bool ok = true;
     int issued = 0;                                     // K blocks whose MMAs were committed
     for (int t = 0; t < nk; ++t) {
-        const int st = t & 1;
-        if (t >= tc::STAGES) {                          // the MMAs that read this stage are done
-            const bool mine = mbar_wait(smem_u32(bar + st), (uint32_t)(((t - tc::STAGES) >> 1) & 1));
-            ok = __syncthreads_and(mine);
+        if (t >= 1 && t + S - 1 < nk) {                 // block t+S-1 reuses the stage of block t-1
+            const int u = t - 1;
+            ok = __syncthreads_and(mbar_wait(smem_u32(bar + u % S), (uint32_t)((u / S) & 1)));
             if (!ok) break;
         }
-        unsigned char* As = sm + st * tc::STAGE_BYTES;
-        unsigned char* Bs = As + tc::A_BYTES;
-        const int k0 = kb + t * tc::BK;
-        load_tile<tc::BM, !A_KM>(As, g.A, g.lda, m0, g.M, k0, ke, tid);
-        load_tile<tc::BN, B_NK>(Bs, g.B, g.ldb, n0, g.N, k0, ke, tid);
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");   // the copies, seen by the tensor cores
+        issue(t + S - 1);
+        asm volatile("cp.async.wait_group %0;\n" :: "n"(S - 1) : "memory");     // block t has landed
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");           // ... and is seen by the tensor cores
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t As = sbase + (t % S) * tc::STAGE_BYTES, Bs = As + tc::A_BYTES;
 #pragma unroll
             for (int kk = 0; kk < tc::BK / 16; ++kk) {
-                const uint64_t ad = smem_desc(smem_u32(As + kk * 2 * tc::kLBO));
-                const uint64_t bd = smem_desc(smem_u32(Bs + kk * 2 * tc::kLBO));
+                const uint64_t ad = smem_desc(As + kk * 2 * tc::kLBO);
+                const uint64_t bd = smem_desc(Bs + kk * 2 * tc::kLBO);
                 const uint32_t accumulate = (t > 0 || kk > 0) ? 1u : 0u;
                 asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
-                             :: "r"(tmem), "l"(ad), "l"(bd), "r"(tc::kIdesc), "r"(accumulate) : "memory");
+                             :: "r"(tmem), "l"(ad), "l"(bd), "r"(kId), "r"(accumulate) : "memory");
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" :: "r"(smem_u32(bar + st)) : "memory");
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" :: "r"(smem_u32(bar + t % S)) : "memory");
         }
         issued = t + 1;
     }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");      // no copy outlives the block
     if (issued > 0) {                                   // the last commit covers every earlier MMA
         const int t = issued - 1;
-        const bool mine = mbar_wait(smem_u32(bar + (t & 1)), (uint32_t)((t >> 1) & 1));
-        const bool all = __syncthreads_and(mine);
-        if (!all && ok && tid == 0) atomicOr(&g_tc_error, tc::kTcTimeout);
-        if (!ok && tid == 0) atomicOr(&g_tc_error, tc::kTcTimeout);
+        const bool all = __syncthreads_and(mbar_wait(smem_u32(bar + t % S), (uint32_t)((t / S) & 1)));
+        if ((!ok || !all) && tid == 0) atomicOr(&g_tc_error, tc::kTcTimeout);
         ok = ok && all;
     }
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
