@@ -204,3 +204,43 @@ def test_gpu_warm_start_gain_over_plain_wang_landau(engine_lib):
     mlp.close()
     print(f"\nwarm start L=32: max|dlng| {err_warm0:.3f} at injection (zero start {err_zero:.1f}); "
           f"plain WL needs {need} intervals ({flips} flips) to reach it; warm run after {len(errs)}: {errs[-1]:.3f}")
+
+
+@pytest.mark.gpu
+def test_gpu_warm_start_ashkin_teller(engine_lib):
+    """The warm start on Ashkin-Teller (half spectrum, Baxter-field feature): five L=6 realisations
+    (K=0.5, h ~ N(0, 0.5^2)) run plain WL in one engine; a network trained on four of them
+    predicts the fifth, whose own plain-WL ln g judges it.  The prediction's shape error (ln g is
+    defined up to a constant) must be a small fraction of the zero start's."""
+    rg = engine_lib
+    from rewl_simulator_gb300.mlp import MLP
+    L, K, sh = 6, 0.5, 0.5
+    N = L * L
+    inss = [rg.Instance(model=rg.MODEL_ASHKIN_TELLER2D, L=L, K=K,
+                        fields=np.round(np.random.default_rng(200 + k).normal(0.0, sh, N) * 2**20) / 2**20,
+                        energy_min=-(2.0 + K) * 2 * N, energy_max=0.0, bin_width=0.25, num_windows=4,
+                        replicas_per_window=2, window_overlap=0.75, seed=31 + k) for k in range(5)]
+    batch = rg.Batch(instances=inss, sweeps_per_exchange=500, sweeps_per_check=2000, flatness_param=0.8,
+                     lnf_initial=1.0, lnf_final=1e-5, mask_mode=rg.MASK_VISITED)
+    with rg.Engine(batch) as eng:
+        eng.simulate(max_cycles=600)
+        rows = [ws.training_rows(eng, i, sigma_h=sh) for i in range(4)]
+        E, lng = eng.global_logdos(4, half_spectrum=True)
+        wins = [(lo, hi, ws.window_energies(eng, 4, w)) for w, (lo, hi, nb) in enumerate(eng.windows[4])]
+    X = np.concatenate([r[0] for r in rows])
+    y = np.concatenate([r[1] for r in rows])
+    mlp = MLP(hidden=256, layers=4, seed=11)
+    mlp.set_data(X, y)
+    losses = mlp.train(3000, batch=1024, lr=1e-3)
+    assert np.isfinite(losses).all()
+    pred = {}
+    for lo, hi, Ew in wins:
+        for e, v in zip(Ew, ws.predict_lng(mlp, Ew, L, 1.0, K, sh, lo, hi)):
+            pred.setdefault(round(float(e), 9), v)
+    mlp.close()
+    d = np.array([pred[round(float(e), 9)] for e in E]) - lng
+    err_warm = float(np.max(np.abs(d - d.mean())))
+    err_zero = float(np.max(np.abs(lng - lng.mean())))
+    print(f"\nAshkin-Teller L=6 warm start: shape error {err_warm:.3f} nats against {err_zero:.2f} for the zero start "
+          f"({len(E)} levels)")
+    assert err_warm < 0.15 * err_zero, (err_warm, err_zero)
