@@ -244,3 +244,38 @@ def test_gpu_warm_start_ashkin_teller(engine_lib):
     print(f"\nAshkin-Teller L=6 warm start: shape error {err_warm:.3f} nats against {err_zero:.2f} for the zero start "
           f"({len(E)} levels)")
     assert err_warm < 0.15 * err_zero, (err_warm, err_zero)
+
+
+def test_baseline_interpolates_monotone_pieces_and_sorts():
+    e = np.array([0.5, -1.0, 0.0, -2.0])
+    s = np.array([0.6, 0.4, 0.69, 0.0])
+    b = ws.Baseline(e, s)
+    np.testing.assert_allclose(b(np.array([-2.0, -1.0, 0.0, 0.5])), [0.0, 0.4, 0.69, 0.6], atol=1e-12)
+    x = np.linspace(-2.0, 0.0, 41)
+    assert np.all(np.diff(b(x)) >= -1e-12)                 # monotone data stays monotone (no overshoot)
+
+
+class RowsEngine(FakeEngine):
+    """A converged fake: ln g(E) = 0.01 E^2 on Ising levels, every other bin masked out."""
+
+    def global_logdos(self, i, half_spectrum=False):
+        E = np.arange(-128.0, 132.0, 4.0)
+        return E, 0.01 * E ** 2
+
+    def window_mask(self, i, w):
+        m = np.ones(self.windows[i][w][2], dtype=bool)
+        m[1::2] = False
+        return m
+
+
+def test_training_rows_take_masked_levels_and_subtract_the_baseline():
+    from rewl_simulator_gb300.mlp import features
+    eng = RowsEngine(2, {})
+    base = ws.Baseline(np.array([-2.0, 0.0, 2.0]), np.array([0.0, 0.1, 0.0]))
+    X, y = ws.training_rows(eng, 0, base=base)
+    n_expected = sum((nb + 1) // 2 for _, _, nb in eng.windows[0])
+    assert X.shape == (n_expected, 7) and y.shape == (n_expected,)
+    lo, hi, nb = eng.windows[0][0]
+    E = lo + 4.0 * np.arange(0, nb, 2)
+    np.testing.assert_allclose(X[:len(E)], features(E, 8, 1.0, 0.0, 0.0, lo, hi), rtol=1e-6)
+    np.testing.assert_allclose(y[:len(E)], 0.01 * E ** 2 / 64 - base(E / 64), rtol=1e-5, atol=1e-6)
