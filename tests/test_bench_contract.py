@@ -1,0 +1,46 @@
+"""bench.py's JSON line on the CPU: the reference arm (the oracle port in reference semantics on
+the host cores) prints one line with the contract's keys, and a rank other than 0 prints nothing."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+KEYS = {"metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+        "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"}
+
+
+def _run(args, env_extra=None):
+    env = dict(os.environ)
+    env.update(env_extra or {})
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), *args], cwd=ROOT, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return [l for l in r.stdout.splitlines() if l.startswith("{")]
+
+
+@pytest.mark.parametrize("workload", ["ising", "at"])
+def test_reference_arm_prints_the_contract_line(workload):
+    lines = _run(["--impl", "reference", "--steps", "1", "--warmup", "3", "--workload", workload])
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert KEYS <= set(d)
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "flips/s" and d["higher_is_better"] is True
+    assert d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1 and d["vs_baseline"] is None
+    assert d["config"]["workload"].startswith({"ising": "ising2d_L32", "at": "ashkin_teller2d_L32"}[workload])
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "flips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_print_nothing():
+    assert _run(["--impl", "reference", "--steps", "1", "--warmup", "3"], {"RANK": "1", "WORLD_SIZE": "2"}) == []
+
+
+def test_warmup_below_three_is_refused():
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--warmup", "2"], cwd=ROOT, capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode != 0 and "--warmup must be >= 3" in r.stderr
