@@ -212,15 +212,19 @@ def _ln_big(v: int) -> float:
 
 
 def brute_force_dos(L: int) -> dict[int, int]:
-    """Enumerate all 2^(L*L) configurations (L <= 5)."""
+    """Enumerate all 2^(L*L) configurations (L <= 5), 2^20 at a time: configuration x has spin
+    i = +1 where bit i is set, and E = sum over the 2N bonds of (+1 if the two bits differ, else -1)."""
     N = L * L
-    idx = np.arange(1 << N, dtype=np.int64)
-    E = np.zeros(1 << N, dtype=np.int64)
-    spins = [((idx >> i) & 1) * 2 - 1 for i in range(N)]
-    for y in range(L):
-        for x in range(L):
-            i = y * L + x
-            E -= spins[i] * spins[y * L + (x + 1) % L]
-            E -= spins[i] * spins[((y + 1) % L) * L + x]
-    vals, counts = np.unique(E, return_counts=True)
-    return {int(v): int(c) for v, c in zip(vals, counts)}
+    bonds = [(y * L + x, y * L + (x + 1) % L) for y in range(L) for x in range(L)] + \
+            [(y * L + x, ((y + 1) % L) * L + x) for y in range(L) for x in range(L)]
+    hist: dict[int, int] = {}
+    chunk = 1 << min(N, 20)
+    for base in range(0, 1 << N, chunk):
+        idx = np.arange(base, base + chunk, dtype=np.int64)
+        diff = np.zeros(chunk, dtype=np.int64)
+        for i, j in bonds:
+            diff += ((idx >> i) ^ (idx >> j)) & 1
+        vals, counts = np.unique(2 * diff - len(bonds), return_counts=True)
+        for v, c in zip(vals.tolist(), counts.tolist()):
+            hist[v] = hist.get(v, 0) + c
+    return hist

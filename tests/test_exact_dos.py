@@ -42,3 +42,13 @@ def test_exact_fixture_consistent(L):
         E2, lng2 = beale.exact_lng(L)
         np.testing.assert_array_equal(E, E2)
         np.testing.assert_allclose(lng, lng2, rtol=0, atol=1e-12)
+
+
+def test_brute_force_L5_identities():
+    """L = 5 (2^25 states, odd: no E -> -E symmetry): the low-energy counts that the identities
+    for L >= 5 state, checked by enumeration."""
+    bf = beale.brute_force_dos(5)
+    N = 25
+    assert sum(bf.values()) == 2 ** N
+    assert bf[-2 * N] == 2 and -2 * N + 4 not in bf
+    assert bf[-2 * N + 8] == 2 * N and bf[-2 * N + 12] == 4 * N and bf[-2 * N + 16] == N * N + 9 * N
