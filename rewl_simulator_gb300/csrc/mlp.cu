@@ -11,6 +11,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -58,7 +59,7 @@ constexpr int kOut = 64;       // padded output width
 //   B_NK = true:  B stored [N][K] (ldb = K);  false: B stored [K][N] (ldb = N)
 // M, N multiples of 64, K (per split) a multiple of 32.
 // Epilogues:
-//   EPI_F32:       C fp32 (atomicAdd when split over K)
+//   EPI_F32:       C fp32 (split over K: split z writes its partial at C + z * M * ldc)
 //   EPI_BIAS_GELU: Z = acc + bias -> Zout (fp32), Y = gelu(Z) -> Yout (bf16)
 //   EPI_BIAS_F32:  acc + bias -> fp32
 //   EPI_BF16:      acc -> bf16
@@ -179,8 +180,9 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g)
                 float v0 = acc[i][j][2 * h], v1 = acc[i][j][2 * h + 1];
                 const size_t o = (size_t)row * g.ldc + col;
                 if (EPI == EPI_F32) {
-                    if (gridDim.z > 1) { atomicAdd(g.Cf + o, v0); atomicAdd(g.Cf + o + 1, v1); }
-                    else { g.Cf[o] = v0; g.Cf[o + 1] = v1; }
+                    // a K split stores its partial product in its own slice (summed in order afterwards)
+                    float* c = g.Cf + (size_t)blockIdx.z * g.M * g.ldc;
+                    c[o] = v0; c[o + 1] = v1;
                 } else if (EPI == EPI_BIAS_GELU) {
                     v0 += g.bias[col]; v1 += g.bias[col + 1];
                     g.Cf[o] = v0; g.Cf[o + 1] = v1;
@@ -387,13 +389,10 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const GemmArgs g)
                 const int col = n0 + c0;
                 const size_t o = (size_t)row * g.ldc + col;
                 if (EPI == EPI_F32) {
-                    if (gridDim.z > 1) {
+                    // a K split stores its partial product in its own slice (summed in order afterwards)
+                    float* c = g.Cf + (size_t)blockIdx.z * g.M * g.ldc;
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) atomicAdd(g.Cf + o + j, v[j]);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 16; j += 4) *reinterpret_cast<float4*>(g.Cf + o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-                    }
+                    for (int j = 0; j < 16; j += 4) *reinterpret_cast<float4*>(c + o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
                 } else if (EPI == EPI_BIAS_GELU || EPI == EPI_BIAS_F32) {
 #pragma unroll
                     for (int j = 0; j < 16; ++j) v[j] += g.bias[col + j];
@@ -492,25 +491,55 @@ __global__ void k_gelu_back(const bf16* dY, const float* Z, bf16* G, size_t n)
     G[i] = __float2bfloat16_rn(__bfloat162float(dY[i]) * (cdf + z * pdf));
 }
 
-// column sums over the batch: db[n] += sum_b G[b][n]
-__global__ void k_colsum(const bf16* G, int B, int N, float* db)
+constexpr int kColChunk = 256;                                 // rows per column-sum partial
+
+// column sums over chunks of kColChunk rows: part[chunk][n] = sum_{b in chunk} G[b][n]
+__global__ void k_colsum(const bf16* G, int B, int N, float* part)
 {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    const int b0 = blockIdx.y * 256;
+    const int b0 = blockIdx.y * kColChunk;
     if (n >= N) return;
     float s = 0.f;
-    for (int b = b0; b < b0 + 256 && b < B; ++b) s += __bfloat162float(G[(size_t)b * N + n]);
-    atomicAdd(db + n, s);
+    for (int b = b0; b < b0 + kColChunk && b < B; ++b) s += __bfloat162float(G[(size_t)b * N + n]);
+    part[(size_t)blockIdx.y * N + n] = s;
 }
 
-// loss gradient of 0.5 * mean((out[:,0] - y)^2) * 2 = mean squared error
-__global__ void k_loss_grad(const float* out, const float* y, int B, bf16* dOut, float* loss)
+// dst[i] = sum_p parts[p * stride + i], p in order: gradients are reproducible run to run
+__global__ void k_sum_parts(const float* parts, int nparts, size_t stride, size_t n, float* dst)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int p = 0; p < nparts; ++p) s += parts[(size_t)p * stride + i];
+    dst[i] = s;
+}
+
+int weight_splits(int B) { return B >= 4096 ? 16 : (B >= 1024 ? 4 : 1); }
+
+// loss gradient of the mean squared error mean((out[:,0] - y)^2); each row's share of the loss
+// goes to rows[b] (summed in a fixed order by k_loss_sum)
+__global__ void k_loss_grad(const float* out, const float* y, int B, bf16* dOut, float* rows)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     const float e = out[(size_t)b * kOut] - y[b];
     for (int c = 0; c < kOut; ++c) dOut[(size_t)b * kOut + c] = __float2bfloat16_rn(c == 0 ? 2.0f * e / (float)B : 0.f);
-    atomicAdd(loss, e * e / (float)B);
+    rows[b] = e * e / (float)B;
+}
+
+// loss = sum of rows[0..B): one block of 256 threads, strided partial sums, then a fixed tree
+__global__ void __launch_bounds__(256) k_loss_sum(const float* rows, int B, float* loss)
+{
+    __shared__ float part[256];
+    float s = 0.f;
+    for (int b = threadIdx.x; b < B; b += 256) s += rows[b];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *loss = part[0];
 }
 
 // Adam on fp32 masters; refresh the bf16 copy.  mask zeroes the padded entries.
@@ -573,7 +602,8 @@ struct rewl_mlp {
     // activations for the current batch
     std::vector<Buf<bf16>> H;         // H[0] = input (B x 32), H[l+1] = gelu(Z_l)
     std::vector<Buf<float>> Z;        // pre-activations (hidden layers)
-    Buf<float> out, yb, loss;
+    Buf<float> out, yb, loss, lossrow;
+    Buf<float> Part;                  // per-split weight-gradient and per-chunk bias-gradient partials
     Buf<bf16> dOut, dH, G;
     Buf<bf16> Xall;
     Buf<float> yall;
@@ -587,7 +617,8 @@ struct rewl_mlp {
         P.release(); Mm.release(); Vm.release(); Gr.release(); Mask.release(); Pb.release();
         for (auto& h : H) h.release();
         for (auto& z : Z) z.release();
-        out.release(); yb.release(); loss.release(); dOut.release(); dH.release(); G.release();
+        out.release(); yb.release(); loss.release(); lossrow.release(); dOut.release(); dH.release(); G.release();
+        Part.release();
         Xall.release(); yall.release();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
@@ -601,7 +632,8 @@ int ensure_batch(rewl_mlp* m, int B)
     if (B <= m->batch_cap) return REWL_OK;
     for (auto& h : m->H) h.release();
     for (auto& z : m->Z) z.release();
-    m->out.release(); m->yb.release(); m->dOut.release(); m->dH.release(); m->G.release();
+    m->out.release(); m->yb.release(); m->dOut.release(); m->dH.release(); m->G.release(); m->Part.release();
+    m->lossrow.release();
     m->H.assign(m->layers + 1, Buf<bf16>());
     m->Z.assign(m->layers, Buf<float>());
     int rc;
@@ -613,6 +645,10 @@ int ensure_batch(rewl_mlp* m, int B)
     if ((rc = m->out.alloc((size_t)B * kOut)) || (rc = m->yb.alloc(B)) || (rc = m->dOut.alloc((size_t)B * kOut)) ||
         (rc = m->dH.alloc((size_t)B * m->hidden)) || (rc = m->G.alloc((size_t)B * m->hidden)))
         return rc;
+    const size_t wmax = (size_t)std::max(m->hidden, std::max(kIn, kOut)) * m->hidden;     // largest weight block
+    const size_t part = std::max((size_t)weight_splits(B) * wmax,
+                                 (size_t)((B + kColChunk - 1) / kColChunk) * std::max(m->hidden, kOut));
+    if ((rc = m->Part.alloc(part)) || (rc = m->lossrow.alloc(B))) return rc;
     m->batch_cap = B;
     return REWL_OK;
 }
@@ -644,22 +680,48 @@ int forward(rewl_mlp* m, int B)
                                            1, m->out.p, nullptr, kOut, m->P.p + m->boff[L]);
 }
 
-// backward of the mean squared error on m->yb; gradients accumulate into Gr (zeroed here)
+// dW (M x N, rows of N) = A^T H over the batch (A stored B x M, H stored B x N), split over the
+// batch when it is large; the splits' partial products are summed in a fixed order
+int weight_grad(rewl_mlp* m, const bf16* A, const bf16* H, int M, int N, int B, float* dst)
+{
+    const int splits = weight_splits(B);
+    int rc;
+    if ((rc = gemm<true, false, EPI_F32>(m, A, H, M, N, B, M, N, splits, splits > 1 ? m->Part.p : dst, nullptr, N, nullptr)))
+        return rc;
+    if (splits > 1) {
+        const size_t n = (size_t)M * N;
+        k_sum_parts<<<(unsigned)((n + 255) / 256), 256, 0, m->stream>>>(m->Part.p, splits, n, n, dst);
+        m->launches++;
+        MCUDA(cudaGetLastError());
+    }
+    return REWL_OK;
+}
+
+// db (N) = column sums of G (B x N): per-chunk partials, then their ordered sum
+int bias_grad(rewl_mlp* m, const bf16* G, int B, int N, float* dst)
+{
+    const int chunks = (B + kColChunk - 1) / kColChunk;
+    k_colsum<<<dim3((N + 127) / 128, chunks), 128, 0, m->stream>>>(G, B, N, m->Part.p);
+    k_sum_parts<<<(unsigned)((N + 255) / 256), 256, 0, m->stream>>>(m->Part.p, chunks, (size_t)N, (size_t)N, dst);
+    m->launches += 2;
+    MCUDA(cudaGetLastError());
+    return REWL_OK;
+}
+
+// backward of the mean squared error on m->yb; every gradient entry is written once into Gr
+// (zeroed here, so that padding entries stay zero)
 int backward(rewl_mlp* m, int B)
 {
     MCUDA(cudaMemsetAsync(m->Gr.p, 0, m->nparams * sizeof(float), m->stream));
-    MCUDA(cudaMemsetAsync(m->loss.p, 0, sizeof(float), m->stream));
-    k_loss_grad<<<(B + 127) / 128, 128, 0, m->stream>>>(m->out.p, m->yb.p, B, m->dOut.p, m->loss.p);
-    m->launches++;
+    k_loss_grad<<<(B + 127) / 128, 128, 0, m->stream>>>(m->out.p, m->yb.p, B, m->dOut.p, m->lossrow.p);
+    k_loss_sum<<<1, 256, 0, m->stream>>>(m->lossrow.p, B, m->loss.p);
+    m->launches += 2;
     const int L = m->layers;
-    const int splits = B >= 4096 ? 16 : (B >= 1024 ? 4 : 1);
     int rc;
     // output layer: dW = dOut^T H_L, db = colsum(dOut), dH = dOut W
-    if ((rc = gemm<true, false, EPI_F32>(m, m->dOut.p, m->H[L].p, kOut, m->hidden, B, kOut, m->hidden, splits,
-                                         m->Gr.p + m->woff[L], nullptr, m->hidden, nullptr)))
+    if ((rc = weight_grad(m, m->dOut.p, m->H[L].p, kOut, m->hidden, B, m->Gr.p + m->woff[L])) ||
+        (rc = bias_grad(m, m->dOut.p, B, kOut, m->Gr.p + m->boff[L])))
         return rc;
-    k_colsum<<<dim3((kOut + 127) / 128, (B + 255) / 256), 128, 0, m->stream>>>(m->dOut.p, B, kOut, m->Gr.p + m->boff[L]);
-    m->launches++;
     if ((rc = gemm<false, false, EPI_BF16>(m, m->dOut.p, m->Pb.p + m->woff[L], B, m->hidden, kOut, kOut, m->hidden, 1,
                                            nullptr, m->dH.p, m->hidden, nullptr)))
         return rc;
@@ -667,12 +729,9 @@ int backward(rewl_mlp* m, int B)
         const size_t n = (size_t)B * m->hidden;
         k_gelu_back<<<(unsigned)((n + 255) / 256), 256, 0, m->stream>>>(m->dH.p, m->Z[l].p, m->G.p, n);
         m->launches++;
-        if ((rc = gemm<true, false, EPI_F32>(m, m->G.p, m->H[l].p, m->dout[l], m->din[l], B, m->dout[l], m->din[l],
-                                             splits, m->Gr.p + m->woff[l], nullptr, m->din[l], nullptr)))
+        if ((rc = weight_grad(m, m->G.p, m->H[l].p, m->dout[l], m->din[l], B, m->Gr.p + m->woff[l])) ||
+            (rc = bias_grad(m, m->G.p, B, m->dout[l], m->Gr.p + m->boff[l])))
             return rc;
-        k_colsum<<<dim3((m->dout[l] + 127) / 128, (B + 255) / 256), 128, 0, m->stream>>>(m->G.p, B, m->dout[l],
-                                                                                          m->Gr.p + m->boff[l]);
-        m->launches++;
         if (l > 0)
             if ((rc = gemm<false, false, EPI_BF16>(m, m->G.p, m->Pb.p + m->woff[l], B, m->din[l], m->dout[l], m->dout[l],
                                                    m->din[l], 1, nullptr, m->dH.p, m->din[l], nullptr)))

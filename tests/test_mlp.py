@@ -132,3 +132,23 @@ def test_gpu_tcgen05_gemm_matches_mma_sync(engine_lib, tmp_path):
     ga, gb = a["grads"].astype(np.float64), b["grads"].astype(np.float64)
     assert np.linalg.norm(ga - gb) <= 1e-2 * np.linalg.norm(gb), np.linalg.norm(ga - gb) / np.linalg.norm(gb)
     np.testing.assert_allclose(a["pred"], b["pred"], rtol=0, atol=2e-3)
+
+
+@pytest.mark.gpu
+def test_gpu_training_is_reproducible(engine_lib):
+    """The same seed and data give bit-identical parameters and losses: split-K weight gradients,
+    bias column sums and the loss are summed in a fixed order (no atomics)."""
+    from rewl_simulator_gb300.mlp import MLP
+    rng = np.random.default_rng(2)
+    X = rng.uniform(-1, 1, (6000, 7)).astype(np.float32)
+    y = rng.uniform(0, 0.7, 6000).astype(np.float32)
+    for batch in (1024, 4096):
+        runs = []
+        for _ in range(2):
+            m = MLP(hidden=256, layers=4, seed=13)
+            m.set_data(X, y)
+            losses = m.train(30, batch=batch)
+            runs.append((m.params(), np.asarray(losses)))
+            m.close()
+        assert np.array_equal(runs[0][0], runs[1][0]), batch
+        assert np.array_equal(runs[0][1], runs[1][1]), batch
