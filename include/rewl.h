@@ -146,6 +146,16 @@ int rewl_import_dofs(rewl_engine* eng, int32_t walker, const int8_t* dofs, int32
  * (src/Hamiltonians/Ashkin_Teller2d/ashkin_teller2d_hamiltonian.hpp:159-165). */
 int rewl_import_disorder(rewl_engine* eng, int32_t instance, const double* fields);
 
+/* Random fields as the reference draws them (Disorder::generate_random_field,
+ * src/Hamiltonians/Disorder/random_fields.hpp:41-75, with its Gaussian from
+ * random_number_generator::get_gaussian, src/util/random_number_generators.hpp:33-57),
+ * seeded by the caller instead of the clock: num_sites doubles into out, Gaussian with
+ * standard deviation `strength` or uniform on [-2 strength, 2 strength].  Host only (no
+ * device needed); feed the result to rewl_instance_desc.fields or rewl_import_disorder. */
+#define REWL_DISORDER_UNIFORM 0     /* disorder_distribution::uniform */
+#define REWL_DISORDER_GAUSSIAN 1    /* disorder_distribution::gaussian */
+int rewl_generate_fields(uint64_t seed, double strength, int32_t distribution, int64_t num_sites, double* out);
+
 /* Set the logDoS of every replica of a window (warm start); values are rounded
  * to the engine's 2^-40 grid.  No reference counterpart (the reference starts at 0,
  * src/REWL/rewl_histograms.hpp:42-50). */

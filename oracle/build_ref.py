@@ -118,8 +118,8 @@ def build(model: str, L: int, bw: float, K: float = 0.5, fields: bool = True, fo
         raise FileNotFoundError(f"reference sources not found under {REF}")
     t = tag(model, L, bw, K, fields, corr)
     so = OUT / f"libref_{t}.so"
-    if so.exists() and not force:
-        return so
+    if so.exists() and not force and so.stat().st_mtime >= (HERE / "ref_harness.cpp").stat().st_mtime:
+        return so                                   # built, and not older than the harness source
     gen = OUT / "gen" / t
     stub = OUT / "stub"
     gen.mkdir(parents=True, exist_ok=True)

@@ -29,6 +29,7 @@
 #include <rewl_walker.hpp>
 #include <glazier.hpp>
 #include <array_shift.hpp>
+#include <Disorder/random_fields.hpp>
 
 // Exact bin index for dyadic energies: bin = floor((E - min) * inv_width) where
 // inv_width is an integer (20 for a 0.05 bin).  Energies and window edges are
@@ -131,6 +132,24 @@ void ref_walker_get_obs(void* w, double* out)
 {
     const auto& o = static_cast<walker_t*>(w)->system_obs;
     std::memcpy(out, o.obs_array, sizeof(double) * o.num_bins * convert(System_Obs_enum_t::NUM_OBS));
+}
+
+// The reference's disorder generator, generate_random_field
+// (src/Hamiltonians/Disorder/random_fields.hpp:41-75), run from a given seed instead of the clock:
+// per site WAIT_BETWEEN_FIELD_GENERATION discarded values, then the kept one, drawn by the
+// reference's own gaussian_random_field / uniform_random_field (:27-38).  type follows its
+// disorder_distribution enum (0 uniform, 1 gaussian).
+void ref_random_fields(uint64_t seed, double strength, int type, size_t n, double* out)
+{
+    random_number_generator<double> rng(seed);
+    double (*gen)(random_number_generator<double>&, const double) =
+        type == disorder_distribution::uniform ? &uniform_random_field<double> : &gaussian_random_field<double>;
+    for (size_t i = 0; i != n; ++i) {
+        double h = 0.;
+        for (size_t r = 0; r != WAIT_BETWEEN_FIELD_GENERATION; ++r) h = gen(rng, strength);
+        (void)h;
+        out[i] = gen(rng, strength);
+    }
 }
 
 // Uniforms drawn by the reference's generator with a given seed (the stream a

@@ -88,6 +88,7 @@ def _declare(L: C.CDLL) -> None:
         "rewl_window_info": [vp, i32, i32, vp, vp, vp],
         "rewl_import_dofs": [vp, i32, vp, i32],
         "rewl_import_disorder": [vp, i32, vp],
+        "rewl_generate_fields": [u64, C.c_double, i32, i64, vp],
         "rewl_set_logdos": [vp, i32, i32, vp],
         "rewl_set_lnf": [vp, i32, i32, C.c_double],
         "rewl_set_uniform_stream": [vp, i32, vp, sz],

@@ -42,6 +42,7 @@
 #include <iomanip>
 #include <limits>
 #include <new>
+#include <random>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -2474,6 +2475,43 @@ int rewl_import_dofs(rewl_engine* e, int32_t w, const int8_t* dofs, int32_t flav
     const WinDev& W = e->h_wins[e->h_slot_win[w]];
     const int64_t gb = (((E - I.eglo_u) * I.bin_mul) >> I.bin_shift) - W.gblo;
     if (gb < 0 || gb >= W.nb) return fail(REWL_EINVAL, "imported configuration has energy outside the walker's window");
+    return REWL_OK;
+}
+
+// Random fields drawn as the reference's Disorder::generate_random_field does
+// (src/Hamiltonians/Disorder/random_fields.hpp:41-75), from the given seed instead of the
+// clock.  One std::mt19937_64 stream read through std::uniform_real_distribution<double>(0, 1)
+// (random_number_generator, src/util/random_number_generators.hpp:14-31); for every site 20
+// values are drawn and discarded, then one is kept.  Uniform: 2 h (2u - 1).  Gaussian
+// (get_gaussian, :33-57): Box-Muller on (u, v), both redrawn while u <= DBL_EPSILON; a third
+// uniform keeps the cosine value when below 1/2, else the sine value, combined as the
+// reference combines them (z0 * c + z1 * !c) so that the doubles agree bit for bit.
+int rewl_generate_fields(uint64_t seed, double strength, int32_t distribution, int64_t num_sites, double* out)
+{
+    if (num_sites < 0 || (num_sites > 0 && !out)) return fail(REWL_EINVAL, "num_sites must be >= 0 and out non-null");
+    if (distribution != REWL_DISORDER_UNIFORM && distribution != REWL_DISORDER_GAUSSIAN)
+        return fail(REWL_EINVAL, "distribution must be REWL_DISORDER_UNIFORM or REWL_DISORDER_GAUSSIAN");
+    std::mt19937_64 gen(seed);
+    std::uniform_real_distribution<double> unit(0.0, 1.0);
+    const double two_pi = 2.0 * std::acos(-1.0);
+    auto draw = [&]() -> double {
+        if (distribution == REWL_DISORDER_UNIFORM) return 2.0 * strength * (-1.0 + 2.0 * unit(gen));
+        double u = unit(gen), v = unit(gen);
+        while (u <= std::numeric_limits<double>::epsilon()) {
+            u = unit(gen);
+            v = unit(gen);
+        }
+        const double r = strength * std::sqrt(-2.0 * std::log(u));
+        const double z0 = r * std::cos(two_pi * v) + 0.0;
+        const double z1 = r * std::sin(two_pi * v) + 0.0;
+        const bool c = unit(gen) < 0.5;
+        return z0 * c + z1 * !c;
+    };
+    constexpr int kDiscarded = 20;
+    for (int64_t i = 0; i < num_sites; ++i) {
+        for (int k = 0; k < kDiscarded; ++k) (void)draw();
+        out[i] = draw();
+    }
     return REWL_OK;
 }
 

@@ -32,6 +32,8 @@ MASK_STATIC = 0
 MASK_VISITED = 1
 RNG_PHILOX = 0
 RNG_REPLAY = 1
+DISORDER_UNIFORM = 0        # REWL_DISORDER_*: the reference's disorder_distribution
+DISORDER_GAUSSIAN = 1
 
 
 class REWLError(RuntimeError):
@@ -130,6 +132,19 @@ class Status:
 
 def _p(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def generate_fields(seed: int, strength: float, num_sites: int, distribution: int = DISORDER_GAUSSIAN) -> np.ndarray:
+    """Random fields drawn as the reference's Disorder::generate_random_field draws them
+    (src/Hamiltonians/Disorder/random_fields.hpp:41-75), from `seed` instead of the clock:
+    Gaussian with standard deviation `strength`, or uniform on [-2 strength, 2 strength].
+    Host only; the result goes to Instance.fields (which rounds it to multiples of 2^-20)."""
+    lib = _native.load()
+    out = np.zeros(int(num_sites), dtype=np.float64)
+    rc = lib.rewl_generate_fields(int(seed), float(strength), int(distribution), int(num_sites), _p(out))
+    if rc != 0:
+        raise REWLError(rc, lib.rewl_last_error_string().decode())
+    return out
 
 
 def obs_columns(model: int, observables: int) -> int:

@@ -190,6 +190,20 @@ def gen_rng():
     print("wrote ref_uniforms.json")
 
 
+def gen_fields():
+    """The reference's random-field generator (Disorder::generate_random_field) from fixed seeds."""
+    so = build_ref.build("ising", 8, 4.0)
+    ref = pyoracle.RefWalker(so, -128, -20, 4.0, 27, 1)
+    import ctypes as C
+    cases = []
+    for seed, strength, kind, n in ((1, 0.5, 1, 50), (2024, 1.25, 1, 50), (3141592653, 0.25, 0, 50), (7, 2.0, 0, 50)):
+        h = np.zeros(n)
+        ref.lib.ref_random_fields(seed, strength, kind, n, h.ctypes.data_as(C.c_void_p))
+        cases.append(dict(seed=seed, strength=strength, distribution=kind, fields=[float(x).hex() for x in h]))
+    (OUT / "random_fields.json").write_text(json.dumps(cases, indent=1))
+    print("wrote random_fields.json")
+
+
 def gen_normalize():
     so = build_ref.build("ising", 8, 4.0)
     ref = pyoracle.RefWalker(so, -128, -20, 4.0, 27, 1)
@@ -307,7 +321,7 @@ def gen_cumulants():
 
 
 if __name__ == "__main__":
-    groups = sys.argv[1:] or ["replay", "replay_corr", "glazier", "rng", "normalize", "exact", "thermo", "cumulants",
-                              "writers"]
+    groups = sys.argv[1:] or ["replay", "replay_corr", "glazier", "rng", "fields", "normalize", "exact", "thermo",
+                              "cumulants", "writers"]
     for g in groups:
         globals()[f"gen_{g}"]()
