@@ -153,3 +153,63 @@ def test_oracle_windows_equal_reference_glazier(oracle_lib):
             mn, mx, lo, nb = orc.windows[k]
             assert (mn, mx, nb) == (cases[name]["mins"][k], cases[name]["maxs"][k], cases[name]["nbins"][k]), (name, k)
         orc.close()
+
+
+@pytest.mark.parametrize("semantics", ["reference", "engine"])
+@pytest.mark.parametrize("one_over_t", [0, 1])
+def test_oracle_converges_to_the_exact_dos(oracle_lib, semantics, one_over_t):
+    """The oracle on its own, end to end: Ising L = 4, one window over the whole spectrum with two
+    replicas (flatness 0.8, count-weighted averaging, halving or 1/t) down to ln f < 1e-6; the
+    window's ln g, shifted to sum g = 2^N over the valid levels, against Beale's exact count."""
+    po = oracle_lib
+    from oracle import beale
+    sem = po.SEM_REFERENCE if semantics == "reference" else po.SEM_ENGINE
+    seed = 2 if semantics == "reference" else 1         # seeds that avoid the orbit of the test below
+    cfg = po.Config(model=po.MODEL_ISING, L=4, nwin=1, R=2, sweeps_per_exchange=100, sweeps_per_check=200,
+                    emin=-32.0, emax=36.0, bw=4.0, lnf_final=1e-6, one_over_t=one_over_t, semantics=sem, seed=seed)
+    orc = po.Oracle(cfg)
+    for _ in range(20000):
+        orc.cycle()
+        if orc.all_done():
+            break
+    assert orc.all_done()
+    g, mask = orc.window_logdos(0), orc.window_mask(0)
+    orc.close()
+    exact = np.array([np.log(v) if v else -np.inf for v in beale.exact_dos(4)])    # E = -32, -28, ..., 32
+    valid = mask[:len(exact)].astype(bool)
+    assert np.array_equal(valid, np.isfinite(exact))
+    lng = g[:len(exact)][valid]
+    m = lng.max()
+    lng = lng - (m + np.log(np.exp(lng - m).sum())) + 16 * np.log(2.0)
+    # halving saturates near 0.1 at this size; 1/t keeps improving
+    assert np.max(np.abs(lng - exact[valid])) < (0.03 if one_over_t else 0.1)
+
+
+@pytest.mark.parametrize("semantics,seed", [("reference", 1), ("engine", 4)])
+def test_sequential_sweep_can_lock_into_a_global_flip_orbit(oracle_lib, semantics, seed):
+    """A property of the reference's algorithm, kept by the oracle (and bit for bit by the engine):
+    a walker sweeping the sites in a fixed order can reach a configuration from which every
+    proposal of a sweep is level or downhill in ln g.  The sweep then flips every spin, ending in
+    the global flip of the lattice (same energies), and adds the same visits to two or four levels,
+    whose ln g grow together, so the orbit repeats and ln f stays at 1.  At L = 4 with one window
+    over the spectrum some seeds reach it in both semantics (the convergence test avoids them)."""
+    po = oracle_lib
+    sem = po.SEM_REFERENCE if semantics == "reference" else po.SEM_ENGINE
+    cfg = po.Config(model=po.MODEL_ISING, L=4, nwin=1, R=2, sweeps_per_exchange=100, sweeps_per_check=200,
+                    emin=-32.0, emax=36.0, bw=4.0, lnf_final=1e-6, semantics=sem, seed=seed)
+    orc = po.Oracle(cfg)
+    for _ in range(50):
+        orc.cycle()
+    assert not orc.all_done() and orc.lnf(0) == 1.0
+    locked = 0
+    for _ in range(4):                                  # the orbit has period two sweeps
+        counts = [orc.tables(s)[0].copy() for s in range(2)]
+        dofs = [orc.dofs(s).copy() for s in range(2)]
+        orc.run_sweeps(1)
+        for s in range(2):
+            d = orc.tables(s)[0] - counts[s]
+            levels = d[d > 0]
+            if np.array_equal(orc.dofs(s), -dofs[s]) and len(levels) in (2, 4) and np.all(levels == 16 // len(levels)):
+                locked += 1
+    orc.close()
+    assert locked >= 4
