@@ -226,6 +226,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def instance_seed(seed: int, k: int) -> int:
+    """Seed of the k-th instance of a batch: a multiple of 2^20, so that no two walkers of the
+    batch (fewer than 2^20 per instance) share a Philox key (walker keys are seed XOR walker)."""
+    return (seed * 100000 + k) << 20
+
+
 def make_batch(rg, seed: int, device: int):
     w = WORKLOAD
     if w["model"] == "mixed":
@@ -238,7 +244,7 @@ def make_batch(rg, seed: int, device: int):
                                         energy_min=c["energy_min"], energy_max=c["energy_max"],
                                         bin_width=c["bin_width"], num_windows=c["num_windows"],
                                         replicas_per_window=c["replicas_per_window"],
-                                        window_overlap=c["window_overlap"], seed=seed * 1000 + 100 * ci + k))
+                                        window_overlap=c["window_overlap"], seed=instance_seed(seed, 100 * ci + k)))
         return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
                         sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
                         lnf_final=w["lnf_final"], device=device, mask_mode=rg.MASK_VISITED,
@@ -253,7 +259,7 @@ def make_batch(rg, seed: int, device: int):
         inss = [rg.Instance(model=rg.MODEL_ASHKIN_TELLER2D, L=w["L"], K=w["K"], fields=at_fields(w, k),
                             energy_min=w["energy_min"], energy_max=w["energy_max"], bin_width=w["bin_width"],
                             num_windows=w["num_windows"], replicas_per_window=w["replicas_per_window"],
-                            window_overlap=w["window_overlap"], seed=seed * 1000 + k)
+                            window_overlap=w["window_overlap"], seed=instance_seed(seed, k))
                 for k in range(w["realizations"])]
         mask = rg.MASK_VISITED
     return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
