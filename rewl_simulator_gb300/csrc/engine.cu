@@ -1606,9 +1606,9 @@ struct HostInst {
 struct Launch {
     int model;
     std::vector<int32_t> slots;
-    int smem_per_warp;      // per walker for the bin-tracking kernel, per warp otherwise
-    int nbcap;
-    int wpb;                // warps per block
+    int smem_per_warp = 0;  // per walker for the bin-tracking kernel, per warp otherwise
+    int nbcap = 0;
+    int wpb = 1;            // warps per block
     int bins = 0;           // Ising bin-tracking kernel with `walkers_per_warp` walkers per warp and chunk `chunk`
     int walkers_per_warp = 1;
     int chunk = 32;
