@@ -2041,7 +2041,7 @@ int sm_count(const rewl_engine* e)
 
 // The logDoS tables of the Ashkin-Teller kernel live in global memory and are read through L1,
 // so its shared-memory carveout is the smallest that still holds the blocks resident on an SM
-// (the driver's default leaves L1 far less).
+// (the CUDA runtime's default split leaves L1 far less).
 int at_carveout(rewl_engine* e, Launch& l)
 {
     if (!l.tables) return REWL_OK;
