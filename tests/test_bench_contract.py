@@ -44,3 +44,23 @@ def test_warmup_below_three_is_refused():
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--warmup", "2"], cwd=ROOT, capture_output=True,
                        text=True, timeout=120)
     assert r.returncode != 0 and "--warmup must be >= 3" in r.stderr
+
+
+@pytest.mark.parametrize("workload", ["at", "mixed"])
+def test_bench_batches_give_every_walker_its_own_key(workload):
+    """Walker keys are (seed_lo XOR walker, seed_hi): the bench's instance seeds keep them distinct
+    across all walkers of a batch."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    import rewl_simulator_gb300 as rg
+    old = bench.WORKLOAD
+    try:
+        bench.select_workload(workload)
+        batch = bench.make_batch(rg, bench.rank_seed(0), device=0)
+    finally:
+        bench.WORKLOAD = old
+    keys = set()
+    for ins in batch.instances:
+        for u in range(ins.num_windows * ins.replicas_per_window):
+            keys.add(((ins.seed & 0xFFFFFFFF) ^ u, ins.seed >> 32))
+    assert len(keys) == sum(i.num_windows * i.replicas_per_window for i in batch.instances)
