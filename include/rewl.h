@@ -239,11 +239,30 @@ int rewl_window_state(rewl_engine* eng, int32_t instance, int32_t window, double
  * range and normalise it so that sum_E g(E) = states_per_site^N (minus ln 2 when
  * `half_spectrum`).  Restates concatenate_tables (multiple overlap) and
  * normalize_logDoS (src/util/concatenate_rewl_tables.hpp:167-305,
- * src/util/vector_matching.hpp:38-88, src/util/array_shift.hpp:15-43).
+ * src/util/vector_matching.hpp:38-88, src/util/array_shift.hpp:15-43), splicing
+ * where the derivatives differ least (REWL_MATCH_DERIVATIVE below).
  * Masked bins are left out.  On input *count is the capacity of energies/logdos;
  * on output the number of values written. */
 int rewl_global_logdos(rewl_engine* eng, int32_t instance, int32_t half_spectrum,
                        double* energies, double* logdos, int32_t* count);
+
+/* The same post-processing on caller-held tables, host only (no engine or device):
+ * num_windows windows of sizes[w] rows (ascending energies, valid levels only) stored
+ * one after another; consecutive windows must overlap.  The result is normalised to
+ * sum g = states_per_site^system_size (halved when half_spectrum).  match selects where
+ * neighbouring windows are spliced:
+ *   REWL_MATCH_DERIVATIVE: at the overlap bin whose d ln g / dE differ least (the
+ *     engine's rule, rewl_global_logdos);
+ *   REWL_MATCH_REFERENCE: as the reference's compiled code does, whose abs() of the
+ *     derivative difference (src/util/vector_matching.hpp:74,81,83) resolves to the C
+ *     library's int abs(int) and so truncates it to an integer: bit for bit the
+ *     reference's concatenate_tables + normalize_logDoS.
+ * *count: capacity in, rows out. */
+#define REWL_MATCH_DERIVATIVE 0
+#define REWL_MATCH_REFERENCE 1
+int rewl_concatenate_windows(int32_t num_windows, const int32_t* sizes, const double* energies, const double* logdos,
+                             double states_per_site, int64_t system_size, int32_t half_spectrum, int32_t match,
+                             double* out_energies, double* out_logdos, int32_t* count);
 
 /* Device time spent in the sweep kernels since the last call (ms) and the
  * number of sweep-kernel launches; timed with CUDA events on the engine stream. */

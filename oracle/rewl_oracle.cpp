@@ -24,11 +24,8 @@
 //   REWL_simulation::replica_exchange_update / average_and_redistribute_window /
 //   check_if_window_is_flat / simulate (ln f schedule, termination)
 //       src/Simulation/rewl_simulation.hpp:228-346,361-454,458-470,473-691
-//   normalize_logDoS            src/util/array_shift.hpp:15-43
-//   concatenate_tables (multiple overlap), find_left_concatenation_indices,
-//   derivative_of_vector
-//       src/util/concatenate_rewl_tables.hpp:167-305, src/util/vector_matching.hpp:38-88,
-//       src/util/numerical_derivatives.hpp:47-70
+// (Window concatenation and normalize_logDoS are not restated here: the tests compare the
+// product's versions with the reference's own, run by oracle/ref_harness.cpp.)
 //
 // Two semantics are implemented:
 //   * REFERENCE: each walker owns std::mt19937_64(seed) with

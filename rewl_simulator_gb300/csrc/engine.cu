@@ -2337,8 +2337,20 @@ double derivative(size_t i, const std::vector<double>& f, const std::vector<doub
     return (-f[i + 2] + 8. * f[i + 1] - 8. * f[i - 1] + f[i - 2]) / (12. * (a[i] - a[i - 1]));
 }
 
+// reference_abs: compare derivative differences as the reference's compiled code does.  Its
+// find_left_concatenation_indices calls an unqualified abs() on a double in a translation unit
+// that includes only <cmath> and <vector>, which resolves to the C library's int abs(int): every
+// |difference| is truncated to an integer, so the splice lands on the first overlapping bin unless
+// some derivative difference reaches 1.  Without it the true |difference| is minimised.
+inline double beta_gap(double d, bool reference_abs)
+{
+    if (!reference_abs) return std::fabs(d);
+    const double t = std::trunc(d);                       // double -> int conversion truncates
+    return std::fabs(std::max(-2147483647.0, std::min(2147483647.0, t)));
+}
+
 int concatenate(const std::vector<std::vector<double>>& E, const std::vector<std::vector<double>>& G,
-                std::vector<double>& fe, std::vector<double>& fg)
+                std::vector<double>& fe, std::vector<double>& fg, bool reference_abs = false)
 {
     fe = E[0]; fg = G[0];
     for (size_t w = 1; w < E.size(); ++w) {
@@ -2349,11 +2361,12 @@ int concatenate(const std::vector<std::vector<double>>& E, const std::vector<std
         if (left_start < 0) return fail(REWL_EINVAL, "windows %zu and %zu do not overlap", w - 1, w);
         const size_t nleft = fe.size();
         if (nleft - (size_t)left_start > er.size()) return fail(REWL_EINVAL, "window %zu lies inside window %zu", w, w - 1);
-        double beta_diff = std::fabs(derivative((size_t)left_start, fg, fe) - derivative(0, gr, er));
+        double beta_diff = beta_gap(derivative((size_t)left_start, fg, fe) - derivative(0, gr, er), reference_abs);
         size_t cl = (size_t)left_start;
         for (size_t idx = 1; idx != nleft - (size_t)left_start; ++idx) {
             const double lb = derivative((size_t)left_start + idx, fg, fe), rb = derivative(idx, gr, er);
-            if ((std::fabs(lb - rb) + 0.5) < (beta_diff + 0.5)) { beta_diff = std::fabs(lb - rb); cl = (size_t)left_start + idx; }
+            const double gap = beta_gap(lb - rb, reference_abs);
+            if ((gap + 0.5) < (beta_diff + 0.5)) { beta_diff = gap; cl = (size_t)left_start + idx; }
         }
         double shifter = 0;
         size_t right_idx = 0;
@@ -2982,6 +2995,41 @@ int rewl_global_logdos(rewl_engine* e, int32_t ii, int32_t half_spectrum, double
 // the windows that hold an energy by the reference's running mean
 // average_two_windows(final, window, overlapping_windows, 1)
 // (src/util/concatenate_rewl_tables.hpp:43-49, 241-256), in window order.
+int rewl_concatenate_windows(int32_t num_windows, const int32_t* sizes, const double* energies, const double* logdos,
+                             double states_per_site, int64_t system_size, int32_t half_spectrum, int32_t match,
+                             double* out_energies, double* out_logdos, int32_t* count)
+{
+    if (num_windows < 1 || !sizes || !energies || !logdos || !count || system_size < 1 || !(states_per_site > 0))
+        return fail(REWL_EINVAL, "bad arguments");
+    if (match != REWL_MATCH_DERIVATIVE && match != REWL_MATCH_REFERENCE) return fail(REWL_EINVAL, "bad match rule");
+    std::vector<std::vector<double>> Es(num_windows), Gs(num_windows);
+    size_t off = 0;
+    for (int w = 0; w < num_windows; ++w) {
+        if (sizes[w] < 2) return fail(REWL_EINVAL, "window %d has fewer than 2 rows", w);
+        Es[w].assign(energies + off, energies + off + sizes[w]);
+        Gs[w].assign(logdos + off, logdos + off + sizes[w]);
+        off += (size_t)sizes[w];
+    }
+    std::vector<double> fe, fg;
+    int rc = concatenate(Es, Gs, fe, fg, match == REWL_MATCH_REFERENCE);
+    if (rc) return rc;
+    if ((int64_t)fe.size() > *count) { *count = (int32_t)fe.size(); return fail(REWL_EINVAL, "output capacity too small (%zu needed)", fe.size()); }
+    // normalize_logDoS (src/util/array_shift.hpp:15-43) step for step: its running maximum starts at 0
+    double mx = 0.0;
+    for (double v : fg) mx = mx > v ? mx : v;
+    double sum = 0.0;
+    for (double v : fg) sum += std::exp(-(mx - v));
+    sum = std::log(sum);
+    sum += mx;
+    const double shift = (double)system_size * std::log(states_per_site) - sum - std::log(2.) * (half_spectrum ? 1.0 : 0.0);
+    for (size_t k = 0; k < fe.size(); ++k) {
+        if (out_energies) out_energies[k] = fe[k];
+        if (out_logdos) out_logdos[k] = fg[k] + shift;
+    }
+    *count = (int32_t)fe.size();
+    return REWL_OK;
+}
+
 int rewl_global_observables(rewl_engine* e, int32_t ii, double* obs, int32_t* count)
 {
     if (!e || ii < 0 || ii >= (int)e->inst.size() || !count) return fail(REWL_EINVAL, "bad arguments");

@@ -34,6 +34,8 @@ RNG_PHILOX = 0
 RNG_REPLAY = 1
 DISORDER_UNIFORM = 0        # REWL_DISORDER_*: the reference's disorder_distribution
 DISORDER_GAUSSIAN = 1
+MATCH_DERIVATIVE = 0        # REWL_MATCH_*: where concatenate_windows splices neighbouring windows
+MATCH_REFERENCE = 1
 
 
 class REWLError(RuntimeError):
@@ -145,6 +147,27 @@ def generate_fields(seed: int, strength: float, num_sites: int, distribution: in
     if rc != 0:
         raise REWLError(rc, lib.rewl_last_error_string().decode())
     return out
+
+
+def concatenate_windows(windows, states_per_site: float, system_size: int, half_spectrum: bool = False,
+                        match: int = MATCH_DERIVATIVE):
+    """Concatenate per-window (energies, ln g) tables and normalise, as the reference's
+    post-processing does (concatenate_tables with multiple overlap, then normalize_logDoS);
+    host only.  windows: sequence of (E, lng) arrays, ascending energies, valid levels only.
+    match=MATCH_REFERENCE reproduces the reference's compiled splice rule bit for bit.
+    Returns (E, lng)."""
+    lib = _native.load()
+    Es = [np.ascontiguousarray(e, dtype=np.float64) for e, _ in windows]
+    Gs = [np.ascontiguousarray(g, dtype=np.float64) for _, g in windows]
+    sizes = np.array([len(e) for e in Es], dtype=np.int32)
+    E, G = np.concatenate(Es), np.concatenate(Gs)
+    cap = C.c_int32(int(sizes.sum()))
+    oe, og = np.zeros(cap.value), np.zeros(cap.value)
+    rc = lib.rewl_concatenate_windows(len(Es), _p(sizes), _p(E), _p(G), float(states_per_site), int(system_size),
+                                      int(bool(half_spectrum)), int(match), _p(oe), _p(og), C.byref(cap))
+    if rc != 0:
+        raise REWLError(rc, lib.rewl_last_error_string().decode())
+    return oe[:cap.value].copy(), og[:cap.value].copy()
 
 
 def obs_columns(model: int, observables: int) -> int:

@@ -204,6 +204,49 @@ def gen_fields():
     print("wrote random_fields.json")
 
 
+def gen_concatenate():
+    """The reference's concatenate_tables (multiple overlap) + normalize_logDoS on window tables cut
+    from exact ln g with per-window offsets and noise (Ising), and from a smooth synthetic ln g on a
+    0.05 grid (half spectrum, Ashkin-Teller-like)."""
+    so = build_ref.build("ising", 8, 4.0)
+    ref = pyoracle.RefWalker(so, -128, -20, 4.0, 27, 1)
+    import ctypes as C
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    rng = np.random.default_rng(11)
+    cases = []
+
+    def cut(E, g, bounds, noise):
+        wins = []
+        for a, b in bounds:
+            gw = g[a:b] - g[a] + rng.uniform(-3, 3) + rng.normal(0, noise, b - a)
+            wins.append((E[a:b].astype(float), gw))
+        return wins
+
+    z16 = np.load(OUT / "exact_ising_L16.npz")
+    z8 = np.load(OUT / "exact_ising_L8.npz")
+    e = np.round(np.arange(-60.0, 0.0001, 0.05), 2)
+    s_at = 30.0 * np.sqrt(np.clip((e + 60.0) / 60.0, 0, 1)) + 0.02 * np.sin(e)
+    specs = [("ising_L16_3win", z16["E"], z16["lng"], [(0, 80), (50, 160), (130, len(z16["E"]))], 0.05, 2.0, 256, 1.0),
+             ("ising_L16_4win_clean", z16["E"], z16["lng"], [(0, 70), (40, 130), (100, 200), (170, len(z16["E"]))], 0.0,
+              2.0, 256, 1.0),
+             ("ising_L8_2win_noisy", z8["E"], z8["lng"], [(0, 40), (25, len(z8["E"]))], 0.3, 2.0, 64, 1.0),
+             ("at_half_3win", e, s_at, [(0, 540), (390, 960), (810, len(e))], 0.02, 4.0, 36, 0.0)]
+    for name, E, g, bounds, noise, spp, N, emax in specs:
+        wins = cut(E, g, bounds, noise)
+        sizes = np.array([len(w[0]) for w in wins], dtype=np.uint64)
+        Ef = np.concatenate([w[0] for w in wins])
+        Gf = np.concatenate([w[1] for w in wins])
+        cap = C.c_size_t(len(Ef))
+        oe, og = np.zeros(len(Ef)), np.zeros(len(Ef))
+        ref.lib.ref_concatenate(len(wins), p(sizes), p(Ef), p(Gf), spp, N, emax, p(oe), p(og), C.byref(cap))
+        n = cap.value
+        cases.append(dict(name=name, states_per_site=spp, system_size=N, half_spectrum=emax == 0.0,
+                          sizes=[int(x) for x in sizes], energies=[v.hex() for v in Ef], logdos=[v.hex() for v in Gf],
+                          out_energies=[v.hex() for v in oe[:n]], out_logdos=[v.hex() for v in og[:n]]))
+    (OUT / "concatenate.json").write_text(json.dumps(cases))
+    print("wrote concatenate.json")
+
+
 def gen_normalize():
     so = build_ref.build("ising", 8, 4.0)
     ref = pyoracle.RefWalker(so, -128, -20, 4.0, 27, 1)
@@ -321,7 +364,7 @@ def gen_cumulants():
 
 
 if __name__ == "__main__":
-    groups = sys.argv[1:] or ["replay", "replay_corr", "glazier", "rng", "fields", "normalize", "exact", "thermo",
-                              "cumulants", "writers"]
+    groups = sys.argv[1:] or ["replay", "replay_corr", "glazier", "rng", "fields", "concatenate", "normalize", "exact",
+                              "thermo", "cumulants", "writers"]
     for g in groups:
         globals()[f"gen_{g}"]()
