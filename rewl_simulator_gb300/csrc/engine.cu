@@ -2380,6 +2380,19 @@ int concatenate(const std::vector<std::vector<double>>& E, const std::vector<std
     return REWL_OK;
 }
 
+// normalize_logDoS (src/util/array_shift.hpp:15-43) step for step: the shift that makes
+// sum_E g(E) = states_per_site^N (halved for a half spectrum).  Its running maximum starts at 0.
+double normalisation_shift(const std::vector<double>& g, double states_per_site, double system_size, bool half)
+{
+    double mx = 0.0;
+    for (double v : g) mx = mx > v ? mx : v;
+    double sum = 0.0;
+    for (double v : g) sum += std::exp(-(mx - v));
+    sum = std::log(sum);
+    sum += mx;
+    return system_size * std::log(states_per_site) - sum - std::log(2.) * (half ? 1.0 : 0.0);
+}
+
 } // namespace
 
 // ============================================================================
@@ -2976,14 +2989,8 @@ int rewl_global_logdos(rewl_engine* e, int32_t ii, int32_t half_spectrum, double
     std::vector<double> fe, fg;
     int rc = concatenate(Es, Gs, fe, fg);
     if (rc) return rc;
-    // normalize_logDoS: sum_E g(E) = states_per_site^N (halved for a half spectrum)
-    double mx = fg.empty() ? 0 : fg[0];
-    for (double v : fg) mx = std::max(mx, v);
-    double sum = 0;
-    for (double v : fg) sum += std::exp(-(mx - v));
-    const double lse = std::log(sum) + mx;
     const double states = H.dev.model == REWL_MODEL_ISING2D ? 2.0 : 4.0;
-    const double shift = (double)H.dev.N * std::log(states) - lse - (half_spectrum ? std::log(2.0) : 0.0);
+    const double shift = normalisation_shift(fg, states, (double)H.dev.N, half_spectrum != 0);
     if ((int)fe.size() > *count) { *count = (int)fe.size(); return fail(REWL_EINVAL, "output capacity too small (%zu needed)", fe.size()); }
     for (size_t k = 0; k < fe.size(); ++k) { if (energies) energies[k] = fe[k]; if (logdos) logdos[k] = fg[k] + shift; }
     *count = (int)fe.size();
@@ -3014,14 +3021,7 @@ int rewl_concatenate_windows(int32_t num_windows, const int32_t* sizes, const do
     int rc = concatenate(Es, Gs, fe, fg, match == REWL_MATCH_REFERENCE);
     if (rc) return rc;
     if ((int64_t)fe.size() > *count) { *count = (int32_t)fe.size(); return fail(REWL_EINVAL, "output capacity too small (%zu needed)", fe.size()); }
-    // normalize_logDoS (src/util/array_shift.hpp:15-43) step for step: its running maximum starts at 0
-    double mx = 0.0;
-    for (double v : fg) mx = mx > v ? mx : v;
-    double sum = 0.0;
-    for (double v : fg) sum += std::exp(-(mx - v));
-    sum = std::log(sum);
-    sum += mx;
-    const double shift = (double)system_size * std::log(states_per_site) - sum - std::log(2.) * (half_spectrum ? 1.0 : 0.0);
+    const double shift = normalisation_shift(fg, states_per_site, (double)system_size, half_spectrum != 0);
     for (size_t k = 0; k < fe.size(); ++k) {
         if (out_energies) out_energies[k] = fe[k];
         if (out_logdos) out_logdos[k] = fg[k] + shift;
