@@ -249,8 +249,11 @@ int rewl_global_logdos(rewl_engine* eng, int32_t instance, int32_t half_spectrum
 /* The same post-processing on caller-held tables, host only (no engine or device):
  * num_windows windows of sizes[w] rows (ascending energies, valid levels only) stored
  * one after another; consecutive windows must overlap.  The result is normalised to
- * sum g = states_per_site^system_size (halved when half_spectrum).  match selects where
- * neighbouring windows are spliced:
+ * sum g = states_per_site^system_size (halved when half_spectrum).  With num_obs > 0,
+ * obs holds num_obs values per row (same order as the energies) and out_obs receives them
+ * averaged over each overlap as the reference does (average_two_windows weighted by the
+ * number of windows averaged so far, src/util/concatenate_rewl_tables.hpp:42-49,241-256).
+ * match selects where neighbouring windows are spliced:
  *   REWL_MATCH_DERIVATIVE: at the overlap bin whose d ln g / dE differ least (the
  *     engine's rule, rewl_global_logdos);
  *   REWL_MATCH_REFERENCE: as the reference's compiled code does, whose abs() of the
@@ -261,8 +264,9 @@ int rewl_global_logdos(rewl_engine* eng, int32_t instance, int32_t half_spectrum
 #define REWL_MATCH_DERIVATIVE 0
 #define REWL_MATCH_REFERENCE 1
 int rewl_concatenate_windows(int32_t num_windows, const int32_t* sizes, const double* energies, const double* logdos,
-                             double states_per_site, int64_t system_size, int32_t half_spectrum, int32_t match,
-                             double* out_energies, double* out_logdos, int32_t* count);
+                             int32_t num_obs, const double* obs, double states_per_site, int64_t system_size,
+                             int32_t half_spectrum, int32_t match, double* out_energies, double* out_logdos,
+                             double* out_obs, int32_t* count);
 
 /* Device time spent in the sweep kernels since the last call (ms) and the
  * number of sweep-kernel launches; timed with CUDA events on the engine stream. */

@@ -318,7 +318,8 @@ class RefWalker:
         L.ref_model_id.restype = C.c_int
         L.ref_uniforms.argtypes = [C.c_uint64, C.c_size_t, vp]
         L.ref_random_fields.argtypes = [C.c_uint64, C.c_double, C.c_int, C.c_size_t, vp]
-        L.ref_concatenate.argtypes = [C.c_size_t, vp, vp, vp, C.c_double, C.c_size_t, C.c_double, vp, vp, vp]
+        L.ref_concatenate.argtypes = [C.c_size_t, vp, vp, vp, C.c_size_t, vp, C.c_double, C.c_size_t, C.c_double,
+                                      vp, vp, vp, vp]
         L.ref_glazier.argtypes = [C.c_double, C.c_double, C.c_double, C.c_size_t, C.c_size_t, C.c_double, vp, vp, vp]
         L.ref_normalize_logdos.argtypes = [C.c_double, C.c_size_t, C.c_double, C.c_size_t, vp]
         self.nbins = nbins

@@ -157,24 +157,26 @@ void ref_random_fields(uint64_t seed, double strength, int type, size_t n, doubl
 // (src/util/concatenate_rewl_tables.hpp:167-305, with find_left_concatenation_indices,
 // src/util/vector_matching.hpp:38-88) on (energy, logDoS) tables of num_windows windows stored
 // one after another (sizes[w] rows each), then normalize_logDoS (src/util/array_shift.hpp:15-43).
-// One dummy observable column is carried.  *n: capacity in, rows out.
+// num_obs observables per row ride along in O (rows of num_obs, same order as E) and come
+// back averaged over the overlaps in outO.  *n: capacity in, rows out.
 void ref_concatenate(size_t num_windows, const size_t* sizes, const double* E, const double* G,
-                     double states_per_site, size_t system_size, double energy_max,
-                     double* outE, double* outG, size_t* n)
+                     size_t num_obs, const double* O, double states_per_site, size_t system_size,
+                     double energy_max, double* outE, double* outG, double* outO, size_t* n)
 {
     table<double> et(num_windows), gt(num_windows), ot(num_windows);
     size_t off = 0;
     for (size_t w = 0; w != num_windows; ++w) {
         et[w].assign(E + off, E + off + sizes[w]);
         gt[w].assign(G + off, G + off + sizes[w]);
-        ot[w].assign(sizes[w], 0.0);
+        ot[w].assign(O + off * num_obs, O + (off + sizes[w]) * num_obs);
         off += sizes[w];
     }
     std::vector<double> fe, fg, fo;
-    concatenate_tables_multiple_overlap<double, double, double>(1, 0, et, gt, ot, fe, fg, fo);
+    concatenate_tables_multiple_overlap<double, double, double>(num_obs, num_obs - 1, et, gt, ot, fe, fg, fo);
     normalize_logDoS<double, true>(states_per_site, system_size, energy_max, fg.size(), fg.data());
     const size_t m = fe.size() < *n ? fe.size() : *n;
     for (size_t i = 0; i != m; ++i) { outE[i] = fe[i]; outG[i] = fg[i]; }
+    for (size_t i = 0; i != m * num_obs; ++i) outO[i] = fo[i];
     *n = fe.size();
 }
 

@@ -114,7 +114,7 @@ def _declare(L: C.CDLL) -> None:
         "rewl_export_window_mask": [vp, i32, i32, vp],
         "rewl_window_state": [vp, i32, i32, vp, vp],
         "rewl_global_logdos": [vp, i32, i32, vp, vp, vp],
-        "rewl_concatenate_windows": [i32, vp, vp, vp, C.c_double, i64, i32, i32, vp, vp, vp],
+        "rewl_concatenate_windows": [i32, vp, vp, vp, i32, vp, C.c_double, i64, i32, i32, vp, vp, vp, vp],
         "rewl_sweep_kernel_time": [vp, vp, vp],
         "rewl_get_stream": [vp, vp],
         "rewl_snapshot_size": [vp, vp],

@@ -2349,10 +2349,16 @@ inline double beta_gap(double d, bool reference_abs)
     return std::fabs(std::max(-2147483647.0, std::min(2147483647.0, t)));
 }
 
+// O (optional): per window, rows of nobs observables; they are averaged in each overlap as the
+// reference does (average_two_windows, src/util/concatenate_rewl_tables.hpp:42-49, weighted by
+// the number of windows already averaged at the bin) into fo.
 int concatenate(const std::vector<std::vector<double>>& E, const std::vector<std::vector<double>>& G,
-                std::vector<double>& fe, std::vector<double>& fg, bool reference_abs = false)
+                std::vector<double>& fe, std::vector<double>& fg, bool reference_abs = false,
+                const std::vector<std::vector<double>>* O = nullptr, int nobs = 0, std::vector<double>* fo = nullptr)
 {
     fe = E[0]; fg = G[0];
+    std::vector<size_t> overlap(fe.size(), 1);
+    if (O) *fo = (*O)[0];
     for (size_t w = 1; w < E.size(); ++w) {
         const auto& er = E[w]; const auto& gr = G[w];
         if (er.size() < 2 || fe.size() < 2) return fail(REWL_EINVAL, "window %zu has fewer than 2 valid bins", w);
@@ -2372,10 +2378,24 @@ int concatenate(const std::vector<std::vector<double>>& E, const std::vector<std
         size_t right_idx = 0;
         for (size_t idx = (size_t)left_start; idx != fe.size(); ++idx) {
             right_idx = idx - (size_t)left_start;
+            if (O) {
+                const double c = (double)overlap[idx];
+                for (int k = 0; k < nobs; ++k) {
+                    double& v = (*fo)[idx * nobs + k];
+                    v = (c * v + 1.0 * (*O)[w][right_idx * nobs + k]) / (double)(overlap[idx] + 1);
+                }
+            }
+            ++overlap[idx];
             if (idx == cl) shifter = fg[idx] - gr[right_idx];
             else if (idx > cl) fg[idx] = gr[right_idx] + shifter;
         }
-        for (size_t idx = right_idx + 1; idx < er.size(); ++idx) { fe.push_back(er[idx]); fg.push_back(gr[idx] + shifter); }
+        for (size_t idx = right_idx + 1; idx < er.size(); ++idx) {
+            fe.push_back(er[idx]);
+            fg.push_back(gr[idx] + shifter);
+            overlap.push_back(1);
+            if (O)
+                for (int k = 0; k < nobs; ++k) fo->push_back((*O)[w][idx * nobs + k]);
+        }
     }
     return REWL_OK;
 }
@@ -3003,22 +3023,25 @@ int rewl_global_logdos(rewl_engine* e, int32_t ii, int32_t half_spectrum, double
 // average_two_windows(final, window, overlapping_windows, 1)
 // (src/util/concatenate_rewl_tables.hpp:43-49, 241-256), in window order.
 int rewl_concatenate_windows(int32_t num_windows, const int32_t* sizes, const double* energies, const double* logdos,
-                             double states_per_site, int64_t system_size, int32_t half_spectrum, int32_t match,
-                             double* out_energies, double* out_logdos, int32_t* count)
+                             int32_t num_obs, const double* obs, double states_per_site, int64_t system_size,
+                             int32_t half_spectrum, int32_t match, double* out_energies, double* out_logdos,
+                             double* out_obs, int32_t* count)
 {
-    if (num_windows < 1 || !sizes || !energies || !logdos || !count || system_size < 1 || !(states_per_site > 0))
+    if (num_windows < 1 || !sizes || !energies || !logdos || !count || system_size < 1 || !(states_per_site > 0) ||
+        num_obs < 0 || (num_obs > 0 && !obs))
         return fail(REWL_EINVAL, "bad arguments");
     if (match != REWL_MATCH_DERIVATIVE && match != REWL_MATCH_REFERENCE) return fail(REWL_EINVAL, "bad match rule");
-    std::vector<std::vector<double>> Es(num_windows), Gs(num_windows);
+    std::vector<std::vector<double>> Es(num_windows), Gs(num_windows), Os(num_obs > 0 ? num_windows : 0);
     size_t off = 0;
     for (int w = 0; w < num_windows; ++w) {
         if (sizes[w] < 2) return fail(REWL_EINVAL, "window %d has fewer than 2 rows", w);
         Es[w].assign(energies + off, energies + off + sizes[w]);
         Gs[w].assign(logdos + off, logdos + off + sizes[w]);
+        if (num_obs > 0) Os[w].assign(obs + off * num_obs, obs + (off + sizes[w]) * num_obs);
         off += (size_t)sizes[w];
     }
-    std::vector<double> fe, fg;
-    int rc = concatenate(Es, Gs, fe, fg, match == REWL_MATCH_REFERENCE);
+    std::vector<double> fe, fg, fo;
+    int rc = concatenate(Es, Gs, fe, fg, match == REWL_MATCH_REFERENCE, num_obs > 0 ? &Os : nullptr, num_obs, &fo);
     if (rc) return rc;
     if ((int64_t)fe.size() > *count) { *count = (int32_t)fe.size(); return fail(REWL_EINVAL, "output capacity too small (%zu needed)", fe.size()); }
     const double shift = normalisation_shift(fg, states_per_site, (double)system_size, half_spectrum != 0);
@@ -3026,6 +3049,7 @@ int rewl_concatenate_windows(int32_t num_windows, const int32_t* sizes, const do
         if (out_energies) out_energies[k] = fe[k];
         if (out_logdos) out_logdos[k] = fg[k] + shift;
     }
+    if (out_obs && num_obs > 0) std::copy(fo.begin(), fo.end(), out_obs);
     *count = (int32_t)fe.size();
     return REWL_OK;
 }

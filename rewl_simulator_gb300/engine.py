@@ -151,23 +151,32 @@ def generate_fields(seed: int, strength: float, num_sites: int, distribution: in
 
 def concatenate_windows(windows, states_per_site: float, system_size: int, half_spectrum: bool = False,
                         match: int = MATCH_DERIVATIVE):
-    """Concatenate per-window (energies, ln g) tables and normalise, as the reference's
-    post-processing does (concatenate_tables with multiple overlap, then normalize_logDoS);
-    host only.  windows: sequence of (E, lng) arrays, ascending energies, valid levels only.
+    """Concatenate per-window tables and normalise, as the reference's post-processing does
+    (concatenate_tables with multiple overlap, then normalize_logDoS); host only.
+    windows: sequence of (E, lng) or (E, lng, obs) with ascending energies, valid levels only, and
+    obs of shape (rows, K) averaged over each overlap as the reference averages observables.
     match=MATCH_REFERENCE reproduces the reference's compiled splice rule bit for bit.
-    Returns (E, lng)."""
+    Returns (E, lng) or (E, lng, obs)."""
     lib = _native.load()
-    Es = [np.ascontiguousarray(e, dtype=np.float64) for e, _ in windows]
-    Gs = [np.ascontiguousarray(g, dtype=np.float64) for _, g in windows]
+    Es = [np.ascontiguousarray(w[0], dtype=np.float64) for w in windows]
+    Gs = [np.ascontiguousarray(w[1], dtype=np.float64) for w in windows]
+    with_obs = all(len(w) > 2 for w in windows)
+    Os = [np.ascontiguousarray(w[2], dtype=np.float64).reshape(len(w[0]), -1) for w in windows] if with_obs else []
+    K = Os[0].shape[1] if with_obs else 0
     sizes = np.array([len(e) for e in Es], dtype=np.int32)
     E, G = np.concatenate(Es), np.concatenate(Gs)
+    O = np.concatenate(Os) if with_obs else np.zeros(0)
     cap = C.c_int32(int(sizes.sum()))
-    oe, og = np.zeros(cap.value), np.zeros(cap.value)
-    rc = lib.rewl_concatenate_windows(len(Es), _p(sizes), _p(E), _p(G), float(states_per_site), int(system_size),
-                                      int(bool(half_spectrum)), int(match), _p(oe), _p(og), C.byref(cap))
+    oe, og, oo = np.zeros(cap.value), np.zeros(cap.value), np.zeros(cap.value * K)
+    rc = lib.rewl_concatenate_windows(len(Es), _p(sizes), _p(E), _p(G), K, _p(O) if K else None, float(states_per_site),
+                                      int(system_size), int(bool(half_spectrum)), int(match), _p(oe), _p(og),
+                                      _p(oo) if K else None, C.byref(cap))
     if rc != 0:
         raise REWLError(rc, lib.rewl_last_error_string().decode())
-    return oe[:cap.value].copy(), og[:cap.value].copy()
+    n = cap.value
+    if with_obs:
+        return oe[:n].copy(), og[:n].copy(), oo[:n * K].reshape(n, K).copy()
+    return oe[:n].copy(), og[:n].copy()
 
 
 def obs_columns(model: int, observables: int) -> int:

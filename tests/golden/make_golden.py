@@ -213,7 +213,7 @@ def gen_concatenate():
     import ctypes as C
     p = lambda a: a.ctypes.data_as(C.c_void_p)
     rng = np.random.default_rng(11)
-    cases = []
+    cases = {}
 
     def cut(E, g, bounds, noise):
         wins = []
@@ -224,27 +224,32 @@ def gen_concatenate():
 
     z16 = np.load(OUT / "exact_ising_L16.npz")
     z8 = np.load(OUT / "exact_ising_L8.npz")
-    e = np.round(np.arange(-60.0, 0.0001, 0.05), 2)
-    s_at = 30.0 * np.sqrt(np.clip((e + 60.0) / 60.0, 0, 1)) + 0.02 * np.sin(e)
+    e = np.round(np.arange(-30.0, 0.0001, 0.05), 2)
+    s_at = 20.0 * np.sqrt(np.clip((e + 30.0) / 30.0, 0, 1)) + 0.02 * np.sin(e)
     specs = [("ising_L16_3win", z16["E"], z16["lng"], [(0, 80), (50, 160), (130, len(z16["E"]))], 0.05, 2.0, 256, 1.0),
              ("ising_L16_4win_clean", z16["E"], z16["lng"], [(0, 70), (40, 130), (100, 200), (170, len(z16["E"]))], 0.0,
               2.0, 256, 1.0),
              ("ising_L8_2win_noisy", z8["E"], z8["lng"], [(0, 40), (25, len(z8["E"]))], 0.3, 2.0, 64, 1.0),
-             ("at_half_3win", e, s_at, [(0, 540), (390, 960), (810, len(e))], 0.02, 4.0, 36, 0.0)]
+             ("at_half_3win", e, s_at, [(0, 270), (195, 480), (405, len(e))], 0.02, 4.0, 36, 0.0)]
+    K = 3                                              # two observables and a count column
     for name, E, g, bounds, noise, spp, N, emax in specs:
         wins = cut(E, g, bounds, noise)
         sizes = np.array([len(w[0]) for w in wins], dtype=np.uint64)
         Ef = np.concatenate([w[0] for w in wins])
         Gf = np.concatenate([w[1] for w in wins])
+        Of = np.column_stack([rng.uniform(0, 1, len(Ef)), rng.normal(0, 1, len(Ef)),
+                              rng.integers(1, 1000, len(Ef)).astype(float)]).ravel()
         cap = C.c_size_t(len(Ef))
-        oe, og = np.zeros(len(Ef)), np.zeros(len(Ef))
-        ref.lib.ref_concatenate(len(wins), p(sizes), p(Ef), p(Gf), spp, N, emax, p(oe), p(og), C.byref(cap))
+        oe, og, oo = np.zeros(len(Ef)), np.zeros(len(Ef)), np.zeros(len(Ef) * K)
+        ref.lib.ref_concatenate(len(wins), p(sizes), p(Ef), p(Gf), K, p(Of), spp, N, emax, p(oe), p(og), p(oo),
+                                C.byref(cap))
         n = cap.value
-        cases.append(dict(name=name, states_per_site=spp, system_size=N, half_spectrum=emax == 0.0,
-                          sizes=[int(x) for x in sizes], energies=[v.hex() for v in Ef], logdos=[v.hex() for v in Gf],
-                          out_energies=[v.hex() for v in oe[:n]], out_logdos=[v.hex() for v in og[:n]]))
-    (OUT / "concatenate.json").write_text(json.dumps(cases))
-    print("wrote concatenate.json")
+        for key, val in (("meta", np.array([spp, N, float(emax == 0.0), K])), ("sizes", sizes.astype(np.int64)),
+                         ("energies", Ef), ("logdos", Gf), ("obs", Of), ("out_energies", oe[:n]),
+                         ("out_logdos", og[:n]), ("out_obs", oo[:n * K])):
+            cases[f"{name}.{key}"] = val
+    np.savez_compressed(OUT / "concatenate.npz", **cases)
+    print("wrote concatenate.npz")
 
 
 def gen_normalize():

@@ -1,13 +1,12 @@
 """Window concatenation + normalisation (rewl_concatenate_windows, host only) against the
 reference's own concatenate_tables (multiple overlap) and normalize_logDoS, run by the reference
-harness on the same tables (tests/golden/concatenate.json, written by
-tests/golden/make_golden.py concatenate).
+harness on the same tables, observables averaged over the overlaps included
+(tests/golden/concatenate.npz, written by tests/golden/make_golden.py concatenate).
 
 The reference's splice search takes abs() of a double difference of derivatives in a translation
 unit where that resolves to the C library's int abs(int), so the difference is truncated to an
 integer.  REWL_MATCH_REFERENCE reproduces that bit for bit; REWL_MATCH_DERIVATIVE (the engine's
 rule) minimises the true difference and is checked against a restatement here."""
-import json
 import math
 
 import numpy as np
@@ -16,16 +15,22 @@ import pytest
 from conftest import GOLDEN
 
 
-def _cases():
-    return json.loads((GOLDEN / "concatenate.json").read_text())
+_Z = np.load(GOLDEN / "concatenate.npz")
+NAMES = sorted({k.split(".")[0] for k in _Z.files})
 
 
-def _windows(c):
-    E = np.array([float.fromhex(v) for v in c["energies"]])
-    G = np.array([float.fromhex(v) for v in c["logdos"]])
-    out, k = [], 0
+def _case(name):
+    c = {k.split(".", 1)[1]: _Z[k] for k in _Z.files if k.startswith(name + ".")}
+    spp, N, half, K = c["meta"]
+    c.update(states_per_site=float(spp), system_size=int(N), half_spectrum=bool(half), num_obs=int(K))
+    return c
+
+
+def _windows(c, with_obs=False):
+    out, k, K = [], 0, c["num_obs"]
     for n in c["sizes"]:
-        out.append((E[k:k + n], G[k:k + n]))
+        w = (c["energies"][k:k + n], c["logdos"][k:k + n])
+        out.append(w + (c["obs"][k * K:(k + n) * K].reshape(n, K),) if with_obs else w)
         k += n
     return out
 
@@ -69,25 +74,24 @@ def _restated(windows, spp, N, half, truncate):
     return np.array(fe), np.array([v + sh for v in fg])
 
 
-@pytest.mark.parametrize("case", [c["name"] for c in _cases()])
+@pytest.mark.parametrize("case", NAMES)
 def test_reference_rule_is_bit_identical_to_the_reference(engine_lib, case):
     rg = engine_lib
-    c = next(x for x in _cases() if x["name"] == case)
-    E, G = rg.concatenate_windows(_windows(c), c["states_per_site"], c["system_size"], c["half_spectrum"],
-                                  rg.MATCH_REFERENCE)
-    refE = np.array([float.fromhex(v) for v in c["out_energies"]])
-    refG = np.array([float.fromhex(v) for v in c["out_logdos"]])
-    assert np.array_equal(E, refE)
-    assert np.array_equal(G.view(np.uint64), refG.view(np.uint64))
+    c = _case(case)
+    E, G, O = rg.concatenate_windows(_windows(c, True), c["states_per_site"], c["system_size"], c["half_spectrum"],
+                                     rg.MATCH_REFERENCE)
+    assert np.array_equal(E, c["out_energies"])
+    assert np.array_equal(G.view(np.uint64), c["out_logdos"].view(np.uint64))
+    assert np.array_equal(O.ravel().view(np.uint64), c["out_obs"].view(np.uint64))
     # the restatement of the reference's rule agrees, so the one of the engine's rule is trusted
     rE, rG = _restated(_windows(c), c["states_per_site"], c["system_size"], c["half_spectrum"], True)
-    assert np.array_equal(rE, refE) and np.allclose(rG, refG, rtol=0, atol=1e-12)
+    assert np.array_equal(rE, c["out_energies"]) and np.allclose(rG, c["out_logdos"], rtol=0, atol=1e-12)
 
 
-@pytest.mark.parametrize("case", [c["name"] for c in _cases()])
+@pytest.mark.parametrize("case", NAMES)
 def test_derivative_rule_matches_its_restatement(engine_lib, case):
     rg = engine_lib
-    c = next(x for x in _cases() if x["name"] == case)
+    c = _case(case)
     E, G = rg.concatenate_windows(_windows(c), c["states_per_site"], c["system_size"], c["half_spectrum"])
     rE, rG = _restated(_windows(c), c["states_per_site"], c["system_size"], c["half_spectrum"], False)
     assert np.array_equal(E, rE) and np.allclose(G, rG, rtol=0, atol=1e-12)
@@ -95,7 +99,7 @@ def test_derivative_rule_matches_its_restatement(engine_lib, case):
 
 def test_the_two_rules_differ_on_noisy_windows(engine_lib):
     rg = engine_lib
-    c = next(x for x in _cases() if x["name"] == "ising_L16_3win")
+    c = _case("ising_L16_3win")
     _, a = rg.concatenate_windows(_windows(c), 2.0, 256, False, rg.MATCH_REFERENCE)
     _, b = rg.concatenate_windows(_windows(c), 2.0, 256, False, rg.MATCH_DERIVATIVE)
     assert np.abs(a - b).max() > 0.01
