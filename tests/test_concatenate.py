@@ -110,3 +110,26 @@ def test_windows_that_do_not_overlap_are_refused(engine_lib):
     w = [(np.array([0.0, 4.0, 8.0]), np.zeros(3)), (np.array([12.0, 16.0, 20.0]), np.zeros(3))]
     with pytest.raises(rg.REWLError):
         rg.concatenate_windows(w, 2.0, 16)
+
+
+def test_arguments_are_checked(engine_lib):
+    import ctypes as C
+    rg = engine_lib
+    lib = rg.load_library()
+    E = np.array([0.0, 4.0, 8.0, 4.0, 8.0, 12.0])
+    G = np.array([0.0, 1.0, 2.0, 0.0, 1.0, 2.0])
+    sizes = np.array([3, 3], dtype=np.int32)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    out_e, out_g = np.zeros(8), np.zeros(8)
+    n = C.c_int32(2)                                    # too small: the needed size comes back
+    assert lib.rewl_concatenate_windows(2, p(sizes), p(E), p(G), 0, None, 2.0, 16, 0, 0, p(out_e), p(out_g), None,
+                                        C.byref(n)) != 0 and n.value == 4
+    n = C.c_int32(8)
+    assert lib.rewl_concatenate_windows(2, p(sizes), p(E), p(G), 0, None, 2.0, 16, 0, 0, p(out_e), p(out_g), None,
+                                        C.byref(n)) == 0 and n.value == 4
+    assert np.array_equal(out_e[:4], [0.0, 4.0, 8.0, 12.0])
+    for bad in (dict(match=7), dict(num_obs=2), dict(sizes=np.array([1, 3], dtype=np.int32))):
+        n = C.c_int32(8)
+        s = bad.get("sizes", sizes)
+        assert lib.rewl_concatenate_windows(2, p(s), p(E), p(G), bad.get("num_obs", 0), None, 2.0, 16, 0,
+                                            bad.get("match", 0), p(out_e), p(out_g), None, C.byref(n)) != 0, bad
