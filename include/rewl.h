@@ -70,7 +70,8 @@ typedef struct rewl_instance_desc {
     double window_overlap;        /* REWL_Parameters::window_overlap */
     int32_t init_mode;            /* 0: spins uniform +-1 from the seed; 1: all +1 */
     int32_t reserved;
-    uint64_t seed;                /* Philox key for this instance's walkers */
+    uint64_t seed;                /* seed of this instance's walkers: the Philox key is its SplitMix64 mix,
+                                     so nearby seeds give unrelated walker streams */
 } rewl_instance_desc;
 
 typedef struct rewl_batch_desc {
@@ -79,7 +80,7 @@ typedef struct rewl_batch_desc {
     int32_t sweeps_per_check;     /* REWL_Parameters::sweeps_per_check (multiple of sweeps_per_exchange) */
     int32_t flatness_mode;        /* REWL_FLAT_* */
     double flatness_param;        /* p of the flatness rule */
-    double lnf_initial;           /* REWL_Walker::incrementer initial value */
+    double lnf_initial;           /* REWL_Walker::incrementer initial value, (0, 64] */
     double lnf_final;             /* REWL_Parameters::final_increment */
     int32_t mask_mode;            /* REWL_MASK_* */
     int32_t one_over_t;           /* ONE_OVER_T_ALGORITHM switch for the ln f schedule */
@@ -161,7 +162,11 @@ int rewl_generate_fields(uint64_t seed, double strength, int32_t distribution, i
  * src/REWL/rewl_histograms.hpp:42-50). */
 int rewl_set_logdos(rewl_engine* eng, int32_t instance, int32_t window, const double* logdos);
 
-/* Set ln f of a window (REWL_Walker::incrementer, src/REWL/rewl_walker.hpp:21). */
+/* Set ln f of a window (REWL_Walker::incrementer, src/REWL/rewl_walker.hpp:21), (0, 64].
+ * Sweep launches are sized so that one launch cannot carry a logDoS entry past int64: a
+ * large ln f on a large lattice splits an exchange interval into several launches (same
+ * results).  A logDoS entry reaching 2^62 units (4.2e6 nats) without a flat event stops the
+ * engine with REWL_ESTATE, as does a per-stage count passing 2^32 - 1. */
 int rewl_set_lnf(rewl_engine* eng, int32_t instance, int32_t window, double lnf);
 
 /* REWL_RNG_REPLAY only: the uniform stream a walker consumes, one value per
@@ -313,19 +318,26 @@ int rewl_mlp_gradient(rewl_mlp* mlp, const float* X, const float* y, int32_t n, 
 int rewl_mlp_set_data(rewl_mlp* mlp, const float* X, const float* y, int32_t n, int32_t in_dim);
 /* `steps` Adam steps on random batches of `batch` rows; per-step losses into `losses` (may be NULL) */
 int rewl_mlp_train(rewl_mlp* mlp, int32_t steps, int32_t batch, float lr, float* losses);
-/* kernels launched by this network so far */
+/* kernels launched by this network so far (updated atomically: calls on one network may come
+ * from several threads) */
 int rewl_mlp_launches(const rewl_mlp* mlp, int64_t* count);
 /* Allocation-free prediction (no counterpart in the reference).  Same result as
  * rewl_mlp_predict, but X (n x in_dim floats) and y (n floats) are DEVICE
  * pointers and the work is enqueued on `stream` (a cudaStream_t; NULL = legacy
  * default stream) without waiting for it.  Activations live in a static 9.5 MiB
- * device array, so no call allocates device memory; for callers that cannot
- * allocate (while a stream is being captured, or at a device-memory limit).
- * At most 4096 rows per call and hidden width at most 256, else REWL_EINVAL.
- * The first call on a device looks up the array's address: make it before any
- * stream capture.  The array is shared by all networks on a device: calls that
- * may overlap (other streams, other threads) race and must be ordered by the
- * caller.  Parameters must not change while a call is in flight. */
+ * device array that every GPU loading this library holds until exit, so no call
+ * allocates device memory.  It is for callers that cannot call cudaMalloc: a host
+ * program whose own allocator already holds the device's memory, a loop at its
+ * device-memory limit, or a driver loop that must not stall (cudaMalloc may
+ * synchronise the device).  At most 4096 rows per call and hidden width at most
+ * 256, else REWL_EINVAL.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress): make it before any stream capture.  The array is shared
+ * by all networks on a device and keeps the last call's contents: calls that may
+ * overlap on the GPU (other streams, other threads) race and must be ordered by the
+ * caller.  Parameters must not change while a call is in flight.  The call does not
+ * wait for the GPU, so a tensor-core GEMM whose bounded wait ran out is reported by
+ * the next synchronising rewl_mlp_* call (REWL_EDEVICE); until then this call writes
+ * NaN to y.  The caller's current device is left as it was. */
 int rewl_mlp_predict_noalloc(rewl_mlp* mlp, const float* X, int32_t n, int32_t in_dim, float* y, void* stream);
 
 /* ------------------------------------------------------------------------

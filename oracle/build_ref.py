@@ -1,7 +1,8 @@
 """Build recipe for the reference harness (TEST INFRASTRUCTURE ONLY).
 
 Compiles oracle/ref_harness.cpp against the reference's own headers where they
-lie (REWL_REFERENCE_DIR, default /root/reference) into oracle/_ref/, one shared
+lie (the directory named by the environment variable REWL_REFERENCE_DIR, which
+must be set: without it the harness is simply not available) into oracle/_ref/, one shared
 library per (model, L, K, bin width) because the reference fixes those at
 compile time (src/Hamiltonians/Ising2d/ising2d_parameters.cxx:13-69,
 src/Hamiltonians/Ashkin_Teller2d/ashkin_teller2d_parameters.cxx:13-70).
@@ -24,11 +25,12 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REF = Path(os.environ.get("REWL_REFERENCE_DIR", "/root/reference"))
+_REF_ENV = os.environ.get("REWL_REFERENCE_DIR")
+REF = Path(_REF_ENV) if _REF_ENV else None
 
 
 def reference_available() -> bool:
-    return (REF / "src" / "REWL" / "rewl_walker.hpp").is_file()
+    return REF is not None and (REF / "src" / "REWL" / "rewl_walker.hpp").is_file()
 
 
 def _ising_params(L: int, bw: float) -> str:

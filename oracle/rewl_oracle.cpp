@@ -85,6 +85,17 @@ static inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
 // Counter streams (third counter word) of the engine semantics.
 enum : uint32_t { STREAM_WL = 0x574C0001u, STREAM_EXCH = 0x45580002u, STREAM_INIT = 0x494E0003u, STREAM_ADJ = 0x41440004u };
 
+// An instance's Philox key comes from its seed through the SplitMix64 finaliser
+// (Steele, Lea, Flood, "Fast splittable pseudorandom number generators", OOPSLA 2014), so
+// that seeds differing only in low bits do not give walkers the same (seed ^ walker) key.
+static inline uint64_t instance_key(uint64_t seed)
+{
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
 static inline uint32_t key0(uint64_t seed, uint32_t uid) { return (uint32_t)seed ^ uid; }
 static inline uint32_t key1(uint64_t seed) { return (uint32_t)(seed >> 32); }
 
@@ -446,6 +457,7 @@ template <class M> struct alignas(128) Walker
 template <class M> struct Sim
 {
     Config c;
+    uint64_t key = 0;                   // Philox key of the engine semantics: instance_key(c.seed)
     Binning bn;
     std::vector<WinDef> wins;
     std::vector<Walker<M>> wk;          // slot = w*R + r
@@ -540,6 +552,7 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
 {
     auto* S = new Sim<M>();
     S->c = c;
+    S->key = instance_key(c.seed);
     S->bn = make_binning(c);
     S->nobs = c.observables == 2 ? M::num_obs_corr : M::num_obs;
     if (c.observables == 2) S->q.build((size_t)c.L);
@@ -576,7 +589,7 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
                     for (size_t i = 0; i < nd; ++i)
                     {   // engine layout: sigma plane then tau plane; ours is interleaved
                         const size_t e_idx = (M::num_obs == 13) ? ((i & 1) ? (i >> 1) + k.sys.N : (i >> 1)) : i;
-                        k.sys.spin[i] = (philox_word(c.seed, k.uid, e_idx, STREAM_INIT) >> 31) ? -1.0 : 1.0;
+                        k.sys.spin[i] = (philox_word(S->key, k.uid, e_idx, STREAM_INIT) >> 31) ? -1.0 : 1.0;
                     }
                 else
                 {
@@ -588,7 +601,7 @@ template <class M> static Sim<M>* create(const Config& c, const double* fields, 
             if (c.semantics == SEM_REFERENCE) k.gen.seed((uint32_t)(c.seed + k.uid));
             size_t start;
             if (c.semantics == SEM_ENGINE)
-                start = (size_t)(((uint64_t)philox_word(c.seed, k.uid, 0, STREAM_ADJ) * k.sys.N) >> 32);
+                start = (size_t)(((uint64_t)philox_word(S->key, k.uid, 0, STREAM_ADJ) * k.sys.N) >> 32);
             else { start = (size_t)(k.U(k.gen) * (double)k.sys.N); ++k.draws; }
             const size_t cap = 4000 * nd;
             bool ok = adjust(*S, k, start, cap);
@@ -652,7 +665,7 @@ template <class M, int SEM> static inline void wl_update(Sim<M>& S, Walker<M>& w
         }
         else
         {
-            const float thr = neglog_u32(philox_word(S.c.seed, w.uid, attempt, STREAM_WL));
+            const float thr = neglog_u32(philox_word(S.key, w.uid, attempt, STREAM_WL));
             acc = (dg <= 0.f) || (dg < thr);
         }
         if (acc) { w.sys.set_state(idx, t); cur = nb; }
@@ -727,7 +740,7 @@ template <class M> static void exchange(Sim<M>& S)
         {
             for (int i = R - 1; i >= 1; --i)
             {
-                const uint32_t word = philox_word(S.c.seed, 0x80000000u, ((uint64_t)(R - 1 - i)),
+                const uint32_t word = philox_word(S.key, 0x80000000u, ((uint64_t)(R - 1 - i)),
                                                   STREAM_EXCH, (uint32_t)((S.exch_round << 8) ^ (uint64_t)lw));
                 const int j = (int)(((uint64_t)word * (uint64_t)(i + 1)) >> 32);
                 std::swap(perm[i], perm[j]);
@@ -753,7 +766,7 @@ template <class M> static void exchange(Sim<M>& S)
                 const double a = lo.logdos[S.lbin(lo, Eh)] - lo.logdos[S.lbin(lo, El)];
                 const double b = hi.logdos[S.lbin(hi, El)] - hi.logdos[S.lbin(hi, Eh)];
                 const double delta = std::max(0., a) + std::max(0., b);
-                const uint32_t word = philox_word(S.c.seed, 0x80000000u, (uint64_t)(32 + r),
+                const uint32_t word = philox_word(S.key, 0x80000000u, (uint64_t)(32 + r),
                                                   STREAM_EXCH, (uint32_t)((S.exch_round << 8) ^ (uint64_t)lw));
                 const float thr = neglog_u32(word);
                 const int64_t d = (int64_t)std::llround(delta * QSCALE);

@@ -79,11 +79,41 @@ int fail(int code, const char* fmt, ...)
 constexpr int kMaxReplicas = 32;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 
-enum : int { ERR_BOUNDS = 1, ERR_ADJUST = 2, ERR_REPLAY_EXHAUSTED = 4, ERR_RANGE = 8 };
-// |logDoS| beyond which a window is reported instead of risking int64 overflow: 2^62 units
-// (4.2e6 nats) leaves 4.2e6 nats of headroom, more than one check interval can add to a bin
-// at ln f = 1 in the configured workloads (sweeps_per_check x N visits per walker)
+enum : int { ERR_BOUNDS = 1, ERR_ADJUST = 2, ERR_REPLAY_EXHAUSTED = 4, ERR_RANGE = 8, ERR_COUNT = 16 };
+// |logDoS| at which a window is reported (REWL_ESTATE) instead of risking int64 overflow: 2^62
+// units (4.2e6 nats).  Every kernel that adds to g checks the values it wrote against it, and
+// every kernel returns without work once the error word is set, so at most one launch's growth
+// lies beyond the limit.  The host splits sweep launches so that one launch adds at most
+// kLaunchGrowth to any bin (ln f bound x sweeps x degrees of freedom, plus one exchange visit):
+// 2^62 + 2^62 - 2^58 stays below 2^63 with room for the acceptance thresholds (< 2^45).
 constexpr long long kLogdosLimit = 1LL << 62;
+constexpr long long kLaunchGrowth = (1LL << 62) - (1LL << 58);
+
+// Any device error stops further work: a kernel that finds the error word set returns at once.
+// Another block may set the word while this one reads it, so a warp acts on lane 0's reading
+// (all 32 lanes must be active) and a block on thread 0's.
+__device__ __forceinline__ bool engine_failed(const int32_t* counters)
+{
+    return *reinterpret_cast<const volatile int32_t*>(counters) != 0;
+}
+__device__ __forceinline__ bool engine_failed_warp(const int32_t* counters)
+{
+    return __shfl_sync(0xFFFFFFFFu, (int)engine_failed(counters), 0) != 0;
+}
+
+// A launch's derived visits to bin k (its logDoS change over ln f) into the per-stage count
+// (uint32, the reference keeps uint64: a count that would pass 2^32 - 1 saturates and is
+// reported) and the cumulative visits; also checks the new logDoS against the range limit.
+__device__ __forceinline__ int commit_visits(uint32_t* gH, uint64_t* gv, int k, long long dv, long long gnew)
+{
+    int err = 0;
+    const unsigned long long h = (unsigned long long)gH[k] + (unsigned long long)dv;
+    if (h > 0xFFFFFFFFull) { err |= ERR_COUNT; gH[k] = 0xFFFFFFFFu; }
+    else gH[k] = (uint32_t)h;
+    gv[k] += (uint64_t)dv;
+    if (gnew >= kLogdosLimit) err |= ERR_RANGE;
+    return err;
+}
 
 struct InstDev {
     int32_t model, L, N, ndof;
@@ -94,7 +124,7 @@ struct InstDev {
     int64_t bin_mul;         // global bin = ((E - eglo_u) * bin_mul) >> bin_shift
     int64_t field_off;       // offset into fields (int64 units per site) or -1
     int64_t qtab_off;        // offset into qtab (cos then sin of q_min x, x < L) or -1 without correlators
-    uint64_t seed;
+    uint64_t seed;           // Philox key: instance_key(descriptor seed)
 };
 
 struct WinDev {
@@ -403,7 +433,7 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int li = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (li >= p.nslots) return;
+    if (li >= p.nslots || engine_failed_warp(p.P.counters)) return;
     const DevPtrs& P = p.P;
     const int s = p.slots[li];
     const InstDev I = P.inst[P.slot_inst[s]];
@@ -576,8 +606,8 @@ __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
     for (int k = lane; k < nb; k += 32) {
         const long long gnew = gs[k];
         const long long dv = (gnew - gg[k]) / lnf;
-        gH[k] += (uint32_t)dv;
-        gv[k] += (uint64_t)dv;
+        const int e = commit_visits(gH, gv, k, dv, gnew);
+        if (e) atomicOr(&P.counters[0], e);
         gg[k] = gnew;
     }
     if (lane == 0) {
@@ -652,7 +682,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     const int grp = lane / P, q = lane - grp * P, gbase = grp * P;
     const int li = (blockIdx.x * (blockDim.x >> 5) + wib) * G + grp;
     const bool valid = li < p.nslots;
-    if (__ballot_sync(kFull, valid) == 0) return;             // whole warp without walkers
+    if (__ballot_sync(kFull, valid) == 0 || engine_failed_warp(p.P.counters)) return;   // no walkers, or stopped
     const DevPtrs& P_ = p.P;
     const int s = p.slots[valid ? li : 0];                     // idle groups shadow a walker, never write
     const InstDev I = P_.inst[P_.slot_inst[s]];
@@ -966,8 +996,8 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
         for (int k = q; k < nb; k += P) {
             const long long gnew = gs[k];
             const long long dv = (gnew - gg[k]) / lnf;
-            gH[k] += (uint32_t)dv;
-            gv[k] += (uint64_t)dv;
+            const int e = commit_visits(gH, gv, k, dv, gnew);
+            if (e) atomicOr(&P_.counters[0], e);
             gg[k] = gnew;
         }
         if (q == 0) {
@@ -1116,7 +1146,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep_tables(const SweepParams p)
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int li = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (li >= p.nslots) return;
+    if (li >= p.nslots || engine_failed_warp(p.P.counters)) return;
     const DevPtrs& P = p.P;
     const int s = p.slots[li];
     const InstDev I = P.inst[P.slot_inst[s]];
@@ -1289,11 +1319,10 @@ __global__ void __launch_bounds__(256, 2) k_sweep_tables(const SweepParams p)
     uint32_t* gH = P.H + P.slot_tab[s];
     uint64_t* gv = P.visits + P.slot_tab[s];
     for (int k = lane; k < nb; k += 32) {
-        const long long dg = gg[k] - g0[k];
+        const long long gnew = gg[k], dg = gnew - g0[k];
         if (dg != 0) {
-            const long long dv = dg / lnf;
-            gH[k] += (uint32_t)dv;
-            gv[k] += (uint64_t)dv;
+            const int e = commit_visits(gH, gv, k, dg / lnf, gnew);
+            if (e) atomicOr(&P.counters[0], e);
         }
     }
     if (lane == 0) {
@@ -1322,8 +1351,11 @@ __device__ inline void touch(const DevPtrs& P, const InstDev& I, int slot)
     const int w = P.slot_win[slot];
     if (b < 0 || b >= P.slot_nb[slot]) { atomicOr(&P.counters[0], ERR_BOUNDS); return; }
     const int64_t o = P.slot_tab[slot] + b;
-    P.g[o] += P.win_lnf[w];
-    P.H[o] += 1u;
+    const long long gnew = P.g[o] + P.win_lnf[w];
+    P.g[o] = gnew;
+    if (P.H[o] == 0xFFFFFFFFu) atomicOr(&P.counters[0], ERR_COUNT);   // saturated, as in commit_visits
+    else P.H[o] += 1u;
+    if (gnew >= kLogdosLimit) atomicOr(&P.counters[0], ERR_RANGE);
     const uint64_t seen = P.visits[o];         // the bin's count before this visit
     P.visits[o] = seen + 1u;
     if (P.obs) {
@@ -1399,7 +1431,8 @@ __global__ void k_exchange(DevPtrs P, const int32_t* pairs0, int n0, const int32
     const uint64_t round = *(volatile unsigned long long*)P.xround;
     const int dir = (int)(round & 1u);
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < (dir ? n1 : n0)) exchange_pair(P, dir ? pairs1 : pairs0, k, round);
+    // after a device error no pair moves; the round still advances with the host's mirror
+    if (k < (dir ? n1 : n0) && !engine_failed(P.counters)) exchange_pair(P, dir ? pairs1 : pairs0, k, round);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -1466,7 +1499,7 @@ __device__ inline bool bin_valid(const DevPtrs& P, const WinDev& W, int first_sl
 __global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
 {
     __shared__ unsigned long long red_u[32];
-    __shared__ int flat_sh;
+    __shared__ int flat_sh, stop_sh;
     __shared__ long long g0_sh[kMaxReplicas];
     const DevPtrs& P = fp.P;
     const int w = blockIdx.x;
@@ -1476,8 +1509,13 @@ __global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
     const int first = I.first_slot + W.local * R;
     const int nb = W.nb;
 
-    if (threadIdx.x == 0) { P.win_sweepctr[w] += fp.sweeps_since_check; flat_sh = 1; }
+    if (threadIdx.x == 0) {
+        stop_sh = engine_failed(P.counters);
+        if (!stop_sh) P.win_sweepctr[w] += fp.sweeps_since_check;
+        flat_sh = 1;
+    }
     __syncthreads();
+    if (stop_sh) return;
 
     for (int r = 0; r < R; ++r) {
         const uint32_t* H = P.H + P.slot_tab[first + r];
@@ -1486,7 +1524,7 @@ __global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
         for (int b = threadIdx.x; b < nb; b += blockDim.x) {
             // a window that never goes flat (a replica trapped away from part of its
             // range) lets ln g grow without bound: report it before int64 overflows
-            big |= (unsigned long long)(g[b] > kLogdosLimit || g[b] < -kLogdosLimit);
+            big |= (unsigned long long)(g[b] >= kLogdosLimit || g[b] <= -kLogdosLimit);
             if (!bin_valid(P, W, first, R, b, fp.mask_mode)) continue;
             const unsigned long long h = H[b];
             mn = h < mn ? h : mn; mx = h > mx ? h : mx; sum += h; ++n; zero += (h == 0);
@@ -1498,7 +1536,7 @@ __global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
         zero = block_reduce(zero, OpAdd(), red_u, 0ull);
         big = block_reduce(big, OpMax(), red_u, 0ull);
         if (threadIdx.x == 0) {
-            if (big) atomicOr(&P.counters[0], ERR_RANGE);
+            if (big) { atomicOr(&P.counters[0], ERR_RANGE); flat_sh = 0; }   // no averaging or reset
             bool f;
             if (fp.flat_mode == REWL_FLAT_ALL_VISITED) f = P.win_oot[w] ? true : (zero == 0);
             else if (n == 0 || mn == 0) f = false;
@@ -1649,6 +1687,10 @@ struct rewl_engine {
     uint64_t sweeps_since_check = 0;
     int64_t sweeps_total = 0, cycles = 0, flat_events = 0, flips_total = 0;
     int64_t flips_per_sweep = 0;
+    // sweep launches are split so that one launch adds at most kLaunchGrowth to a bin: an upper
+    // bound of every window's ln f (2^-40 units; k_flat only lowers it, except the 1/t rule,
+    // which never exceeds 1) and the largest number of degrees of freedom of a walker
+    int64_t lnf_bound_u = 0, ndof_max = 0;
     cudaStream_t stream = nullptr;
     std::vector<Launch> launches;
     std::vector<cudaEvent_t> ev_pool;
@@ -1826,7 +1868,8 @@ int build_host(rewl_engine* e)
     if (D.num_instances < 1 || !D.instances) return fail(REWL_EINVAL, "no instances");
     if (D.sweeps_per_exchange < 1 || D.sweeps_per_check < D.sweeps_per_exchange || D.sweeps_per_check % D.sweeps_per_exchange)
         return fail(REWL_EINVAL, "sweeps_per_check must be a positive multiple of sweeps_per_exchange");
-    if (!(D.lnf_initial > 0) || !(D.lnf_final > 0)) return fail(REWL_EINVAL, "ln f must be positive");
+    if (!(D.lnf_initial > 0) || !(D.lnf_final > 0) || D.lnf_initial > 64)
+        return fail(REWL_EINVAL, "ln f must be positive and the initial ln f at most 64");
     if (D.flatness_mode < 0 || D.flatness_mode > 2) return fail(REWL_EINVAL, "bad flatness mode");
     if (D.mask_mode < 0 || D.mask_mode > 1) return fail(REWL_EINVAL, "bad mask mode");
     if (D.rng_mode != REWL_RNG_PHILOX && D.rng_mode != REWL_RNG_REPLAY) return fail(REWL_EINVAL, "bad rng mode");
@@ -1856,7 +1899,7 @@ int build_host(rewl_engine* e)
         InstDev I{};
         I.model = d.model; I.L = d.L; I.N = d.L * d.L; I.ndof = d.model == REWL_MODEL_ISING2D ? I.N : 2 * I.N;
         I.nwin = d.num_windows; I.R = d.replicas_per_window; I.first_win = win; I.first_slot = slot;
-        I.seed = d.seed; I.chunk = largest_chunk(d.L); I.init_mode = d.init_mode;
+        I.seed = instance_key(d.seed); I.chunk = largest_chunk(d.L); I.init_mode = d.init_mode;
         int shift = 0;
         if (d.model == REWL_MODEL_ISING2D) {
             if (d.J != std::floor(d.J) || d.J == 0 || std::fabs(d.J) > 1024) return fail(REWL_EINVAL, "instance %d: Ising J must be a non-zero integer", ii);
@@ -1937,7 +1980,10 @@ int build_host(rewl_engine* e)
         slot += d.num_windows * d.replicas_per_window;
         win += d.num_windows;
         e->flips_per_sweep += (int64_t)d.num_windows * d.replicas_per_window * I.ndof;
+        e->ndof_max = std::max<int64_t>(e->ndof_max, I.ndof);
     }
+    e->lnf_bound_u = std::max<int64_t>(std::max<int64_t>(1, (int64_t)std::llround(D.lnf_initial * kLogdosScale)),
+                                       D.one_over_t ? (int64_t)kLogdosScale : 0);
     e->nslots = slot; e->nwin_total = win;
     e->table_total = tab; e->spin_total = spin; e->mask_total = maskoff;
     // exchange pair lists
@@ -2191,6 +2237,8 @@ int check_device_error(rewl_engine* e)
     if (h[0] & ERR_RANGE)
         return fail(REWL_ESTATE, "a window's logDoS passed 2^62 units (4.2e6 nats) without a flat event: "
                                  "a replica is trapped away from part of its window");
+    if (h[0] & ERR_COUNT)
+        return fail(REWL_ESTATE, "a per-stage histogram count passed 2^32 - 1 without a flat event");
     return REWL_OK;
 }
 
@@ -2253,7 +2301,38 @@ cudaError_t record_timing(rewl_engine* e)
     return e->capturing ? cudaEventRecordWithFlags(ev, e->stream, cudaEventRecordExternal) : cudaEventRecord(ev, e->stream);
 }
 
+// Sweeps per launch such that one launch plus one exchange visit add at most kLaunchGrowth to
+// any bin: lnf_bound x (sweeps x ndof_max + 1) <= kLaunchGrowth.
+int max_launch_sweeps(const rewl_engine* e)
+{
+    const int64_t visits = kLaunchGrowth / std::max<int64_t>(1, e->lnf_bound_u) - 1;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(1 << 20, visits / std::max<int64_t>(1, e->ndof_max)));
+}
+
+// Raise the ln f bound (rewl_set_lnf, rewl_restore); a captured check interval split its sweeps
+// for the old bound, so it is captured again.
+void raise_lnf_bound(rewl_engine* e, int64_t lnf_u)
+{
+    if (lnf_u <= e->lnf_bound_u) return;
+    const int before = max_launch_sweeps(e);
+    e->lnf_bound_u = lnf_u;
+    if (max_launch_sweeps(e) != before) e->drop_graph();
+}
+
+int launch_sweeps_once(rewl_engine* e, int nsweeps);
+
 int launch_sweeps(rewl_engine* e, int nsweeps)
+{
+    const int most = max_launch_sweeps(e);
+    while (nsweeps > 0) {
+        const int n = std::min(nsweeps, most);
+        if (int rc = launch_sweeps_once(e, n)) return rc;
+        nsweeps -= n;
+    }
+    return REWL_OK;
+}
+
+int launch_sweeps_once(rewl_engine* e, int nsweeps)
 {
     const DevPtrs P = e->ptrs();
     CUDA_TRY(record_timing(e));
@@ -2616,6 +2695,7 @@ int rewl_set_lnf(rewl_engine* e, int32_t ii, int32_t w, double lnf)
     if (wi < 0 || !(lnf > 0) || lnf > 64) return fail(REWL_EINVAL, "bad window or ln f");
     const int64_t q = std::max<int64_t>(1, (int64_t)std::llround(lnf * kLogdosScale));
     cudaSetDevice(e->desc.device);
+    raise_lnf_bound(e, q);
     CUDA_TRY(cudaMemcpyAsync(e->win_lnf.p + wi, &q, 8, cudaMemcpyHostToDevice, e->stream));
     const int32_t done = (lnf < e->desc.lnf_final) ? 1 : 0;
     CUDA_TRY(cudaMemcpyAsync(e->win_done.p + wi, &done, 4, cudaMemcpyHostToDevice, e->stream));
@@ -3310,6 +3390,12 @@ int rewl_restore(rewl_engine* e, const void* buffer, size_t bytes)
     const char* src = static_cast<const char*>(buffer) + sizeof h;
     for (auto& p : snapshot_parts(e)) {
         if (p.bytes) CUDA_TRY(cudaMemcpyAsync(p.dev, src, p.bytes, cudaMemcpyHostToDevice, e->stream));
+        if (p.dev == (void*)e->win_lnf.p)          // the restored ln f values bound the launch size
+            for (size_t k = 0; k < p.bytes / 8; ++k) {
+                int64_t v;
+                std::memcpy(&v, src + 8 * k, 8);
+                raise_lnf_bound(e, v);
+            }
         src += (p.bytes + 15) & ~size_t(15);
     }
     const unsigned long long xr[2] = {h.exch_round, 0};
@@ -3353,9 +3439,10 @@ int rewl_autotune(rewl_engine* e, int32_t sweeps)
         int64_t dof = 0;
         for (int s : l.slots) dof += e->inst[e->h_slot_inst[s]].dev.ndof;
         // about 2e7 attempted flips of the group per trial, at least one sweep
-        const int ts = sweeps > 0 ? sweeps
-                                  : (int)std::max<int64_t>(1, std::min<int64_t>(e->desc.sweeps_per_exchange,
-                                                                                 20000000 / std::max<int64_t>(1, dof)));
+        const int ts = std::min(max_launch_sweeps(e),
+                                sweeps > 0 ? sweeps
+                                           : (int)std::max<int64_t>(1, std::min<int64_t>(e->desc.sweeps_per_exchange,
+                                                                                          20000000 / std::max<int64_t>(1, dof))));
         std::vector<std::pair<int, int>> cand;
         // the bin-tracking kernel takes at most 4 warps per block (its launch bounds); 4 walkers
         // per warp is left to the planner's rule for very large batches

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -452,8 +453,8 @@ cudaError_t launch_gemm(cudaStream_t st, const GemmArgs& g, int splits)
 }
 
 // The tensor-core GEMMs need more than the default 48 KB of dynamic shared memory.  Set
-// once per device when a network is created, so that launches made while a stream is
-// being captured (rewl_mlp_predict_noalloc) need no attribute call.
+// once per device when a network is created, so that rewl_mlp_predict_noalloc, which only
+// enqueues work, makes no attribute call.
 cudaError_t prepare_tc_kernels()
 {
     const void* kernels[] = {
@@ -610,7 +611,7 @@ struct rewl_mlp {
     int nall = 0;
     int64_t step = 0;
     uint64_t seed = 1;
-    int64_t launches = 0;
+    std::atomic<int64_t> launches{0};   // calls on one network from several threads may overlap
 
     void release()
     {
@@ -961,12 +962,14 @@ int rewl_mlp_launches(const rewl_mlp* m, int64_t* n)
 // Allocation-free prediction (rewl_mlp_predict_noalloc).
 //
 // rewl_mlp_predict grows its activation buffers with cudaMalloc when a larger
-// batch arrives and stages inputs through host memory.  Callers that must not
-// allocate -- code enqueuing work while a CUDA stream is being captured, or a
-// loop holding device memory at its limit -- use this variant instead: inputs
-// and outputs are device pointers owned by the caller, and the activations live
-// in one file-scope static device array.  Its address is looked up once per
-// device (cudaGetSymbolAddress with that device current) on the first call.
+// batch arrives and stages inputs through host memory.  Some callers cannot do
+// that: a host program whose own allocator already holds the device's memory, a
+// loop running at its device-memory limit, or a driver loop that must not stall,
+// since cudaMalloc may synchronise the device.  They use this variant instead:
+// inputs and outputs are device pointers owned by the caller, and the activations
+// live in one file-scope static device array.  Its address is looked up once per
+// device (cudaGetSymbolAddress with that device current) on the first call, so
+// make that first call before any stream capture.
 //
 // Limits: at most kNoAllocMaxRows rows per call and hidden width at most
 // kNoAllocMaxHidden (9.5 MiB of scratch); larger requests fail with REWL_EINVAL.
@@ -975,6 +978,11 @@ int rewl_mlp_launches(const rewl_mlp* m, int64_t* n)
 // is shared by every network on a device, so calls that may overlap -- on
 // different streams, or from different host threads -- race on it and must be
 // ordered by the caller (for example, issue them on one stream).
+//
+// The call never waits for the GPU, so a GEMM whose bounded wait ran out cannot
+// be reported by its return code: the last kernel then writes NaN to every y
+// instead of the stale scratch, for as long as the timeout flag stands (it is
+// reported and cleared by the next rewl_mlp_* call that synchronises).
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -1025,7 +1033,8 @@ __global__ void k_noalloc_stage(const float* X, int n, int in_dim, int rows, bf1
 __global__ void k_noalloc_take(const float* out, int n, float* y)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = out[(size_t)i * kOut];
+    const bool timed_out = *reinterpret_cast<const volatile int*>(&g_tc_error) != 0;
+    if (i < n) y[i] = timed_out ? __int_as_float(0x7FC00000) : out[(size_t)i * kOut];
 }
 
 template <int EPI>
@@ -1035,6 +1044,8 @@ cudaError_t noalloc_layer(cudaStream_t st, const bf16* A, const bf16* W, int M, 
     const GemmArgs g{A, W, M, N, K, K, K, K, Cf, Cb, N, bias};
     return launch_gemm<false, true, EPI>(st, g, 1);
 }
+
+int predict_noalloc_on_device(rewl_mlp* m, const float* X, int32_t n, int32_t in_dim, float* y, void* stream);
 
 } // namespace
 
@@ -1047,7 +1058,20 @@ extern "C" int rewl_mlp_predict_noalloc(rewl_mlp* m, const float* X, int32_t n, 
     if (m->hidden > kNoAllocMaxHidden)
         return mfail(REWL_EINVAL, "rewl_mlp_predict_noalloc: hidden width %d exceeds the static scratch limit of %d",
                      m->hidden, kNoAllocMaxHidden);
+    int caller_device = 0;
+    MCUDA(cudaGetDevice(&caller_device));
     MCUDA(cudaSetDevice(m->device));
+    const int rc = predict_noalloc_on_device(m, X, n, in_dim, y, stream);
+    // leave the caller's current device as it was, whatever happened
+    const cudaError_t back = cudaSetDevice(caller_device);
+    if (rc) return rc;
+    if (back != cudaSuccess) return mfail(REWL_EDEVICE, "restoring the current device: %s", cudaGetErrorString(back));
+    return REWL_OK;
+}
+
+namespace {
+int predict_noalloc_on_device(rewl_mlp* m, const float* X, int32_t n, int32_t in_dim, float* y, void* stream)
+{
     unsigned char* s = nullptr;
     int rc = noalloc_scratch(m->device, &s);
     if (rc) return rc;
@@ -1076,3 +1100,4 @@ extern "C" int rewl_mlp_predict_noalloc(rewl_mlp* m, const float* X, int32_t n, 
     m->launches += L + 3;
     return REWL_OK;
 }
+} // namespace

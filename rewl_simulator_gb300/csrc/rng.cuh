@@ -33,6 +33,18 @@ enum : uint32_t {
 
 struct Philox4 { uint32_t x, y, z, w; };
 
+// Philox key of an instance from its seed: the SplitMix64 finaliser (Steele, Lea, Flood,
+// "Fast splittable pseudorandom number generators", OOPSLA 2014).  Walker keys are
+// (key_lo ^ walker, key_hi); mixing first keeps instances whose seeds differ only in low bits
+// from handing their walkers each other's streams.
+REWL_HD uint64_t instance_key(uint64_t seed)
+{
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
 REWL_HD uint32_t mulhi32(uint32_t a, uint32_t b)
 {
 #if defined(__CUDA_ARCH__)

@@ -1,8 +1,8 @@
 """Generate the golden fixtures in tests/golden/ (run in a container that has the
 reference sources; the fixtures are committed so the tests need no reference).
 
-    python tests/golden/make_golden.py            # everything
-    python tests/golden/make_golden.py replay     # one group
+    REWL_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py            # everything
+    REWL_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py replay     # one group
 
 Groups
   replay   -- the reference's own REWL_Walker (oracle/build_ref.py harness):

@@ -1,11 +1,13 @@
-"""Walkers stay inside their windows whatever their logDoS holds.
+"""Walkers stay inside their windows whatever their logDoS holds, and no logDoS entry can
+overflow int64.
 
-The bin-tracking Ising sweep rejects proposals outside the window through guard
-bins that hold INT64_MAX, so no value of g at the current bin can let a walker
-step out of its window's table.  A window whose logDoS grows past 2^62 grid
-units without a flat event (a replica trapped away from part of its range, so
-the window never goes flat) is reported as REWL_ESTATE at the next flatness
-check instead of being left to overflow int64.
+The bin-tracking Ising sweep rejects proposals outside the window through guard bins that
+hold INT64_MAX, so no value of g at the current bin can let a walker step out of its window's
+table.  Every kernel that adds to g checks the values it wrote against 2^62 grid units
+(4.2e6 nats) and, once one passes, the engine stops with REWL_ESTATE: every later kernel
+returns without work.  Sweep launches are split so that one launch adds at most
+2^62 - 2^58 units to a bin (here ln f = 64 nats at L = 16: at most 240 sweeps per launch), so
+the largest value ever stored stays below 2^63.
 """
 import numpy as np
 import pytest
@@ -13,10 +15,12 @@ import pytest
 from rewl_simulator_gb300.engine import REWL_ESTATE
 
 UNITS = 2.0 ** 40                 # logDoS grid: 2^-40 nats
+LIMIT = 2.0 ** 62 / UNITS         # 4.19e6 nats
+INT64_TOP = 2.0 ** 63 / UNITS     # 8.39e6 nats
 
 
 @pytest.mark.gpu
-def test_walkers_stay_in_window_with_logdos_beyond_2_62_units(engine_lib):
+def test_logdos_past_the_limit_stops_the_engine_before_int64_overflow(engine_lib):
     rg = engine_lib
     L, N = 16, 256
     ins = rg.Instance(model=rg.MODEL_ISING2D, L=L, energy_min=-2.0 * N, energy_max=2.0 * N + 4, bin_width=4.0,
@@ -28,18 +32,62 @@ def test_walkers_stay_in_window_with_logdos_beyond_2_62_units(engine_lib):
             eng.set_logdos(0, w, np.full(nb, 1e6))
             eng.set_lnf(0, w, 64.0)                       # 64 nats per visit: g climbs fast
         walkers = [(eng.walker_id(0, w, r), w) for w in range(len(wins)) for r in range(2)]
-        top = 0.0
-        for _ in range(14):
-            eng.run_sweeps(1000)                          # raises on a device error word
+
+        def check_walkers():
+            top = 0.0
             for wk, w in walkers:
                 out = eng.export_walker(wk)
                 lo, hi, nb = wins[w]
                 E = float(out["state"][0])
                 assert lo <= E < hi, (wk, w, E, lo, hi)
-                top = max(top, float(out["logdos"].max()))
-            if top > 4.5e6:
+                g = out["logdos"]
+                assert np.isfinite(g).all() and g.min() >= 1e6 - 1e-6      # only grows: no wrap
+                top = max(top, float(g.max()))
+            return top
+
+        stopped = None
+        for k in range(40):
+            try:
+                eng.run_sweeps(1000)
+            except rg.REWLError as err:
+                stopped = err
                 break
-        assert top * UNITS > 2.0 ** 62 + 2.0 ** 58, top   # past the old guard value 2^62
-        with pytest.raises(rg.REWLError) as err:
-            eng.check_flat()
-        assert err.value.code == REWL_ESTATE
+            assert check_walkers() < LIMIT
+        assert stopped is not None and stopped.code == REWL_ESTATE, stopped
+        top = check_walkers()
+        assert LIMIT <= top < INT64_TOP, top                # past the limit, far from overflow
+        # the engine has stopped: later calls report it and change nothing
+        before = eng.export_walker(0)["logdos"].copy()
+        with pytest.raises(rg.REWLError) as again:
+            eng.run_sweeps(10)
+        assert again.value.code == REWL_ESTATE
+        np.testing.assert_array_equal(eng.export_walker(0)["logdos"], before)
+
+
+@pytest.mark.gpu
+def test_large_lnf_splits_launches_without_changing_results(engine_lib, oracle_lib):
+    """ln f = 32 nats on L = 24 allows at most (2^62 - 2^58) / (32 x 2^40) / 576 = 213 sweeps per
+    launch: an exchange interval of 500 sweeps becomes three launches, bit for bit the oracle's
+    run."""
+    rg, po = engine_lib, oracle_lib
+    L, N = 24, 576
+    ins = rg.Instance(model=0, L=L, energy_min=-2.0 * N, energy_max=2.0 * N + 4, bin_width=4.0, num_windows=4,
+                      replicas_per_window=2, seed=5)
+    b = rg.Batch(instances=[ins], sweeps_per_exchange=500, sweeps_per_check=1000, lnf_initial=32.0, lnf_final=1e-6)
+    cfg = po.Config(model=0, L=L, nwin=4, R=2, sweeps_per_exchange=500, sweeps_per_check=1000, emin=-2.0 * N,
+                    emax=2.0 * N + 4, bw=4.0, lnf0=32.0, lnf_final=1e-6, semantics=po.SEM_ENGINE, seed=5)
+    orc = po.Oracle(cfg)
+    with rg.Engine(b) as eng:
+        st0 = eng.status()
+        eng.run_cycles(1)
+        orc.cycle()
+        st = eng.status()
+        # 2 exchange intervals x 3 launches + 2 exchanges + 1 flatness step
+        assert st.kernel_launches - st0.kernel_launches == 9, st.kernel_launches - st0.kernel_launches
+        for s in range(8):
+            out = eng.export_walker(s)
+            c, g, v = orc.tables(s)
+            np.testing.assert_array_equal(out["counts"], c)
+            np.testing.assert_array_equal(out["logdos"], g)
+            np.testing.assert_array_equal(out["dofs"], orc.dofs(s))
+    orc.close()

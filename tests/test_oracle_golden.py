@@ -185,7 +185,7 @@ def test_oracle_converges_to_the_exact_dos(oracle_lib, semantics, one_over_t):
     assert np.max(np.abs(lng - exact[valid])) < (0.03 if one_over_t else 0.1)
 
 
-@pytest.mark.parametrize("semantics,seed", [("reference", 1), ("engine", 4)])
+@pytest.mark.parametrize("semantics,seed", [("reference", 1), ("engine", 14)])
 def test_sequential_sweep_can_lock_into_a_global_flip_orbit(oracle_lib, semantics, seed):
     """A property of the reference's algorithm, kept by the oracle (and bit for bit by the engine):
     a walker sweeping the sites in a fixed order can reach a configuration from which every

@@ -54,3 +54,40 @@ def test_accept_threshold_exact(oracle_lib):
             assert (d < T) == _float_lt(d, thr), (thr, T, d)
         for d in rng.integers(1, max(2, 4 * T), 50):
             assert (int(d) < T) == _float_lt(int(d), thr), (thr, T, int(d))
+
+
+def _splitmix64_finaliser(seed: int) -> int:
+    """SplitMix64's output function (Steele, Lea, Flood, OOPSLA 2014), the instance-key mix."""
+    m = (1 << 64) - 1
+    z = (seed + 0x9E3779B97F4A7C15) & m
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    return z ^ (z >> 31)
+
+
+def test_nearby_seeds_give_distinct_walker_keys():
+    """Walker keys are (key_lo ^ walker, key_hi) with key = mix(seed).  Without the mix, seeds
+    that differ in bits below the walker count handed their walkers each other's keys; with it,
+    no two walkers of a thousand consecutive seeds x 64 walkers share a key."""
+    keys = set()
+    for seed in range(1000):
+        k = _splitmix64_finaliser(seed)
+        for w in range(64):
+            keys.add(((k & 0xFFFFFFFF) ^ w, k >> 32))
+    assert len(keys) == 1000 * 64
+    assert _splitmix64_finaliser(0) == 0xE220A8397B1DCDAF       # SplitMix64's first output from state 0
+
+
+def test_seeds_two_and_three_no_longer_run_identically(oracle_lib):
+    po = oracle_lib
+    runs = []
+    for seed in (2, 3):
+        cfg = po.Config(model=po.MODEL_ISING, L=4, nwin=1, R=2, sweeps_per_exchange=20, sweeps_per_check=40,
+                        emin=-32.0, emax=36.0, bw=4.0, semantics=po.SEM_ENGINE, seed=seed)
+        orc = po.Oracle(cfg)
+        for _ in range(3):
+            orc.cycle()
+        runs.append([orc.tables(s)[0].copy() for s in range(2)])
+        orc.close()
+    assert not np.array_equal(runs[0][0], runs[1][1]) and not np.array_equal(runs[0][1], runs[1][0])
+    assert not np.array_equal(runs[0][0], runs[1][0])
