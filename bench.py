@@ -1,32 +1,42 @@
 #!/usr/bin/env python3
 """Benchmark of the REWL hot path on GB300.
 
-Workload (the batched configuration the headline metric is quoted on): 2D Ising,
-L = 32 periodic, J = 1, energy levels -2048..2048 step 4 (bins of width 4 over
-[-2048, 2052)), 16 equal windows at 75 % overlap x 8 walkers = 128 walkers in one
-launch, int8 spins, replica exchange every 500 sweeps, flatness (min >= 0.8 mean)
-checked every 1000 sweeps, ln f halved from 1 towards 1e-8, int64 logDoS in 2^-40
-units.  Inputs are synthetic (spins drawn from the seed).
+Default workload (the configuration the headline metric is quoted on): 2D Ising,
+L = 64 periodic, J = 1, energy levels -8192..8192 step 4 (bins of width 4 over
+[-8192, 8196)), 64 equal windows at 75 % overlap x 8 walkers = 512 walkers, int8
+spins, replica exchange every 500 sweeps, flatness (min >= 0.8 mean over the valid
+levels) checked every 1000 sweeps, ln f from 1 with the reference's default 1/t
+schedule (ONE_OVER_T_ALGORITHM), walkers started from all spins +1 as the
+reference's are, int64 logDoS in 2^-40 units.  Inputs are synthetic.
 
-A step is one check interval: 2 x (500 sweeps of all 128 walkers + one replica
-exchange round) + the flatness / averaging / ln f kernel, i.e. 131,072,000
-attempted single-spin flips.  `value` is attempted flips per second over the
-whole job (device time, CUDA events on the engine's stream, L2 flushed between
-steps by a 256 MiB write).  `e2e` runs the same steps through the public API with
-the walker state host-resident in pinned memory: restore (H2D) + step +
-snapshot (D2H) per step, wall clock.
+A step is one check interval: 2 x (500 sweeps of all 512 walkers + one replica
+exchange round) + the flatness / averaging / ln f kernel, i.e. 2,097,152,000
+attempted single-spin flips.  `value` is attempted flips per second over the whole
+job (device time, CUDA events on the engine's stream, L2 flushed between steps by a
+256 MiB write).  `e2e` runs the same steps through the public API with the walker
+state host-resident in pinned memory: restore (H2D) + step + snapshot (D2H) per
+step, wall clock.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}] [--tta]
+The default line also carries `time_to_accuracy`: for the same L = 64 system, the
+simulation time until the concatenated, normalised ln g is within each of a ladder
+of tolerances (1 .. 1e-2) of the exact density of states (Beale), for the MLP warm
+start (trained here on plain GPU runs at L <= 32) and for plain WL from ln f0 = 1,
+each capped at --tta-seconds; and the same criterion for 2D Ising L = 16 (4 windows x
+8 walkers) run to 1e-2 on the GPU, whose CPU counterpart is the reference arm's
+`time_to_accuracy`.
 
---impl reference times the CPU restatement of the reference's hot path (the
-oracle port, reference semantics: mt19937_64 streams, draw-on-demand, FP64
-logDoS) on all host cores for the same workload; under torchrun only rank 0 runs.
---tta additionally measures, for 2D Ising L=64 (64 windows x 8 walkers), the wall
-time until the concatenated, normalised ln g is within each of a ladder of
-tolerances (1 .. 1e-2) of the exact density of states, for the MLP warm start
-(trained here on plain GPU runs at L <= 32) and for plain WL from ln f0 = 1, both
-with the reference's default build: the 1/t schedule (ONE_OVER_T_ALGORITHM) and
-every walker started from all spins +1.
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
+                    [--workload {c5,c2,at,mixed}] [--observables {0,1,2}] [--no-tta]
+                    [--at-spread CYCLES]
+
+Other workloads: c2 (Ising L = 32, 16 windows x 8 walkers), at (Ashkin-Teller L = 32,
+K = 0.5, Baxter fields sigma 0.5, bins of 0.05, 64 realisations x 8 windows x 4
+walkers), mixed (Ising L = 16..48 and Ashkin-Teller L = 24 at three K in one batch).
+
+--impl reference times the CPU restatement of the reference's hot path (the oracle
+port, reference semantics: mt19937_64 streams, draw-on-demand, FP64 logDoS) on all
+host cores for the same workload, and runs Ising L = 16 (4 windows x 8 walkers) to
+max |d ln g| <= 1e-2 on those cores; under torchrun only rank 0 runs.
 """
 from __future__ import annotations
 
@@ -46,19 +56,35 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "time to ln g within 1e-2 of exact, MLP warm-start vs plain WL, 1 GB300; flips/s"
+# Cycles per attempted flip of one walker's accept chain at the speed of light of the
+# bin-tracking kernel's design, from probe kernels on a GB300: a dependent shared-memory load
+# (29 cycles) plus a 64-bit compare and select (11 cycles).
+CHAIN_FLOOR_CYCLES = 40.0
+
+
+def _ising_workload(name, L, nwin, R, se, sc, lnf_final, one_over_t, init_mode, profile):
+    N = L * L
+    return dict(name=name, model="ising2d", L=L, energy_min=-2.0 * N, energy_max=2.0 * N + 4, bin_width=4.0,
+                num_windows=nwin, replicas_per_window=R, window_overlap=0.75, sweeps_per_exchange=se,
+                sweeps_per_check=sc, lnf_initial=1.0, lnf_final=lnf_final, one_over_t=one_over_t,
+                init_mode=init_mode, flatness="min >= 0.8 mean over valid levels", realizations=1,
+                bytes_per_flip=46, kernel="k_sweep_ising_bins", bound="latency", profile=profile, graphs=1)
+
+
 WORKLOADS = {
-    # the headline configuration (default)
-    "ising": dict(name="ising2d_L32_16win_x8walkers_rewl", model="ising2d", L=32, energy_min=-2048.0,
-                  energy_max=2052.0, bin_width=4.0, num_windows=16, replicas_per_window=8, window_overlap=0.75,
-                  sweeps_per_exchange=500, sweeps_per_check=1000, lnf_initial=1.0, lnf_final=1e-8,
-                  flatness="min >= 0.8 mean over valid bins", realizations=1,
-                  bytes_per_flip=46, kernel="k_sweep_ising_bins", profile="sweep_ising_L32_rewl.md"),
+    # the headline configuration (default): 2D Ising L = 64, 64 windows x 8 walkers
+    "c5": _ising_workload("ising2d_L64_64win_x8walkers_rewl", 64, 64, 8, 500, 1000, 1e-8, 1, 1,
+                          "sweep_ising_L64_64x8_rewl.md"),
+    # batched Ising L = 32, 16 windows x 8 walkers, halving ln f 1 -> 1e-8, random initial spins
+    "c2": _ising_workload("ising2d_L32_16win_x8walkers_rewl", 32, 16, 8, 500, 1000, 1e-8, 0, 0,
+                          "sweep_ising_L32_rewl.md"),
     # 2D Ashkin-Teller, K = 0.5, Gaussian Baxter fields (sigma 0.5), 64 realisations x 8 windows x 4 walkers
     "at": dict(name="ashkin_teller2d_L32_K0.5_h0.5_64real_8win_x4walkers_rewl", model="ashkin_teller2d", L=32, K=0.5,
                sigma_h=0.5, energy_min=-5120.0, energy_max=0.0, bin_width=0.05, num_windows=8, replicas_per_window=4,
                window_overlap=0.75, sweeps_per_exchange=100, sweeps_per_check=200, lnf_initial=1.0, lnf_final=1e-7,
-               flatness="min >= 0.8 mean over visited bins", realizations=64,
-               bytes_per_flip=51, kernel="k_sweep_tables<AshkinTeller2dModel>", profile="sweep_at_L32_64real_rewl.md"),
+               flatness="min >= 0.8 mean over visited bins", realizations=64, one_over_t=0, init_mode=0,
+               bytes_per_flip=51, kernel="k_sweep_tables<AshkinTeller2dModel>", bound="latency",
+               profile="sweep_at_L32_64real_rewl.md", graphs=0),
 }
 
 
@@ -82,12 +108,12 @@ def _mixed_components():
 WORKLOADS["mixed"] = dict(
     name="mixed_ising_L16_24_32_48_x16win_x4_at_L24_K0.25_0.5_0.75_x32real_x8win_x4_rewl", model="mixed",
     components=_mixed_components(), sweeps_per_exchange=100, sweeps_per_check=200, lnf_initial=1.0,
-    lnf_final=1e-8, flatness="min >= 0.8 mean over visited bins", realizations=1,
-    kernel="k_sweep_tables<AshkinTeller2dModel> + k_sweep_ising_bins (launch groups on concurrent streams)", profile="",
-    graphs=1, autotune=1)
+    lnf_final=1e-8, flatness="min >= 0.8 mean over visited bins", realizations=1, one_over_t=0, init_mode=0,
+    kernel="k_sweep_tables<AshkinTeller2dModel> + k_sweep_ising_bins (launch groups on concurrent streams)",
+    bound="latency", profile="", graphs=1, autotune=1)
 for _c in WORKLOADS["mixed"]["components"]:
     _c["bytes_per_flip"] = 46 if _c["model"] == "ising2d" else 51
-WORKLOAD = WORKLOADS["ising"]
+WORKLOAD = WORKLOADS["c5"]
 
 
 def select_workload(name: str) -> None:
@@ -151,24 +177,29 @@ def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        return float(d["hbm_gbs"]), float(d.get("sm_max_mhz", 2070.0)), "measured"
+    return 6800.0, 2070.0, "fallback"
 
 
-def traffic_per_launch():
-    """dram bytes per sweep-kernel launch from the committed ncu summary, if any."""
+def profile_figures():
+    """Figures of the committed ncu summary of the workload's sweep kernel, if any: lines
+    `key: value ...` (traffic per launch, shared-memory and issue throughput)."""
     if not WORKLOAD["profile"]:
-        return None
+        return {}
     p = ROOT / "profiles" / WORKLOAD["profile"]
     if not p.exists():
-        return None
+        return {}
+    out = {}
     for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+        for key in ("traffic_bytes_per_launch", "shared_throughput_pct", "l1_throughput_pct",
+                    "issue_slots_busy_pct", "dram_throughput_pct", "warps_active_pct", "ncu_workload"):
+            if line.startswith(key + ":"):
+                val = line.split(":", 1)[1].strip()
+                try:
+                    out[key] = float(val.split()[0])
+                except ValueError:
+                    out[key] = val
+    return out
 
 
 class ClockSampler:
@@ -227,13 +258,13 @@ class ClockSampler:
 
 
 def instance_seed(seed: int, k: int) -> int:
-    """Seed of the k-th instance of a batch: a multiple of 2^20, so that no two walkers of the
-    batch (fewer than 2^20 per instance) share a Philox key (walker keys are seed XOR walker)."""
-    return (seed * 100000 + k) << 20
+    """Seed of the k-th instance of a batch (the engine mixes it into the walkers' Philox keys)."""
+    return seed * 100000 + k
 
 
-def make_batch(rg, seed: int, device: int):
+def make_batch(rg, seed: int, device: int, observables: int | None = None):
     w = WORKLOAD
+    obs = w.get("observables", 0) if observables is None else observables
     if w["model"] == "mixed":
         inss = []
         for ci, c in enumerate(w["components"]):
@@ -248,12 +279,12 @@ def make_batch(rg, seed: int, device: int):
         return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
                         sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
                         lnf_final=w["lnf_final"], device=device, mask_mode=rg.MASK_VISITED,
-                        graphs=w["graphs"], autotune=w["autotune"])
+                        graphs=w["graphs"], autotune=w["autotune"], observables=obs)
     if w["model"] == "ising2d":
         inss = [rg.Instance(model=rg.MODEL_ISING2D, L=w["L"], energy_min=w["energy_min"], energy_max=w["energy_max"],
                             bin_width=w["bin_width"], num_windows=w["num_windows"],
                             replicas_per_window=w["replicas_per_window"], window_overlap=w["window_overlap"],
-                            seed=seed)]
+                            init_mode=w["init_mode"], seed=seed)]
         mask = rg.MASK_STATIC
     else:
         inss = [rg.Instance(model=rg.MODEL_ASHKIN_TELLER2D, L=w["L"], K=w["K"], fields=at_fields(w, k),
@@ -264,18 +295,39 @@ def make_batch(rg, seed: int, device: int):
         mask = rg.MASK_VISITED
     return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
                     sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
-                    lnf_final=w["lnf_final"], device=device, mask_mode=mask, observables=w.get("observables", 0))
+                    lnf_final=w["lnf_final"], device=device, mask_mode=mask, observables=obs,
+                    one_over_t=w["one_over_t"], graphs=w["graphs"])
 
 
 # --------------------------------------------------------------------------- CPU leg
-def cpu_port_rate(target_seconds: float, threads: int, steps: int | None = None, warmup: int = 0):
+def _port_config(po, w, threads, observables=0, seed=2024):
+    at = w["model"] != "ising2d"
+    return po.Config(model=po.MODEL_AT if at else po.MODEL_ISING, L=w["L"], K=w.get("K", 0.0),
+                     escale_bits=20 if at else 0, nwin=w["num_windows"], R=w["replicas_per_window"],
+                     sweeps_per_exchange=w["sweeps_per_exchange"], sweeps_per_check=w["sweeps_per_check"],
+                     emin=w["energy_min"], emax=w["energy_max"], bw=w["bin_width"], overlap=w["window_overlap"],
+                     lnf0=w["lnf_initial"], lnf_final=w["lnf_final"], semantics=po.SEM_REFERENCE, nthreads=threads,
+                     mask_mode=po.MASK_VISITED if at else po.MASK_STATIC, one_over_t=w.get("one_over_t", 0),
+                     init_mode=w.get("init_mode", 0), observables=observables, seed=seed)
+
+
+def sample_sweeps(w) -> int:
+    """Sweeps per timed CPU sample: about 2e8 attempted flips of the instance (one exchange
+    interval at most), so that a sample takes about a second on the host cores."""
+    per = w["num_windows"] * w["replicas_per_window"] * ndof(w)
+    return int(max(1, min(w["sweeps_per_exchange"], 200_000_000 // per)))
+
+
+def cpu_port_rate(target_seconds: float, threads: int, steps: int | None = None, warmup: int = 0,
+                  observables: int = 0):
     """Flips/s of the oracle port (reference semantics) on `threads` host threads (one instance:
     the port drives one instance at a time, so for a batch of realisations it times one of them).
+    A sample is sample_sweeps() sweeps of every walker followed by one replica-exchange round.
     For the uneven batch, one instance of every component is timed and the rate is the batch's
     flips over the time the CPU needs for all of them."""
     if WORKLOAD["model"] == "mixed":
         return _cpu_port_rate_mixed(target_seconds, threads, steps, warmup)
-    return _cpu_port_rate_one(WORKLOAD, target_seconds, threads, steps, warmup)
+    return _cpu_port_rate_one(WORKLOAD, target_seconds, threads, steps, warmup, observables)
 
 
 def _cpu_port_rate_mixed(target_seconds, threads, steps, warmup):
@@ -286,33 +338,28 @@ def _cpu_port_rate_mixed(target_seconds, threads, steps, warmup):
                  lnf_initial=WORKLOAD["lnf_initial"], lnf_final=WORKLOAD["lnf_final"])
         rate, n, total, ts = _cpu_port_rate_one(w, target_seconds / len(comps), threads,
                                                 None if steps is None else max(1, steps // len(comps)), 0)
-        cpu_s += flips_per_sweep(c) * WORKLOAD["sweeps_per_check"] / rate     # one check interval of component c
+        cpu_s += flips_per_sweep(c) / rate     # one sweep of component c
         n_total += n
         t_total += total
         times += ts
-    return flips_per_sweep(WORKLOAD) * WORKLOAD["sweeps_per_check"] / cpu_s, n_total, t_total, times
+    return flips_per_sweep(WORKLOAD) / cpu_s, n_total, t_total, times
 
 
-def _cpu_port_rate_one(w, target_seconds, threads, steps, warmup):
+def _cpu_port_rate_one(w, target_seconds, threads, steps, warmup, observables=0):
     from oracle import pyoracle as po
     at = w["model"] != "ising2d"
-    cfg = po.Config(model=po.MODEL_AT if at else po.MODEL_ISING, L=w["L"], K=w.get("K", 0.0),
-                    escale_bits=20 if at else 0, nwin=w["num_windows"], R=w["replicas_per_window"],
-                    sweeps_per_exchange=w["sweeps_per_exchange"], sweeps_per_check=w["sweeps_per_check"],
-                    emin=w["energy_min"], emax=w["energy_max"], bw=w["bin_width"], overlap=w["window_overlap"],
-                    lnf0=w["lnf_initial"], lnf_final=w["lnf_final"], semantics=po.SEM_REFERENCE, nthreads=threads,
-                    mask_mode=po.MASK_VISITED if at else po.MASK_STATIC, seed=2024)
-    orc = po.Oracle(cfg, fields=at_fields(w, 0) if at else None)
-    w = dict(w, realizations=1)
+    orc = po.Oracle(_port_config(po, w, threads, observables), fields=at_fields(w, 0) if at else None)
+    sweeps = sample_sweeps(w)
     fps = w["num_windows"] * w["replicas_per_window"] * ndof(w)
     for _ in range(warmup):
-        orc.run_sweeps(w["sweeps_per_exchange"])
+        orc.run_sweeps(max(1, sweeps // 10))
     times = []
     done_steps = 0
     t_start = time.perf_counter()
     while True:
         t0 = time.perf_counter()
-        orc.cycle()
+        orc.run_sweeps(sweeps)
+        orc.exchange()
         times.append(time.perf_counter() - t0)
         done_steps += 1
         if steps is not None:
@@ -322,8 +369,75 @@ def _cpu_port_rate_one(w, target_seconds, threads, steps, warmup):
             break
     orc.close()
     total = sum(times)
-    rate = done_steps * w["sweeps_per_check"] * fps / total
+    rate = done_steps * sweeps * fps / total
     return rate, done_steps, total, times
+
+
+def _sample_text(n, total):
+    w = WORKLOAD
+    if w["model"] == "mixed":
+        return (f"{n} samples of one instance of each of the {len(w['components'])} components "
+                f"({sample_sweeps(w['components'][0])} sweeps + exchange each, {total:.1f} s)")
+    return (f"{n} samples of one instance of the workload ({w['num_windows'] * w['replicas_per_window']} walkers; "
+            f"each sample {sample_sweeps(w)} sweeps of every walker + one exchange round, {total:.1f} s)")
+
+
+# Time to accuracy: Ising L = 16, 4 windows x 8 walkers, to 1e-2 (both arms run it)
+SMALL_TTA = dict(L=16, num_windows=4, replicas_per_window=8, sweeps_per_exchange=500, sweeps_per_check=1000,
+                 tolerance=1e-2, cap_seconds=150.0)
+TTA_TOLERANCES = [1.0, 0.5, 0.3, 0.2, 0.15, 0.1, 0.08, 0.05, 0.03, 0.02, 0.01]
+
+
+def exact_lng(L: int):
+    z = np.load(ROOT / "tests" / "golden" / f"exact_ising_L{L}.npz")
+    return dict(zip(z["E"].astype(np.int64).tolist(), z["lng"]))
+
+
+def _max_error(E, g, exact) -> float:
+    return float(np.max(np.abs([g[i] - exact[int(round(E[i]))] for i in range(len(E))])))
+
+
+def cpu_small_tta(threads: int):
+    """The reference's algorithm (oracle port, reference semantics) on the host cores: Ising
+    L = 16, 4 windows x 8 walkers, 1/t, walkers from all +1, until max |d ln g| <= 1e-2 against the
+    exact density of states or the cap.  The clock stops while the accuracy is evaluated."""
+    from oracle import pyoracle as po
+    import rewl_simulator_gb300 as rg
+    s = SMALL_TTA
+    L, N = s["L"], s["L"] ** 2
+    w = dict(model="ising2d", L=L, energy_min=-2.0 * N, energy_max=2.0 * N + 4, bin_width=4.0,
+             num_windows=s["num_windows"], replicas_per_window=s["replicas_per_window"], window_overlap=0.75,
+             sweeps_per_exchange=s["sweeps_per_exchange"], sweeps_per_check=s["sweeps_per_check"], lnf_initial=1.0,
+             lnf_final=1e-12, one_over_t=1, init_mode=1)
+    orc = po.Oracle(_port_config(po, w, threads, seed=5))
+    exact = exact_lng(L)
+    hit, t_sim, cycles, best, flips = {}, 0.0, 0, float("inf"), 0
+    per_cycle = s["sweeps_per_check"] * s["num_windows"] * s["replicas_per_window"] * N
+    while t_sim < s["cap_seconds"]:
+        t0 = time.perf_counter()
+        orc.cycle()
+        t_sim += time.perf_counter() - t0
+        cycles += 1
+        flips += per_cycle
+        wins = []
+        for k in range(s["num_windows"]):
+            lo, _, _, nb = orc.windows[k]
+            m = orc.window_mask(k)
+            wins.append(((lo + 4.0 * np.arange(nb))[m], orc.window_logdos(k)[m]))
+        E, g = rg.concatenate_windows(wins, 2.0, N)
+        err = _max_error(E, g, exact)
+        best = min(best, err)
+        for tol in TTA_TOLERANCES:
+            if err <= tol and str(tol) not in hit:
+                hit[str(tol)] = round(t_sim, 2)
+        if err <= s["tolerance"]:
+            break
+    orc.close()
+    return {"workload": f"ising2d_L{L}_{s['num_windows']}win_x{s['replicas_per_window']}walkers",
+            "schedule": "1/t (ONE_OVER_T_ALGORITHM), min >= 0.8 mean, walkers from all +1, exchange every 500 sweeps, "
+                        "check every 1000", "seconds_to": hit, "best_max_abs_dlng": best, "cycles": cycles,
+            "flips": flips, "seconds": round(t_sim, 2), "cap_seconds": s["cap_seconds"], "threads": threads,
+            "clock": "simulation only (stopped while the accuracy is evaluated)"}
 
 
 def run_reference(args):
@@ -337,59 +451,55 @@ def run_reference(args):
         "metric": METRIC, "value": rate, "unit": "flips/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / n, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": WORKLOAD["name"], **{k: v for k, v in WORKLOAD.items() if k != "name"},
-                   "step": step_text()},
+        "config": {"workload": w["name"], **{k: v for k, v in w.items() if k != "name"},
+                   "step": "a bounded sample: " + _sample_text(n, total)},
         "cpu_baseline": {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
-                         "sample": (f"{n} check intervals of one instance of each of the {len(w['components'])} components"
-                                    if w["model"] == "mixed" else
-                                    f"{n} check intervals of one instance of the workload "
-                                    f"({w['num_windows'] * w['replicas_per_window']} walkers, {w['sweeps_per_check']} sweeps each)")},
+                         "sample": _sample_text(n, total)},
         "e2e": {"value": rate, "unit": "flips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_tta and w["model"] == "ising2d":
+        line["time_to_accuracy"] = cpu_small_tta(threads)
     print(json.dumps(line), flush=True)
     return 0
 
 
 # --------------------------------------------------------------------------- GPU leg
-TTA_TOLERANCES = [1.0, 0.5, 0.3, 0.2, 0.15, 0.1, 0.08, 0.05, 0.03, 0.02, 0.01]
-TTA_SEEDS = (3, 5)
+TTA_SEED = 3
 
 
 def ising_batch(rg, L: int, nwin: int, R: int, lnf0: float, lnf_final: float, seed: int, device: int,
-                one_over_t: int = 0):
+                one_over_t: int = 1, sweeps_per_exchange: int = 500, sweeps_per_check: int = 1000):
     """Ising on the full spectrum; walkers start from all spins +1 and walk up into their windows,
     as the reference's do (a quench from random spins into the lowest windows can end in a
     stripe state that never reaches the window's lowest levels)."""
     N = L * L
     ins = rg.Instance(model=rg.MODEL_ISING2D, L=L, energy_min=-2.0 * N, energy_max=2.0 * N + 4, bin_width=4.0,
                       num_windows=nwin, replicas_per_window=R, window_overlap=0.75, seed=seed, init_mode=1)
-    return rg.Batch(instances=[ins], sweeps_per_exchange=500, sweeps_per_check=1000, flatness_param=0.8,
-                    lnf_initial=lnf0, lnf_final=lnf_final, one_over_t=one_over_t, device=device)
+    return rg.Batch(instances=[ins], sweeps_per_exchange=sweeps_per_exchange, sweeps_per_check=sweeps_per_check,
+                    flatness_param=0.8, lnf_initial=lnf0, lnf_final=lnf_final, one_over_t=one_over_t, device=device,
+                    graphs=1)
 
 
-def exact_lng(L: int):
-    z = np.load(ROOT / "tests" / "golden" / f"exact_ising_L{L}.npz")
-    return dict(zip(z["E"].astype(np.int64).tolist(), z["lng"]))
-
-
-def max_error(eng, exact) -> float:
-    E, g = eng.global_logdos(0)
-    return float(np.max(np.abs([g[i] - exact[int(round(E[i]))] for i in range(len(E))])))
-
-
-def track_accuracy(ws, eng, exact, t_start: float, max_seconds: float, burn_in: int = 0, stall_checks: int = 0):
-    """Run check intervals, recording the first wall time (from t_start) at or below each tolerance."""
-    hit, flips_at, best = {}, {}, [float("inf")]
+def track_accuracy(ws, eng, exact, max_seconds: float, burn_in: int = 0, stall_checks: int = 0, t_setup: float = 0.0,
+                   stop_at: float | None = None):
+    """Run check intervals, recording the simulation time (setup + the intervals, the clock stopped
+    while the accuracy is evaluated) at which the max error first falls to each tolerance."""
+    hit, flips_at, best, t_sim, last = {}, {}, [float("inf")], [t_setup], [None]
+    stop_at = TTA_TOLERANCES[-1] if stop_at is None else stop_at
+    t_mark = [time.perf_counter()]
 
     def on_cycle(e, st):
-        el = time.perf_counter() - t_start
-        err = max_error(e, exact)
+        t_sim[0] += time.perf_counter() - t_mark[0]
+        E, g = e.global_logdos(0)
+        err = _max_error(E, g, exact)
         best[0] = min(best[0], err)
+        last[0] = err
         for tol in TTA_TOLERANCES:
-            if err <= tol and tol not in hit:
-                hit[tol] = round(el, 2)
-                flips_at[tol] = st.attempted_flips
-        return el > max_seconds or TTA_TOLERANCES[-1] in hit
+            if err <= tol and str(tol) not in hit:
+                hit[str(tol)] = round(t_sim[0], 2)
+                flips_at[str(tol)] = st.attempted_flips
+        t_mark[0] = time.perf_counter()
+        return t_sim[0] > max_seconds or err <= stop_at
 
     stopped = None
     try:
@@ -397,78 +507,174 @@ def track_accuracy(ws, eng, exact, t_start: float, max_seconds: float, burn_in: 
         flips = st.attempted_flips
     except Exception as exc:                # e.g. a window that never went flat (REWL_ESTATE)
         stopped, fallbacks, flips = str(exc), None, None
-    out = {"seconds_to": {str(k): v for k, v in sorted(hit.items(), reverse=True)},
-           "flips_to": {str(k): v for k, v in sorted(flips_at.items(), reverse=True)}, "best_max_abs_dlng": best[0],
-           "flips": flips, "seconds": round(time.perf_counter() - t_start, 2), "fallbacks": fallbacks}
+    out = {"seconds_to": hit, "flips_to": flips_at, "best_max_abs_dlng": best[0], "last_max_abs_dlng": last[0],
+           "flips": flips, "seconds": round(t_sim[0], 2), "fallbacks": fallbacks}
     if stopped:
         out["stopped"] = stopped
     return out
 
 
-def warm_start_tta(rg, device: int, max_seconds: float, cpu_rate: float | None):
-    """Time to accuracy of 2D Ising L=64 (64 windows x 8 walkers): MLP warm start at ln f0 = 1e-4
-    against plain WL from ln f0 = 1, both timed from engine creation, for each seed in TTA_SEEDS.
-    The network is trained on the ln g that plain GPU runs at L = 16, 24, 32 converge to (that
-    time is reported separately)."""
+def gpu_small_tta(rg, device: int):
+    """SMALL_TTA on the GPU: the same system and criterion as the reference arm's CPU run."""
+    from rewl_simulator_gb300 import warmstart as ws
+    s = SMALL_TTA
+    t0 = time.perf_counter()
+    eng = rg.Engine(ising_batch(rg, s["L"], s["num_windows"], s["replicas_per_window"], 1.0, 1e-12, 5, device,
+                                sweeps_per_exchange=s["sweeps_per_exchange"], sweeps_per_check=s["sweeps_per_check"]))
+    out = track_accuracy(ws, eng, exact_lng(s["L"]), s["cap_seconds"], t_setup=time.perf_counter() - t0,
+                         stop_at=s["tolerance"])
+    eng.close()
+    out["workload"] = f"ising2d_L{s['L']}_{s['num_windows']}win_x{s['replicas_per_window']}walkers"
+    return out
+
+
+def warm_start_tta(rg, device: int, max_seconds: float, cpu_rate: float | None, data_seconds: float,
+                   train_steps: int, replicas: int = 8):
+    """Time to accuracy of 2D Ising L=64 (64 windows x `replicas` walkers): MLP warm start at
+    ln f0 = 1e-4 against plain WL from ln f0 = 1, both from engine creation, each capped at
+    max_seconds.  The network is trained on the ln g that plain GPU runs at L = 16, 24, 32 (one
+    batched engine, data_seconds of GPU time) reach; that time and the training time are
+    reported separately."""
     from rewl_simulator_gb300 import warmstart as ws
     from rewl_simulator_gb300.mlp import MLP
 
     t0 = time.perf_counter()
-    engines = [rg.Engine(ising_batch(rg, L, nw, R, 1.0, fin, 3, device))
-               for L, nw, R, fin in ((32, 16, 8, 1e-8), (24, 16, 4, 1e-8), (16, 4, 8, 1e-6))]
-    for e in engines:
-        e.simulate(max_cycles=4000)
-    base = ws.Baseline.from_engine(engines[0], 0)
-    rows = [ws.training_rows(e, 0, base=base) for e in engines]
-    for e in engines:
-        e.close()
+    sizes = ((32, 16, 8), (24, 16, 4), (16, 4, 8))
+    inss = [ising_batch(rg, L, nw, R, 1.0, 1e-12, TTA_SEED + k, device).instances[0]
+            for k, (L, nw, R) in enumerate(sizes)]
+    train_batch = rg.Batch(instances=inss, sweeps_per_exchange=500, sweeps_per_check=1000, flatness_param=0.8,
+                           lnf_initial=1.0, lnf_final=1e-12, one_over_t=1, device=device, graphs=1)
+    with rg.Engine(train_batch) as eng:
+        t_end = time.perf_counter() + data_seconds
+        while time.perf_counter() < t_end:
+            eng.run_cycles(1)
+        base = ws.Baseline.from_engine(eng, 0)
+        rows = [ws.training_rows(eng, i, base=base) for i in range(len(sizes))]
+        data_err = {}
+        for i, (L, _, _) in enumerate(sizes):
+            E, g = eng.global_logdos(i)
+            data_err[f"L{L}"] = _max_error(E, g, exact_lng(L))
     X = np.concatenate([r[0] for r in rows])
     y = np.concatenate([r[1] for r in rows])
     data_s = time.perf_counter() - t0
-    steps = 20000
     mlp = MLP(hidden=256, layers=4, seed=7, device=device)
     mlp.set_data(X, y)
     t0 = time.perf_counter()
-    losses = mlp.train(steps, batch=4096, lr=1e-3)
+    losses = mlp.train(train_steps, batch=4096, lr=1e-3)
     train_s = time.perf_counter() - t0
 
     exact = exact_lng(64)
-    arms, infer_s = {}, None
-    for seed in TTA_SEEDS:
-        t0 = time.perf_counter()
-        eng = rg.Engine(ising_batch(rg, 64, 64, 8, 1e-4, 1e-12, seed, device, one_over_t=1))
-        t1 = time.perf_counter()
-        ws.warm_start(eng, mlp, 0, lnf0=1e-4, base=base)
-        infer_s = time.perf_counter() - t1
-        warm = track_accuracy(ws, eng, exact, t0, max_seconds, burn_in=8, stall_checks=40)
-        warm["engine_create_seconds"] = round(t1 - t0, 2)
-        eng.close()
-        t0 = time.perf_counter()
-        eng = rg.Engine(ising_batch(rg, 64, 64, 8, 1.0, 1e-12, seed, device, one_over_t=1))
-        plain = track_accuracy(ws, eng, exact, t0, max_seconds)
-        eng.close()
-        speedup = {k: round(plain["seconds_to"][k] / v, 2) for k, v in warm["seconds_to"].items()
-                   if k in plain["seconds_to"]}
-        arms[f"seed{seed}"] = {"warm": warm, "plain": plain, "speedup_warm_over_plain": speedup}
+    t0 = time.perf_counter()
+    eng = rg.Engine(ising_batch(rg, 64, 64, replicas, 1e-4, 1e-12, TTA_SEED, device))
+    ws.warm_start(eng, mlp, 0, lnf0=1e-4, base=base)
+    setup = time.perf_counter() - t0
+    E, g = eng.global_logdos(0)
+    warm0 = _max_error(E, g, exact)
+    warm = track_accuracy(ws, eng, exact, max_seconds, burn_in=8, stall_checks=40, t_setup=setup)
+    warm["setup_seconds"] = round(setup, 3)
+    warm["max_abs_dlng_at_injection"] = warm0
+    eng.close()
     mlp.close()
-    out = {"workload": "ising2d_L64_64win_x8walkers", "criterion": "max |ln g - exact| over all levels, "
-           "windows concatenated and normalised to sum g = 2^N, checked every 1000 sweeps",
-           "schedule": "1/t (the reference's ONE_OVER_T_ALGORITHM default), walkers started from all +1",
-           "runs": arms,
+    t0 = time.perf_counter()
+    eng = rg.Engine(ising_batch(rg, 64, 64, replicas, 1.0, 1e-12, TTA_SEED, device))
+    plain = track_accuracy(ws, eng, exact, max_seconds, t_setup=time.perf_counter() - t0)
+    eng.close()
+    speedup = {k: round(plain["seconds_to"][k] / v, 2) for k, v in warm["seconds_to"].items()
+               if k in plain["seconds_to"] and v > 0}
+    out = {"workload": f"ising2d_L64_64win_x{replicas}walkers", "seed": TTA_SEED, "cap_seconds": max_seconds,
+           "criterion": "max |ln g - exact| over all levels, windows concatenated and normalised to sum g = 2^N, "
+                        "checked every 1000 sweeps",
+           "clock": "simulation only: engine creation, warm-start inference and upload, check intervals "
+                    "(stopped while the accuracy is evaluated)",
+           "schedule": "1/t (the reference's ONE_OVER_T_ALGORITHM default), min >= 0.8 mean, walkers from all +1",
+           "warm": warm, "plain": plain, "speedup_warm_over_plain": speedup,
            "mlp": {"training_rows": int(len(y)), "training_data_seconds": round(data_s, 1),
-                   "adam_steps": steps, "train_seconds": round(train_s, 2), "final_loss": float(np.mean(losses[-50:])),
+                   "training_data_max_abs_dlng": data_err, "adam_steps": train_steps,
+                   "train_seconds": round(train_s, 2), "final_loss": float(np.mean(losses[-50:])),
                    "target": "ln g/N minus the L=32 ln g/N interpolated in E/N",
-                   "inference_and_upload_seconds": round(infer_s, 3),
                    "warm_start": "ln f0 = 1e-4, histograms cleared after each of the first 8 check intervals, "
                                  "plain-WL fallback for windows without a flat event in 40 intervals"}}
     if cpu_rate:
         # not a run: what the CPU port would need for the same number of flips
         out["cpu_port_estimate"] = {
-            "basis": "flips the plain GPU arm needed to each tolerance / the CPU port's measured flips/s "
-                     "(estimate; the CPU run itself was not made)",
-            "seconds_to": {name: {k: round(v / cpu_rate, 1) for k, v in run["plain"]["flips_to"].items()}
-                           for name, run in arms.items()}}
+            "basis": "flips the plain GPU arm needed to each tolerance / the CPU port's measured flips/s on this "
+                     "workload (an estimate, not a CPU run; the reference arm times a CPU run at L = 16)",
+            "seconds_to": {k: round(v / cpu_rate, 1) for k, v in plain["flips_to"].items()}}
     return out
+
+
+def at_spread(rg, device: int, cycles: int, runs: int):
+    """Ashkin-Teller ln g on the GPU against the run-to-run spread of the reference's algorithm on
+    the host cores, at the benchmark's size: one realisation of L = 32, K = 0.5, Baxter fields
+    sigma 0.5, bins of 0.05, 8 windows x 4 walkers, halving ln f from 1, `cycles` check intervals
+    of 200 sweeps.  `runs` reference-semantics runs (the oracle port: mt19937_64 streams,
+    draw-on-demand, FP64 logDoS) with different seeds give the spread; `runs` GPU instances with
+    other seeds run in one engine.  Each run's windows are concatenated and normalised (half
+    spectrum, sum g = 4^N / 2) on the energies every run visited.  Reported: every run's RMS
+    distance from the mean of the reference runs (a reference run held out of that mean)."""
+    from oracle import pyoracle as po
+    w = dict(WORKLOADS["at"], realizations=1)
+    threads = os.cpu_count() or 1
+    fields = at_fields(w, 0)
+    N = w["L"] ** 2
+    cpu = []
+    t0 = time.perf_counter()
+    for k in range(runs):
+        orc = po.Oracle(_port_config(po, w, threads, seed=1 + k), fields=fields)
+        for _ in range(cycles):
+            orc.cycle()
+        wins = []
+        for j in range(w["num_windows"]):
+            lo, _, _, nb = orc.windows[j]
+            m = orc.window_mask(j)
+            wins.append(((lo + w["bin_width"] * np.arange(nb))[m], orc.window_logdos(j)[m]))
+        lnfs = [orc.lnf(j * w["replicas_per_window"]) for j in range(w["num_windows"])]
+        orc.close()
+        E, g = rg.concatenate_windows(wins, 4.0, N, half_spectrum=True)
+        cpu.append((dict(zip(np.round(E, 6), g)), lnfs))
+    cpu_s = time.perf_counter() - t0
+    inss = [rg.Instance(model=rg.MODEL_ASHKIN_TELLER2D, L=w["L"], K=w["K"], fields=fields, energy_min=w["energy_min"],
+                        energy_max=w["energy_max"], bin_width=w["bin_width"], num_windows=w["num_windows"],
+                        replicas_per_window=w["replicas_per_window"], window_overlap=w["window_overlap"],
+                        seed=101 + k) for k in range(runs)]
+    b = rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"], sweeps_per_check=w["sweeps_per_check"],
+                 flatness_param=0.8, lnf_initial=1.0, lnf_final=w["lnf_final"], mask_mode=rg.MASK_VISITED,
+                 device=device)
+    t0 = time.perf_counter()
+    gpu = []
+    with rg.Engine(b) as eng:
+        eng.run_cycles(cycles)
+        for k in range(runs):
+            E, g = eng.global_logdos(k, half_spectrum=True)
+            gpu.append((dict(zip(np.round(E, 6), g)), [eng.window_state(k, j)[0] for j in range(w["num_windows"])]))
+    gpu_s = time.perf_counter() - t0
+    common = sorted(set.intersection(*[set(d) for d, _ in cpu + gpu]))
+    C = np.array([[d[e] for e in common] for d, _ in cpu])
+    G = np.array([[d[e] for e in common] for d, _ in gpu])
+    mu = C.mean(0)
+    d_ref = [float(np.sqrt(np.mean((C[k] - np.delete(C, k, 0).mean(0)) ** 2))) for k in range(runs)]
+    d_gpu = [float(np.sqrt(np.mean((G[k] - mu) ** 2))) for k in range(runs)]
+    # a GPU run against the mean of runs-1 reference runs, like the held-out reference runs
+    d_gpu_loo = [float(np.sqrt(np.mean((G[k] - np.delete(C, k, 0).mean(0)) ** 2))) for k in range(runs)]
+    return {"workload": "ashkin_teller2d_L32_K0.5_h0.5_bw0.05_8win_x4walkers (one realisation)",
+            "check_intervals": cycles, "sweeps": cycles * w["sweeps_per_check"], "runs_per_side": runs,
+            "energies_compared": len(common),
+            "rms_from_reference_mean": {"reference_held_out": d_ref, "gpu": d_gpu, "gpu_vs_held_out_mean": d_gpu_loo},
+            "rms_gpu_mean_minus_reference_mean": float(np.sqrt(np.mean((G.mean(0) - mu) ** 2))),
+            "lnf_by_window": {"reference": [l for _, l in cpu], "gpu": [l for _, l in gpu]},
+            "seconds": {"reference_runs": round(cpu_s, 1), "gpu_engine": round(gpu_s, 1)}, "threads": threads}
+
+
+def time_steps(eng, stream, flush, steps):
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        flush.zero_()
+        evs[k][0].record(stream)
+        eng.run_cycles(1)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
 
 
 def run_gpu(args):
@@ -499,20 +705,14 @@ def run_gpu(args):
         st0 = eng.status()
         barrier()
         torch.cuda.synchronize()
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         sampler = ClockSampler(device)
         with sampler:
-            for k in range(args.steps):
-                flush.zero_()
-                evs[k][0].record(stream)
-                eng.run_cycles(1)
-                evs[k][1].record(stream)
-            torch.cuda.synchronize()
+            step_ms = time_steps(eng, stream, flush, args.steps)
         barrier()
-        step_ms = [a.elapsed_time(b) for a, b in evs]
         st1 = eng.status()
         kern_ms, kern_launches = eng.sweep_kernel_time()
-        groups = max(1, len(eng.launch_shapes()))
+        shapes = np.asarray(eng.launch_shapes()).tolist()
+        groups = max(1, len(shapes))
     total_ms = sum(step_ms)
     flips = st1.attempted_flips - st0.attempted_flips
     launches = st1.kernel_launches - st0.kernel_launches
@@ -545,11 +745,35 @@ def run_gpu(args):
             dist.destroy_process_group()
         return 0
 
-    peak, peak_kind = peaks()
+    hbm_peak, sm_max_mhz, peak_kind = peaks()
+    clocks = sampler.summary()
     # one sweep phase = one launch per launch group, concurrent; its span is what the events time
     avg_launch_ms = kern_ms / max(kern_launches / groups, 1)
     flips_per_launch = WORKLOAD["sweeps_per_exchange"] * flips_per_sweep(WORKLOAD)
-    achieved = bytes_per_flip(WORKLOAD) * flips_per_launch / (avg_launch_ms * 1e-3) / 1e9
+    achieved_gbs = bytes_per_flip(WORKLOAD) * flips_per_launch / (avg_launch_ms * 1e-3) / 1e9
+    prof = profile_figures()
+    sm_mhz = clocks.get("sm_mhz") or sm_max_mhz
+    roofline = {"bound": WORKLOAD["bound"], "kernel": WORKLOAD["kernel"], "avg_launch_ms": avg_launch_ms,
+                "flips_per_launch": flips_per_launch, "launch_shapes": shapes}
+    if WORKLOAD["model"] == "ising2d":
+        # the serial accept chain of one walker: cycles per attempted flip against the design's floor
+        walker_flips = WORKLOAD["sweeps_per_exchange"] * ndof(WORKLOAD)
+        cycles = avg_launch_ms * 1e-3 * sm_mhz * 1e6 / walker_flips
+        roofline.update({"unit": "cycles/flip", "achieved": cycles, "peak": CHAIN_FLOOR_CYCLES,
+                         "frac": CHAIN_FLOOR_CYCLES / cycles, "walkers_per_warp": int(shapes[0][2]) if shapes else 1,
+                         "peak_kind": "chain floor: dependent shared load (29) + 64-bit compare/select (11), "
+                                      "measured on a GB300",
+                         "note": "per walker: launch time x median SM clock / flips of one walker; frac = floor / "
+                                 "achieved"})
+    else:
+        roofline.update({"unit": "GB/s", "achieved": achieved_gbs, "peak": hbm_peak, "frac": achieved_gbs / hbm_peak,
+                         "peak_kind": peak_kind + " HBM copy bandwidth"})
+    roofline["hbm"] = {"algorithmic_gbs": achieved_gbs, "peak_gbs": hbm_peak, "frac": achieved_gbs / hbm_peak,
+                       "bytes_per_flip": bytes_per_flip(WORKLOAD),
+                       "traffic_bytes_per_launch": prof.get("traffic_bytes_per_launch")}
+    roofline["traffic"] = prof.get("traffic_bytes_per_launch")
+    if prof:
+        roofline["ncu"] = prof
     line = {
         "metric": METRIC, "value": value, "unit": "flips/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -557,25 +781,41 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD["name"], **{k: v for k, v in WORKLOAD.items() if k != "name"},
                    "step": step_text(),
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"instances x{world}"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": traffic_per_launch(),
-                     "kernel": WORKLOAD["kernel"], "bytes_per_flip": bytes_per_flip(WORKLOAD),
-                     "avg_launch_ms": avg_launch_ms, "flips_per_launch": flips_per_launch},
+        "roofline": roofline,
         "e2e": {"value": e2e_rate, "unit": "flips/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps},
-        "clocks": sampler.summary(),
+        "clocks": clocks,
         "gpu_launches": int(launches),
     }
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, n, total, _ = cpu_port_rate(args.cpu_seconds, threads)
-        sample = (f"{n} check intervals of one instance of each of the {len(WORKLOAD['components'])} components "
-                  f"({total:.1f} s)" if WORKLOAD["model"] == "mixed"
-                  else f"{n} check intervals of the same workload ({total:.1f} s)")
-        line["cpu_baseline"] = {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port", "sample": sample}
-    if args.tta and world == 1:
+        line["cpu_baseline"] = {"value": rate, "unit": "flips/s", "cores": threads, "kind": "port",
+                                "sample": _sample_text(n, total)}
+        if WORKLOAD["model"] != "mixed" and not args.observables:
+            # the reference's default build keeps per-bin observables and the G(q_min) correlators
+            obs_rate, on, ot, _ = cpu_port_rate(args.cpu_seconds / 2, threads, observables=2)
+            oeng = rg.Engine(make_batch(rg, seed=rank_seed(rank), device=device, observables=2))
+            ostream = torch.cuda.ExternalStream(oeng.stream_handle(), device=torch.device("cuda", device))
+            with torch.cuda.stream(ostream):
+                for _ in range(3):
+                    oeng.run_cycles(1)
+                ost0 = oeng.status()
+                oms = time_steps(oeng, ostream, flush, max(3, args.steps // 4))
+                ost1 = oeng.status()
+            oeng.close()
+            gpu_obs = (ost1.attempted_flips - ost0.attempted_flips) / (sum(oms) * 1e-3)
+            line["observables_on"] = {
+                "observables": "per-bin moments and G(q_min) correlators (the reference's default build)",
+                "value": gpu_obs, "unit": "flips/s", "steps": len(oms),
+                "cpu_baseline": {"value": obs_rate, "unit": "flips/s", "cores": threads, "kind": "port",
+                                 "sample": _sample_text(on, ot)},
+                "gpu_over_cpu": gpu_obs / obs_rate, "gpu_over_cpu_observables_off": value / rate}
+    if world == 1 and not args.no_tta and WORKLOAD["model"] == "ising2d" and WORKLOAD["L"] == 64:
         line["time_to_accuracy"] = warm_start_tta(rg, device, args.tta_seconds,
-                                                  line.get("cpu_baseline", {}).get("value"))
+                                                  line.get("cpu_baseline", {}).get("value"), args.tta_data_seconds,
+                                                  args.tta_train_steps, args.tta_replicas)
+        line["time_to_accuracy"]["small"] = gpu_small_tta(rg, device)
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -589,20 +829,32 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--tta", action="store_true",
-                    help="also measure time to accuracy at L=64: MLP warm start against plain WL")
-    ap.add_argument("--tta-seconds", type=float, default=90.0, help="wall-time limit of each time-to-accuracy arm")
+    ap.add_argument("--no-tta", action="store_true", help="skip the time-to-accuracy runs")
+    ap.add_argument("--tta-seconds", type=float, default=60.0, help="cap of each L=64 time-to-accuracy arm")
+    ap.add_argument("--tta-replicas", type=int, default=8, help="walkers per window of the L=64 time-to-accuracy arms")
+    ap.add_argument("--tta-data-seconds", type=float, default=30.0,
+                    help="GPU time of the plain L <= 32 runs that make the network's training data")
+    ap.add_argument("--tta-train-steps", type=int, default=20000, help="Adam steps of the warm-start network")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--observables", type=int, choices=[0, 1, 2], default=0,
                     help="1: keep the per-bin observables during the sweeps; 2: also the G(q_min) correlators "
                          "(the reference's default build)")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="ising",
-                    help="ising: the headline configuration (default); at: 2D Ashkin-Teller, 64 realisations; "
-                         "mixed: the uneven batch (Ising L = 16..48 and Ashkin-Teller L = 24, K = 0.25..0.75)")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c5",
+                    help="c5: Ising L=64, 64 windows x 8 walkers (default, the headline configuration); c2: Ising "
+                         "L=32, 16 x 8; at: Ashkin-Teller L=32, 64 realisations; mixed: the uneven batch")
+    ap.add_argument("--at-spread", type=int, default=0, metavar="CYCLES",
+                    help="only measure Ashkin-Teller L=32 ln g on the GPU against the spread of reference runs on "
+                         "the host cores after CYCLES check intervals")
+    ap.add_argument("--at-spread-runs", type=int, default=4)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.at_spread:
+        import rewl_simulator_gb300 as rg
+        rg.build()
+        print(json.dumps({"at_spread": at_spread(rg, 0, args.at_spread, args.at_spread_runs)}), flush=True)
+        return 0
     select_workload(args.workload)
     if args.observables:
         WORKLOADS[args.workload]["observables"] = args.observables

@@ -10,7 +10,7 @@ from ._native import build as _build_native, load as load_library, LIB as LIBRAR
 from .engine import (Batch, Engine, Instance, REWLError, Status, DISORDER_GAUSSIAN, DISORDER_UNIFORM,
                      FLAT_ALL_VISITED, FLAT_MAX_MIN_RATIO, FLAT_MIN_OVER_MEAN, MASK_STATIC, MASK_VISITED,
                      MODEL_ASHKIN_TELLER2D, MODEL_ISING2D, RNG_PHILOX, RNG_REPLAY, MATCH_DERIVATIVE, MATCH_REFERENCE,
-                     concatenate_windows, generate_fields)
+                     concatenate_windows, generate_fields, instance_key)
 
 
 def build(force: bool = False, verbose: bool = False):
@@ -21,4 +21,4 @@ def build(force: bool = False, verbose: bool = False):
 __all__ = ["Batch", "Engine", "Instance", "REWLError", "Status", "build", "load_library", "LIBRARY_PATH",
            "MODEL_ISING2D", "MODEL_ASHKIN_TELLER2D", "FLAT_MIN_OVER_MEAN", "FLAT_MAX_MIN_RATIO", "FLAT_ALL_VISITED",
            "MASK_STATIC", "MASK_VISITED", "RNG_PHILOX", "RNG_REPLAY", "DISORDER_GAUSSIAN", "DISORDER_UNIFORM",
-           "generate_fields", "concatenate_windows", "MATCH_DERIVATIVE", "MATCH_REFERENCE"]
+           "generate_fields", "concatenate_windows", "instance_key", "MATCH_DERIVATIVE", "MATCH_REFERENCE"]

@@ -136,6 +136,16 @@ def _p(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
 
 
+def instance_key(seed: int) -> int:
+    """The Philox key the engine derives from an instance's seed: SplitMix64's output function
+    (Steele, Lea, Flood, OOPSLA 2014).  Walker u of the instance is keyed (key_lo ^ u, key_hi)."""
+    m = (1 << 64) - 1
+    z = (int(seed) + 0x9E3779B97F4A7C15) & m
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    return z ^ (z >> 31)
+
+
 def generate_fields(seed: int, strength: float, num_sites: int, distribution: int = DISORDER_GAUSSIAN) -> np.ndarray:
     """Random fields drawn as the reference's Disorder::generate_random_field draws them
     (src/Hamiltonians/Disorder/random_fields.hpp:41-75), from `seed` instead of the clock:

@@ -268,7 +268,7 @@ def gen_normalize():
 
 
 def gen_exact():
-    for L in (4, 6, 8, 16, 32, 64):
+    for L in (4, 6, 8, 16, 24, 32, 64):
         E, lng = beale.exact_lng(L)
         extra = {}
         if L <= 8:

@@ -22,15 +22,15 @@ def _run(args, env_extra=None):
     return [l for l in r.stdout.splitlines() if l.startswith("{")]
 
 
-@pytest.mark.parametrize("workload", ["ising", "at"])
+@pytest.mark.parametrize("workload", ["c5", "at"])
 def test_reference_arm_prints_the_contract_line(workload):
-    lines = _run(["--impl", "reference", "--steps", "1", "--warmup", "3", "--workload", workload])
+    lines = _run(["--impl", "reference", "--steps", "1", "--warmup", "3", "--workload", workload, "--no-tta"])
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert KEYS <= set(d)
     assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "flips/s" and d["higher_is_better"] is True
     assert d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1 and d["vs_baseline"] is None
-    assert d["config"]["workload"].startswith({"ising": "ising2d_L32", "at": "ashkin_teller2d_L32"}[workload])
+    assert d["config"]["workload"].startswith({"c5": "ising2d_L64_64win_x8", "at": "ashkin_teller2d_L32"}[workload])
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "flips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
@@ -38,6 +38,18 @@ def test_reference_arm_prints_the_contract_line(workload):
 
 def test_reference_arm_other_ranks_print_nothing():
     assert _run(["--impl", "reference", "--steps", "1", "--warmup", "3"], {"RANK": "1", "WORLD_SIZE": "2"}) == []
+
+
+def test_default_workload_is_the_headline_configuration():
+    """The default line is quoted on Ising L = 64, 64 windows x 8 walkers (the configuration the
+    metric names), with the 1/t schedule and walkers started from all +1 as the reference's."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    w = bench.WORKLOADS["c5"]
+    assert bench.WORKLOAD is w
+    assert (w["L"], w["num_windows"], w["replicas_per_window"]) == (64, 64, 8)
+    assert (w["sweeps_per_exchange"], w["sweeps_per_check"], w["one_over_t"], w["init_mode"]) == (500, 1000, 1, 1)
+    assert bench.flips_per_sweep(w) * w["sweeps_per_check"] == 2_097_152_000
 
 
 def test_warmup_below_three_is_refused():
@@ -48,8 +60,8 @@ def test_warmup_below_three_is_refused():
 
 @pytest.mark.parametrize("workload", ["at", "mixed"])
 def test_bench_batches_give_every_walker_its_own_key(workload):
-    """Walker keys are (seed_lo XOR walker, seed_hi): the bench's instance seeds keep them distinct
-    across all walkers of a batch."""
+    """Walker keys are (key_lo XOR walker, key_hi) with key the instance seed's SplitMix64 mix: the
+    bench's consecutive instance seeds give every walker of a batch its own key."""
     sys.path.insert(0, str(ROOT))
     import bench
     import rewl_simulator_gb300 as rg
@@ -61,6 +73,7 @@ def test_bench_batches_give_every_walker_its_own_key(workload):
         bench.WORKLOAD = old
     keys = set()
     for ins in batch.instances:
+        k = rg.instance_key(ins.seed)
         for u in range(ins.num_windows * ins.replicas_per_window):
-            keys.add(((ins.seed & 0xFFFFFFFF) ^ u, ins.seed >> 32))
+            keys.add(((k & 0xFFFFFFFF) ^ u, k >> 32))
     assert len(keys) == sum(i.num_windows * i.replicas_per_window for i in batch.instances)

@@ -28,7 +28,7 @@ def test_beale_identities(L):
     assert all(v > 0 for v in g[2:-2])
 
 
-@pytest.mark.parametrize("L", [4, 6, 8, 16, 32, 64])
+@pytest.mark.parametrize("L", [4, 6, 8, 16, 24, 32, 64])
 def test_exact_fixture_consistent(L):
     z = np.load(GOLDEN / f"exact_ising_L{L}.npz")
     E, lng = z["E"], z["lng"]
@@ -38,7 +38,7 @@ def test_exact_fixture_consistent(L):
     assert abs(m + np.log(np.exp(lng - m).sum()) - N * np.log(2.0)) < 1e-9 * N
     np.testing.assert_allclose(lng, lng[::-1], rtol=0, atol=1e-9)
     assert abs(lng[0] - np.log(2.0)) < 1e-12
-    if L <= 16:
+    if L <= 24:
         E2, lng2 = beale.exact_lng(L)
         np.testing.assert_array_equal(E, E2)
         np.testing.assert_allclose(lng, lng2, rtol=0, atol=1e-12)
