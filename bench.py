@@ -609,32 +609,28 @@ def at_spread(rg, device: int, cycles: int, runs: int):
     sigma 0.5, bins of 0.05, 8 windows x 4 walkers, halving ln f from 1, `cycles` check intervals
     of 200 sweeps.  `runs` reference-semantics runs (the oracle port: mt19937_64 streams,
     draw-on-demand, FP64 logDoS) with different seeds give the spread; `runs` GPU instances with
-    other seeds run in one engine.  Each run's windows are concatenated and normalised (half
-    spectrum, sum g = 4^N / 2) on the energies every run visited.  Reported: every run's RMS
-    distance from the mean of the reference runs (a reference run held out of that mean)."""
+    other seeds run in one engine.  Windows are compared one by one, each run's window ln g
+    (replicas averaged by their visits) on the bins every run visited, shifted to zero mean there
+    (early in a run the visited parts of neighbouring windows need not overlap yet, so the windows
+    are not concatenated).  Reported: every run's RMS distance from the mean of the reference
+    runs, over all compared bins (a reference run held out of that mean)."""
     from oracle import pyoracle as po
     w = dict(WORKLOADS["at"], realizations=1)
     threads = os.cpu_count() or 1
     fields = at_fields(w, 0)
-    N = w["L"] ** 2
+    nw = w["num_windows"]
     cpu = []
     t0 = time.perf_counter()
     for k in range(runs):
         orc = po.Oracle(_port_config(po, w, threads, seed=1 + k), fields=fields)
         for _ in range(cycles):
             orc.cycle()
-        wins = []
-        for j in range(w["num_windows"]):
-            lo, _, _, nb = orc.windows[j]
-            m = orc.window_mask(j)
-            wins.append(((lo + w["bin_width"] * np.arange(nb))[m], orc.window_logdos(j)[m]))
-        lnfs = [orc.lnf(j * w["replicas_per_window"]) for j in range(w["num_windows"])]
+        cpu.append(([(orc.window_logdos(j), orc.window_mask(j)) for j in range(nw)],
+                    [orc.lnf(j * w["replicas_per_window"]) for j in range(nw)]))
         orc.close()
-        E, g = rg.concatenate_windows(wins, 4.0, N, half_spectrum=True)
-        cpu.append((dict(zip(np.round(E, 6), g)), lnfs))
     cpu_s = time.perf_counter() - t0
     inss = [rg.Instance(model=rg.MODEL_ASHKIN_TELLER2D, L=w["L"], K=w["K"], fields=fields, energy_min=w["energy_min"],
-                        energy_max=w["energy_max"], bin_width=w["bin_width"], num_windows=w["num_windows"],
+                        energy_max=w["energy_max"], bin_width=w["bin_width"], num_windows=nw,
                         replicas_per_window=w["replicas_per_window"], window_overlap=w["window_overlap"],
                         seed=101 + k) for k in range(runs)]
     b = rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"], sweeps_per_check=w["sweeps_per_check"],
@@ -645,12 +641,23 @@ def at_spread(rg, device: int, cycles: int, runs: int):
     with rg.Engine(b) as eng:
         eng.run_cycles(cycles)
         for k in range(runs):
-            E, g = eng.global_logdos(k, half_spectrum=True)
-            gpu.append((dict(zip(np.round(E, 6), g)), [eng.window_state(k, j)[0] for j in range(w["num_windows"])]))
+            gpu.append(([(eng.window_logdos(k, j), eng.window_mask(k, j).astype(bool)) for j in range(nw)],
+                        [eng.window_state(k, j)[0] for j in range(nw)]))
     gpu_s = time.perf_counter() - t0
-    common = sorted(set.intersection(*[set(d) for d, _ in cpu + gpu]))
-    C = np.array([[d[e] for e in common] for d, _ in cpu])
-    G = np.array([[d[e] for e in common] for d, _ in gpu])
+    C_parts, G_parts, per_window = [], [], []
+    for j in range(nw):
+        common = np.logical_and.reduce([t[j][1] for t, _ in cpu + gpu])
+        if common.sum() < 2:
+            continue
+        Cw = np.array([t[j][0][common] - t[j][0][common].mean() for t, _ in cpu])
+        Gw = np.array([t[j][0][common] - t[j][0][common].mean() for t, _ in gpu])
+        C_parts.append(Cw)
+        G_parts.append(Gw)
+        per_window.append({"window": j, "bins": int(common.sum()),
+                           "reference_rms_spread": float(np.sqrt(np.mean(Cw.var(0, ddof=1)))),
+                           "gpu_mean_minus_reference_mean_rms": float(np.sqrt(np.mean((Gw.mean(0) - Cw.mean(0)) ** 2)))})
+    C = np.concatenate(C_parts, axis=1)
+    G = np.concatenate(G_parts, axis=1)
     mu = C.mean(0)
     d_ref = [float(np.sqrt(np.mean((C[k] - np.delete(C, k, 0).mean(0)) ** 2))) for k in range(runs)]
     d_gpu = [float(np.sqrt(np.mean((G[k] - mu) ** 2))) for k in range(runs)]
@@ -658,7 +665,7 @@ def at_spread(rg, device: int, cycles: int, runs: int):
     d_gpu_loo = [float(np.sqrt(np.mean((G[k] - np.delete(C, k, 0).mean(0)) ** 2))) for k in range(runs)]
     return {"workload": "ashkin_teller2d_L32_K0.5_h0.5_bw0.05_8win_x4walkers (one realisation)",
             "check_intervals": cycles, "sweeps": cycles * w["sweeps_per_check"], "runs_per_side": runs,
-            "energies_compared": len(common),
+            "bins_compared": int(C.shape[1]), "per_window": per_window,
             "rms_from_reference_mean": {"reference_held_out": d_ref, "gpu": d_gpu, "gpu_vs_held_out_mean": d_gpu_loo},
             "rms_gpu_mean_minus_reference_mean": float(np.sqrt(np.mean((G.mean(0) - mu) ** 2))),
             "lnf_by_window": {"reference": [l for _, l in cpu], "gpu": [l for _, l in gpu]},
@@ -843,6 +850,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c5",
                     help="c5: Ising L=64, 64 windows x 8 walkers (default, the headline configuration); c2: Ising "
                          "L=32, 16 x 8; at: Ashkin-Teller L=32, 64 realisations; mixed: the uneven batch")
+    ap.add_argument("--replicas", type=int, default=0,
+                    help="walkers per window (default: the workload's; Ising workloads only)")
     ap.add_argument("--at-spread", type=int, default=0, metavar="CYCLES",
                     help="only measure Ashkin-Teller L=32 ln g on the GPU against the spread of reference runs on "
                          "the host cores after CYCLES check intervals")
@@ -859,6 +868,12 @@ def main():
     if args.observables:
         WORKLOADS[args.workload]["observables"] = args.observables
         select_workload(args.workload)
+    if args.replicas:
+        if WORKLOAD["model"] != "ising2d":
+            ap.error("--replicas applies to the Ising workloads")
+        w = WORKLOADS[args.workload]
+        w["replicas_per_window"] = args.replicas
+        w["name"] = w["name"].replace("x8walkers", f"x{args.replicas}walkers")
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
