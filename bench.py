@@ -672,6 +672,147 @@ def at_spread(rg, device: int, cycles: int, runs: int):
             "seconds": {"reference_runs": round(cpu_s, 1), "gpu_engine": round(gpu_s, 1)}, "threads": threads}
 
 
+AT_WARM_TOLERANCES = [100.0, 50.0, 20.0, 10.0, 5.0, 2.0, 1.0, 0.5]
+
+
+def warm_start_at(rg, device: int, cap: float, ref_seconds: float, data_seconds: float, train_steps: int,
+                  realizations: int = 32):
+    """The Ashkin-Teller arm of the warm-start measurement: L = 48, K = 0.5, Baxter fields sigma 0.5,
+    `realizations` realisations x 8 windows x 4 walkers in one engine, bins of width 1 over the half
+    spectrum [-(2J + K) 2N, 0), halving ln f (the Ashkin-Teller benchmark's schedule), walkers from
+    random spins.  There is no exact density of states: each realisation is judged against a long
+    plain-WL run of its own (ref_seconds, other seeds).  Accuracy of a snapshot: per realisation the
+    largest |ln g - ln g_judge| over the energies both visited (both normalised to sum g = 4^N / 2),
+    then the median over the realisations (the largest is reported too).  The network is trained on
+    plain runs at L = 8, 12, 16 (4 realisations each, data_seconds of GPU time); the warm arm starts
+    at ln f0 = 1e-4 with 8 burn-in intervals and the 40-interval stall fallback; both arms from ln f0
+    as stated, each capped at `cap` seconds of simulation (clock stopped while accuracy is measured)."""
+    from rewl_simulator_gb300 import warmstart as ws
+    from rewl_simulator_gb300.mlp import MLP
+    K, sh, bw = 0.5, 0.5, 1.0
+
+    def fields(L, k):
+        return np.round(np.random.default_rng(7000 + 100 * L + k).normal(0.0, sh, L * L) * 2**20) / 2**20
+
+    def batch(L, nreal, R, lnf0, seed0, fk=None):
+        N = L * L
+        inss = [rg.Instance(model=rg.MODEL_ASHKIN_TELLER2D, L=L, K=K, fields=fields(L, k if fk is None else fk(k)),
+                            energy_min=-(2.0 + K) * 2 * N, energy_max=0.0, bin_width=bw, num_windows=8 if L >= 32 else 4,
+                            replicas_per_window=R, window_overlap=0.75, seed=seed0 + k) for k in range(nreal)]
+        return rg.Batch(instances=inss, sweeps_per_exchange=100, sweeps_per_check=200, flatness_param=0.8,
+                        lnf_initial=lnf0, lnf_final=1e-7, mask_mode=rg.MASK_VISITED, device=device, graphs=1)
+
+    def tables(eng, n):
+        out = []
+        for i in range(n):
+            try:
+                E, g = eng.global_logdos(i, half_spectrum=True)
+                out.append(dict(zip(np.round(E, 6), g)))
+            except rg.REWLError:              # visited parts of neighbouring windows do not overlap yet
+                out.append(None)
+        return out
+
+    def accuracy(tabs, judge):
+        errs = []
+        for t, j in zip(tabs, judge):
+            if t is None:
+                errs.append(float("inf"))
+                continue
+            common = [e for e in t if e in j]
+            errs.append(float(np.max(np.abs([t[e] - j[e] for e in common]))) if common else float("inf"))
+        return float(np.median(errs)), float(np.max(errs))
+
+    n = realizations
+    # the judge: long plain runs of the same realisations
+    t0 = time.perf_counter()
+    with rg.Engine(batch(48, n, 4, 1.0, 90000)) as eng:
+        t_end = time.perf_counter() + ref_seconds
+        while time.perf_counter() < t_end:
+            eng.run_cycles(10)
+        judge = tables(eng, n)
+        judge_lnf = [min(eng.window_state(i, w)[0] for w in range(8)) for i in range(n)]
+    ref_s = time.perf_counter() - t0
+    # training data
+    t0 = time.perf_counter()
+    sizes = (16, 12, 8)
+    inss = []
+    for L in sizes:
+        inss += batch(L, 4, 4, 1.0, 500 + L).instances
+    tb = rg.Batch(instances=inss, sweeps_per_exchange=100, sweeps_per_check=200, flatness_param=0.8, lnf_initial=1.0,
+                  lnf_final=1e-7, mask_mode=rg.MASK_VISITED, device=device, graphs=1)
+    with rg.Engine(tb) as eng:
+        t_end = time.perf_counter() + data_seconds
+        while time.perf_counter() < t_end:
+            eng.run_cycles(5)
+        base = ws.Baseline.from_engine(eng, 0)
+        rows = [ws.training_rows(eng, i, sigma_h=sh, base=base) for i in range(len(inss))]
+    X = np.concatenate([r[0] for r in rows])
+    y = np.concatenate([r[1] for r in rows])
+    data_s = time.perf_counter() - t0
+    mlp = MLP(hidden=256, layers=4, seed=9, device=device)
+    mlp.set_data(X, y)
+    t0 = time.perf_counter()
+    losses = mlp.train(train_steps, batch=4096, lr=1e-3)
+    train_s = time.perf_counter() - t0
+
+    def arm(warm: bool):
+        t0 = time.perf_counter()
+        eng = rg.Engine(batch(48, n, 4, 1e-4 if warm else 1.0, 1000))
+        if warm:
+            for i in range(n):
+                ws.warm_start(eng, mlp, i, sigma_h=sh, lnf0=1e-4, base=base)
+        hit, t_sim, t_mark, best = {}, [time.perf_counter() - t0], [time.perf_counter()], [float("inf"), None]
+        first = accuracy(tables(eng, n), judge)
+
+        def on_cycle(e, st):
+            t_sim[0] += time.perf_counter() - t_mark[0]
+            med, mx = accuracy(tables(e, n), judge)
+            if med < best[0]:
+                best[0], best[1] = med, mx
+            for tol in AT_WARM_TOLERANCES:
+                if med <= tol and str(tol) not in hit:
+                    hit[str(tol)] = round(t_sim[0], 2)
+            t_mark[0] = time.perf_counter()
+            return t_sim[0] > cap
+
+        def on_cycle_every(k):
+            count = [0]
+
+            def f(e, st):
+                count[0] += 1
+                if count[0] % k:
+                    return False
+                return on_cycle(e, st)
+            return f
+
+        try:
+            st, fb = ws.run(eng, 1 << 30, stall_checks=40 if warm else 0, burn_in=8 if warm else 0,
+                            on_cycle=on_cycle_every(5))
+            stopped = None
+        except Exception as exc:
+            st, fb, stopped = None, None, str(exc)
+        eng.close()
+        out = {"seconds_to": hit, "best_median": best[0], "max_at_best": best[1], "at_start": {"median": first[0],
+               "max": first[1]}, "seconds": round(t_sim[0], 2), "fallbacks": fb}
+        if stopped:
+            out["stopped"] = stopped
+        return out
+
+    warm = arm(True)
+    mlp.close()
+    plain = arm(False)
+    speedup = {k: round(plain["seconds_to"][k] / v, 2) for k, v in warm["seconds_to"].items()
+               if k in plain["seconds_to"] and v > 0}
+    return {"workload": f"ashkin_teller2d_L48_K0.5_h0.5_bw1_{n}real_8win_x4walkers", "cap_seconds": cap,
+            "criterion": "median over realisations of max |ln g - judge| over energies both visited (normalised, "
+                         "half spectrum); judge = a long plain run of each realisation",
+            "judge": {"seconds": round(ref_s, 1), "smallest_lnf_by_realisation": judge_lnf},
+            "warm": warm, "plain": plain, "speedup_warm_over_plain": speedup,
+            "mlp": {"training_rows": int(len(y)), "training_data_seconds": round(data_s, 1), "adam_steps": train_steps,
+                    "train_seconds": round(train_s, 2), "final_loss": float(np.mean(losses[-50:])),
+                    "training_sizes": list(sizes), "target": "ln g/N minus the first L=16 realisation's ln g/N"}}
+
+
 def time_steps(eng, stream, flush, steps):
     import torch
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -856,9 +997,17 @@ def main():
                     help="only measure Ashkin-Teller L=32 ln g on the GPU against the spread of reference runs on "
                          "the host cores after CYCLES check intervals")
     ap.add_argument("--at-spread-runs", type=int, default=4)
+    ap.add_argument("--at-warm", type=float, default=0.0, metavar="CAP",
+                    help="only measure the Ashkin-Teller L=48 warm-start arm (each arm capped at CAP seconds)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.at_warm:
+        import rewl_simulator_gb300 as rg
+        rg.build()
+        print(json.dumps({"at_warm_start": warm_start_at(rg, 0, args.at_warm, 2.0 * args.at_warm, 40.0,
+                                                         args.tta_train_steps)}), flush=True)
+        return 0
     if args.at_spread:
         import rewl_simulator_gb300 as rg
         rg.build()

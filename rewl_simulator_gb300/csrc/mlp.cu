@@ -544,11 +544,23 @@ __global__ void __launch_bounds__(256) k_loss_sum(const float* rows, int B, floa
 }
 
 // Adam on fp32 masters; refresh the bf16 copy.  mask zeroes the padded entries.
+// Device state of a training call: the network's step counter and the index of the step within
+// the call.  The kernels of a step read it, so that one captured step replays as the next.
+struct TrainCursor {
+    unsigned long long step;
+    int k;
+    int pad;
+};
+
+// Adam with the bias corrections of the cursor's step (c1 = 1 - b1^t, c2 = 1 - b2^t, computed on
+// the host for every step of the call, two floats per step).
 __global__ void k_adam(float* p, float* m, float* v, const float* grad, const float* mask, bf16* pb, size_t n,
-                       float lr, float b1, float b2, float eps, float c1, float c2)
+                       float lr, float b1, float b2, float eps, const float* ctab, const TrainCursor* cur)
 {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const int k = cur->k;
+    const float c1 = ctab[2 * k], c2 = ctab[2 * k + 1];
     const float gi = grad[i] * mask[i];
     const float mi = b1 * m[i] + (1.f - b1) * gi;
     const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
@@ -559,15 +571,25 @@ __global__ void k_adam(float* p, float* m, float* v, const float* grad, const fl
 }
 
 // batch gather with Philox indices: Xb = X[idx], yb = y[idx]
-__global__ void k_gather(const bf16* X, const float* y, int n, bf16* Xb, float* yb, int B, uint64_t seed, uint64_t step)
+__global__ void k_gather(const bf16* X, const float* y, int n, bf16* Xb, float* yb, int B, uint64_t seed,
+                         const TrainCursor* cur)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
+    const uint64_t step = cur->step;
     const uint32_t w = rewl::philox_word(seed, 0x4D4C5000u, step * (uint64_t)B + (uint64_t)b, 0x4D4C5001u);
     const int i = (int)rewl::mulhi32(w, (uint32_t)n);
     for (int c = 0; c < kIn; c += 8)
         *reinterpret_cast<uint4*>(Xb + (size_t)b * kIn + c) = *reinterpret_cast<const uint4*>(X + (size_t)i * kIn + c);
     yb[b] = y[i];
+}
+
+// End of a training step: keep its loss, advance the cursor.
+__global__ void k_train_advance(TrainCursor* cur, const float* loss, float* losses)
+{
+    losses[cur->k] = *loss;
+    cur->step += 1;
+    cur->k += 1;
 }
 
 template <typename T>
@@ -608,6 +630,8 @@ struct rewl_mlp {
     Buf<bf16> dOut, dH, G;
     Buf<bf16> Xall;
     Buf<float> yall;
+    Buf<TrainCursor> cursor;          // training: step counter on the device
+    Buf<float> ctab, lossv;           // training: bias corrections and losses of the call's steps
     int nall = 0;
     int64_t step = 0;
     uint64_t seed = 1;
@@ -621,6 +645,7 @@ struct rewl_mlp {
         out.release(); yb.release(); loss.release(); lossrow.release(); dOut.release(); dH.release(); G.release();
         Part.release();
         Xall.release(); yall.release();
+        cursor.release(); ctab.release(); lossv.release();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -925,27 +950,66 @@ int rewl_mlp_train(rewl_mlp* m, int32_t steps, int32_t batch, float lr, float* l
 {
     if (!m || steps < 0 || batch < 64 || batch % kBM || !(lr > 0)) return mfail(REWL_EINVAL, "bad arguments");
     if (m->nall < 1) return mfail(REWL_ESTATE, "no training data (rewl_mlp_set_data)");
+    if (steps == 0) return REWL_OK;
     cudaSetDevice(m->device);
     int rc = ensure_batch(m, batch);
     if (rc) return rc;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    std::vector<float> lh(steps);
-    for (int s = 0; s < steps; ++s) {
-        k_gather<<<(batch + 127) / 128, 128, 0, m->stream>>>(m->Xall.p, m->yall.p, m->nall, m->H[0].p, m->yb.p, batch,
-                                                             m->seed, (uint64_t)m->step);
-        m->launches++;
-        if ((rc = forward(m, batch)) || (rc = backward(m, batch))) return rc;
-        m->step++;
-        const float c1 = 1.f - std::pow(b1, (float)m->step), c2 = 1.f - std::pow(b2, (float)m->step);
-        k_adam<<<(unsigned)((m->nparams + 255) / 256), 256, 0, m->stream>>>(m->P.p, m->Mm.p, m->Vm.p, m->Gr.p, m->Mask.p,
-                                                                            m->Pb.p, m->nparams, lr, b1, b2, eps, c1, c2);
-        m->launches++;
-        MCUDA(cudaGetLastError());
-        if (losses) MCUDA(cudaMemcpyAsync(&lh[s], m->loss.p, 4, cudaMemcpyDeviceToHost, m->stream));
+    // the call's bias corrections and its losses live on the device; the cursor starts at the
+    // network's step
+    if (m->ctab.n < (size_t)2 * steps) {
+        m->ctab.release(); m->lossv.release();
+        if ((rc = m->ctab.alloc((size_t)2 * steps)) || (rc = m->lossv.alloc((size_t)steps))) return rc;
     }
-    MCUDA(cudaStreamSynchronize(m->stream));
+    if (!m->cursor.p && (rc = m->cursor.alloc(1))) return rc;
+    std::vector<float> ct((size_t)2 * steps);
+    for (int s = 0; s < steps; ++s) {
+        const float t = (float)(m->step + s + 1);
+        ct[2 * s] = 1.f - std::pow(b1, t);
+        ct[2 * s + 1] = 1.f - std::pow(b2, t);
+    }
+    const TrainCursor c0{(unsigned long long)m->step, 0, 0};
+    MCUDA(cudaMemcpyAsync(m->ctab.p, ct.data(), ct.size() * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+    MCUDA(cudaMemcpyAsync(m->cursor.p, &c0, sizeof c0, cudaMemcpyHostToDevice, m->stream));
+    MCUDA(cudaStreamSynchronize(m->stream));       // the host copies above leave scope
+
+    // one step: sample the batch, forward, backward, Adam, keep the loss and advance; captured as
+    // a CUDA graph and replayed `steps` times (about 30 launches a step, launch-bound otherwise)
+    const int64_t l0 = m->launches;
+    auto enqueue_step = [&]() -> int {
+        k_gather<<<(batch + 127) / 128, 128, 0, m->stream>>>(m->Xall.p, m->yall.p, m->nall, m->H[0].p, m->yb.p, batch,
+                                                             m->seed, m->cursor.p);
+        m->launches++;
+        int r;
+        if ((r = forward(m, batch)) || (r = backward(m, batch))) return r;
+        k_adam<<<(unsigned)((m->nparams + 255) / 256), 256, 0, m->stream>>>(m->P.p, m->Mm.p, m->Vm.p, m->Gr.p, m->Mask.p,
+                                                                            m->Pb.p, m->nparams, lr, b1, b2, eps,
+                                                                            m->ctab.p, m->cursor.p);
+        k_train_advance<<<1, 1, 0, m->stream>>>(m->cursor.p, m->loss.p, m->lossv.p);
+        m->launches += 2;
+        MCUDA(cudaGetLastError());
+        return REWL_OK;
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    MCUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeRelaxed));
+    rc = enqueue_step();
+    const cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
+    if (rc == REWL_OK && ce != cudaSuccess) rc = mfail(REWL_EDEVICE, "capturing a training step: %s", cudaGetErrorString(ce));
+    if (rc == REWL_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+        rc = mfail(REWL_EDEVICE, "instantiating the training-step graph failed");
+    if (graph) cudaGraphDestroy(graph);
+    const int64_t per_step = m->launches - l0;
+    for (int s = 0; s < steps && rc == REWL_OK; ++s)
+        if (cudaGraphLaunch(exec, m->stream) != cudaSuccess) rc = mfail(REWL_EDEVICE, "training-step graph launch failed");
+    const cudaError_t se = cudaStreamSynchronize(m->stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (rc) return rc;
+    if (se != cudaSuccess) return mfail(REWL_EDEVICE, "training: %s", cudaGetErrorString(se));
+    m->launches += per_step * (steps - 1);     // the capture counted one step
+    m->step += steps;
     if ((rc = take_tc_error())) return rc;
-    if (losses) std::memcpy(losses, lh.data(), lh.size() * 4);
+    if (losses) MCUDA(cudaMemcpy(losses, m->lossv.p, (size_t)steps * sizeof(float), cudaMemcpyDeviceToHost));
     return REWL_OK;
 }
 

@@ -152,3 +152,26 @@ def test_gpu_training_is_reproducible(engine_lib):
             m.close()
         assert np.array_equal(runs[0][0], runs[1][0]), batch
         assert np.array_equal(runs[0][1], runs[1][1]), batch
+
+
+@pytest.mark.gpu
+def test_gpu_training_resumes_across_calls(engine_lib):
+    """A training call replays one captured step as a CUDA graph, with the step counter (batch
+    sampling, Adam's bias corrections) kept on the device: 20 steps in one call and 7 + 13 in two
+    calls give bit-identical parameters and losses, and the launch counter counts every step."""
+    from rewl_simulator_gb300.mlp import MLP
+    rng = np.random.default_rng(4)
+    X = rng.uniform(-1, 1, (3000, 7)).astype(np.float32)
+    y = rng.uniform(0, 0.7, 3000).astype(np.float32)
+    out = []
+    for split in ((20,), (7, 13)):
+        m = MLP(hidden=128, layers=3, seed=5)
+        m.set_data(X, y)
+        n0 = m.launches()
+        losses = np.concatenate([np.asarray(m.train(k, batch=1024)) for k in split])
+        out.append((m.params(), losses, m.launches() - n0))
+        m.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2] and out[0][2] % 20 == 0
+    assert np.all(np.isfinite(out[0][1])) and out[0][1][-1] < out[0][1][0]
