@@ -672,7 +672,7 @@ def at_spread(rg, device: int, cycles: int, runs: int):
             "seconds": {"reference_runs": round(cpu_s, 1), "gpu_engine": round(gpu_s, 1)}, "threads": threads}
 
 
-AT_WARM_TOLERANCES = [200.0, 100.0, 50.0, 20.0, 10.0, 5.0, 2.0, 1.0, 0.5]
+AT_WARM_TOLERANCES = [100.0, 50.0, 20.0, 10.0, 5.0, 2.0, 1.0, 0.5, 0.3, 0.2, 0.1, 0.05]
 
 
 def warm_start_at(rg, device: int, cap: float, ref_seconds: float, data_seconds: float, train_steps: int,
