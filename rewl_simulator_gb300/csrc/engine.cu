@@ -669,8 +669,10 @@ __device__ __forceinline__ long long lds64(const char* base, int off)
 }
 __device__ __forceinline__ void sts64(char* base, int off, long long v) { *reinterpret_cast<long long*>(base + off) = v; }
 
+// The sweeps of one warp's G walkers (launch position warp_index; its shared memory starts at
+// warp_base, one region of p.smem_per_warp bytes per walker).
 template <int G, int C, bool OBS>
-__global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
+__device__ __forceinline__ void sweep_bins_warp(const SweepParams& p, const int warp_index, unsigned char* warp_base)
 {
     constexpr int P = 32 / G;
     constexpr int SPL = (C + P - 1) / P;          // sites per lane in a chunk
@@ -678,9 +680,9 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     constexpr int kAhead = 4;                     // per-site inputs are read this many sites early
     static_assert(C % 4 == 0 && C >= 4 && C <= 32 && P >= 4, "chunk");
     extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     const int grp = lane / P, q = lane - grp * P, gbase = grp * P;
-    const int li = (blockIdx.x * (blockDim.x >> 5) + wib) * G + grp;
+    const int li = warp_index * G + grp;
     const bool valid = li < p.nslots;
     if (__ballot_sync(kFull, valid) == 0 || engine_failed_warp(p.P.counters)) return;   // no walkers, or stopped
     const DevPtrs& P_ = p.P;
@@ -689,7 +691,7 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     const int w = P_.slot_win[s];
     const WinDev W = P_.win[w];
     const int L = I.L, N = I.N, nb = W.nb;
-    unsigned char* base = smem + (size_t)(wib * G + grp) * p.smem_per_warp;
+    unsigned char* base = warp_base + (size_t)grp * p.smem_per_warp;
     const int gs_bytes = ((p.nbcap + 2 * kGuard) * 8 + 15) & ~15;
     long long* gs = reinterpret_cast<long long*>(base) + kGuard;     // gs[-kGuard .. nb+kGuard)
     int8_t* lat = reinterpret_cast<int8_t*>(base + gs_bytes);
@@ -1009,6 +1011,14 @@ __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p
     }
 }
 
+template <int G, int C, bool OBS>
+__global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wib = threadIdx.x >> 5;
+    sweep_bins_warp<G, C, OBS>(p, blockIdx.x * (blockDim.x >> 5) + wib, smem + (size_t)wib * G * p.smem_per_warp);
+}
+
 template <int G, bool OBS>
 void launch_bins_t(int C, dim3 grid, dim3 block, size_t smem, cudaStream_t st, const SweepParams& sp)
 {
@@ -1139,13 +1149,12 @@ __device__ __forceinline__ void table_step(TableChain& c, const int j, TableStag
 // Ashkin-Teller instances, whose windows hold tens of thousands of bins, and Ising windows too
 // large for shared memory).  One warp per walker; the planes sweep in turn (sigma then tau for
 // Ashkin-Teller, wang_landau.hpp:109-119), the flipped plane toggling after each pass.
+// The sweeps of one walker (launch position li; the warp's shared memory starts at warp_base).
 template <class Model, bool REPLAY, bool OBS>
-__global__ void __launch_bounds__(256, 2) k_sweep_tables(const SweepParams p)
+__device__ __forceinline__ void sweep_tables_warp(const SweepParams& p, const int li, unsigned char* warp_base)
 {
     constexpr int NP = Model::kPlanes, NM = Model::kMags, NC = Model::kCorrPlanes;
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int li = blockIdx.x * (blockDim.x >> 5) + wib;
+    const int lane = threadIdx.x & 31;
     if (li >= p.nslots || engine_failed_warp(p.P.counters)) return;
     const DevPtrs& P = p.P;
     const int s = p.slots[li];
@@ -1153,7 +1162,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep_tables(const SweepParams p)
     const int w = P.slot_win[s];
     const WinDev W = P.win[w];
     const int L = I.L, N = I.N, C = I.chunk, nb = W.nb;
-    unsigned char* base = smem + (size_t)wib * p.smem_per_warp;
+    unsigned char* base = warp_base;
     TableStage* st = reinterpret_cast<TableStage*>(base);
     int8_t* sp = reinterpret_cast<int8_t*>(st + 1);       // NP planes of N spins
     const int64_t* hf = I.field_off >= 0 ? P.fields + I.field_off : nullptr;
@@ -1332,6 +1341,84 @@ __global__ void __launch_bounds__(256, 2) k_sweep_tables(const SweepParams p)
         if (NP == 2) P.slot_flavour[s] = flavour;
         if (REPLAY) P.slot_draws[s] = c.draws;
         if (c.err) atomicOr(&P.counters[0], c.err);
+    }
+}
+
+template <class Model, bool REPLAY, bool OBS>
+__global__ void __launch_bounds__(256, 2) k_sweep_tables(const SweepParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wib = threadIdx.x >> 5;
+    sweep_tables_warp<Model, REPLAY, OBS>(p, blockIdx.x * (blockDim.x >> 5) + wib, smem + (size_t)wib * p.smem_per_warp);
+}
+
+// --------------------------------------------------------------------------
+// One persistent, work-stealing launch for every launch group of a batch
+// (rewl_batch_desc.persistent): a grid sized to the resident capacity, each warp
+// taking the next walker from a device counter until all walkers of the sweep phase
+// are done.  A task is one walker (one walker per warp); tasks are ordered by
+// expected cost, the Ashkin-Teller walkers and the largest lattices first.  Each
+// kind of group runs its own kernel's per-warp function, not inlined here, so the
+// fused kernel's registers are those of its dispatch loop plus the largest callee.
+// --------------------------------------------------------------------------
+enum FusedKind : int {
+    kFusedBins32 = 0, kFusedBins24 = 1, kFusedBins16 = 2, kFusedBins8 = 3, kFusedBins4 = 4,
+    kFusedTablesIsing = 5, kFusedTablesAT = 6
+};
+constexpr int kMaxFusedGroups = 16;
+
+struct FusedGroup {
+    const int32_t* slots;
+    int nslots, smem_per_warp, nbcap, kind, first_task, pad;
+};
+
+struct FusedParams {
+    DevPtrs P;
+    int nsweeps, ngroups, ntasks, slot_bytes;
+    unsigned int* counter;
+    FusedGroup g[kMaxFusedGroups];
+};
+
+template <int C, bool OBS>
+__device__ __noinline__ void fused_bins(const SweepParams& p, int unit, unsigned char* base)
+{
+    sweep_bins_warp<1, C, OBS>(p, unit, base);
+}
+
+template <class Model, bool OBS>
+__device__ __noinline__ void fused_tables(const SweepParams& p, int unit, unsigned char* base)
+{
+    sweep_tables_warp<Model, false, OBS>(p, unit, base);
+}
+
+template <bool OBS>
+__global__ void __launch_bounds__(128) k_sweep_fused(const FusedParams fp)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    unsigned char* base = smem + (size_t)wib * fp.slot_bytes;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = (int)atomicAdd(fp.counter, 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= fp.ntasks) break;
+        int gi = 0;
+        while (gi + 1 < fp.ngroups && t >= fp.g[gi + 1].first_task) ++gi;
+        const FusedGroup& G = fp.g[gi];
+        SweepParams sp;
+        sp.P = fp.P; sp.slots = G.slots; sp.nslots = G.nslots; sp.nsweeps = fp.nsweeps;
+        sp.smem_per_warp = G.smem_per_warp; sp.nbcap = G.nbcap;
+        const int unit = t - G.first_task;
+        switch (G.kind) {
+        case kFusedBins32: fused_bins<32, OBS>(sp, unit, base); break;
+        case kFusedBins24: fused_bins<24, OBS>(sp, unit, base); break;
+        case kFusedBins16: fused_bins<16, OBS>(sp, unit, base); break;
+        case kFusedBins8: fused_bins<8, OBS>(sp, unit, base); break;
+        case kFusedBins4: fused_bins<4, OBS>(sp, unit, base); break;
+        case kFusedTablesIsing: fused_tables<Ising2dModel, OBS>(sp, unit, base); break;
+        default: fused_tables<AshkinTeller2dModel, OBS>(sp, unit, base); break;
+        }
+        __syncwarp();
     }
 }
 
