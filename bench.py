@@ -279,7 +279,8 @@ def make_batch(rg, seed: int, device: int, observables: int | None = None):
         return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
                         sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
                         lnf_final=w["lnf_final"], device=device, mask_mode=rg.MASK_VISITED,
-                        graphs=w["graphs"], autotune=w["autotune"], observables=obs)
+                        graphs=w["graphs"], autotune=w["autotune"], observables=obs,
+                        persistent=w.get("persistent", 0))
     if w["model"] == "ising2d":
         inss = [rg.Instance(model=rg.MODEL_ISING2D, L=w["L"], energy_min=w["energy_min"], energy_max=w["energy_max"],
                             bin_width=w["bin_width"], num_windows=w["num_windows"],
@@ -296,7 +297,7 @@ def make_batch(rg, seed: int, device: int, observables: int | None = None):
     return rg.Batch(instances=inss, sweeps_per_exchange=w["sweeps_per_exchange"],
                     sweeps_per_check=w["sweeps_per_check"], flatness_param=0.8, lnf_initial=w["lnf_initial"],
                     lnf_final=w["lnf_final"], device=device, mask_mode=mask, observables=obs,
-                    one_over_t=w["one_over_t"], graphs=w["graphs"])
+                    one_over_t=w["one_over_t"], graphs=w["graphs"], persistent=w.get("persistent", 0))
 
 
 # --------------------------------------------------------------------------- CPU leg
@@ -986,6 +987,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c5",
                     help="c5: Ising L=64, 64 windows x 8 walkers (default, the headline configuration); c2: Ising "
                          "L=32, 16 x 8; at: Ashkin-Teller L=32, 64 realisations; mixed: the uneven batch")
+    ap.add_argument("--persistent", action="store_true",
+                    help="every launch group in one persistent work-stealing launch per sweep phase")
     ap.add_argument("--replicas", type=int, default=0,
                     help="walkers per window (default: the workload's; Ising workloads only)")
     ap.add_argument("--at-spread", type=int, default=0, metavar="CYCLES",
@@ -1012,6 +1015,9 @@ def main():
     if args.observables:
         WORKLOADS[args.workload]["observables"] = args.observables
         select_workload(args.workload)
+    if args.persistent:
+        WORKLOADS[args.workload]["persistent"] = 1
+        WORKLOADS[args.workload]["name"] += "_persistent"
     if args.replicas:
         if WORKLOAD["model"] != "ising2d":
             ap.error("--replicas applies to the Ising workloads")

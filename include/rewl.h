@@ -97,6 +97,8 @@ typedef struct rewl_batch_desc {
     int32_t graphs;               /* 1: rewl_run_cycles replays each check interval (sweeps, exchanges,
                                      flatness step) as one captured CUDA graph */
     int32_t autotune;             /* 1: the first rewl_run_cycles call runs rewl_autotune first */
+    int32_t persistent;           /* 1: every launch group's walkers in one persistent, work-stealing launch
+                                     per sweep phase (one walker per warp; Philox streams only) */
     const rewl_instance_desc* instances;
 } rewl_batch_desc;
 

@@ -1778,6 +1778,12 @@ struct rewl_engine {
     // bound of every window's ln f (2^-40 units; k_flat only lowers it, except the 1/t rule,
     // which never exceeds 1) and the largest number of degrees of freedom of a walker
     int64_t lnf_bound_u = 0, ndof_max = 0;
+    // rewl_batch_desc.persistent: every launch group in one work-stealing launch (k_sweep_fused)
+    bool fused = false;
+    FusedParams fused_p{};
+    int fused_grid = 0, fused_block = 128;
+    size_t fused_smem = 0;
+    DBuf<unsigned int> fused_counter;
     cudaStream_t stream = nullptr;
     std::vector<Launch> launches;
     std::vector<cudaEvent_t> ev_pool;
@@ -1848,7 +1854,7 @@ struct rewl_engine {
         d_inst.free_(); d_win.free_();
         slot_inst.free_(); slot_win.free_(); slot_cfg.free_(); slot_nb.free_(); slot_flavour.free_();
         pairs[0].free_(); pairs[1].free_();
-        obs.free_(); gsnap.free_(); qtab.free_(); xround.free_();
+        obs.free_(); gsnap.free_(); qtab.free_(); xround.free_(); fused_counter.free_();
         for (cudaStream_t st : gstreams) cudaStreamDestroy(st);
         gstreams.clear();
         for (cudaEvent_t ev : join_ev) cudaEventDestroy(ev);
@@ -1966,6 +1972,11 @@ int build_host(rewl_engine* e)
         return fail(REWL_EINVAL, "observables must be 0 (off), 1 (moments) or 2 (moments and G(q_min) correlators)");
     if (D.walkers_per_warp != 0 && D.walkers_per_warp != 1 && D.walkers_per_warp != 2 && D.walkers_per_warp != 4)
         return fail(REWL_EINVAL, "walkers_per_warp must be 0, 1, 2 or 4");
+    if (D.persistent != 0 && D.persistent != 1) return fail(REWL_EINVAL, "persistent must be 0 or 1");
+    if (D.persistent && D.rng_mode == REWL_RNG_REPLAY)
+        return fail(REWL_EINVAL, "the persistent launch runs Philox streams only (rng_mode REWL_RNG_PHILOX)");
+    if (D.persistent && D.walkers_per_warp > 1)
+        return fail(REWL_EINVAL, "the persistent launch runs one walker per warp");
     int slot = 0, win = 0;
     int64_t tab = 0, spin = 0, maskoff = 0, fieldoff = 0;
     std::vector<int64_t> h_fields;
@@ -2200,6 +2211,63 @@ bool shape_fits(const Launch& l, int G, int wpb)
     return (size_t)wpb * (l.bins ? G : 1) * l.smem_per_warp <= 200 * 1024;
 }
 
+// The persistent launch: every group's walkers as tasks of one work-stealing kernel.  Groups are
+// ordered by the expected cost of one walker's sweep (degrees of freedom x cycles per flip of
+// its kernel, measured: table kernel ~440, bin-tracking ~70), the dearest first, so that the
+// last tasks taken are short.  Every warp gets the largest shared-memory region any group needs.
+int plan_fused(rewl_engine* e, int nsm)
+{
+    if (e->launches.size() > (size_t)kMaxFusedGroups)
+        return fail(REWL_EINVAL, "the persistent launch takes at most %d launch groups (%zu here)", kMaxFusedGroups,
+                    e->launches.size());
+    std::vector<std::pair<double, size_t>> order;
+    for (size_t gi = 0; gi < e->launches.size(); ++gi) {
+        const Launch& l = e->launches[gi];
+        int ndof = 0;
+        for (int s : l.slots) ndof = std::max(ndof, e->inst[e->h_slot_inst[s]].dev.ndof);
+        order.push_back({-(double)ndof * (l.bins ? 70.0 : 440.0), gi});
+    }
+    std::stable_sort(order.begin(), order.end());
+    FusedParams& F = e->fused_p;
+    F = FusedParams{};
+    int task = 0, slot = 16;
+    for (size_t k = 0; k < order.size(); ++k) {
+        const Launch& l = e->launches[order[k].second];
+        FusedGroup& G = F.g[k];
+        G.slots = l.d_slots.p; G.nslots = (int)l.slots.size(); G.smem_per_warp = l.smem_per_warp; G.nbcap = l.nbcap;
+        if (l.bins)
+            G.kind = l.chunk == 32 ? kFusedBins32 : l.chunk == 24 ? kFusedBins24 : l.chunk == 16 ? kFusedBins16
+                   : l.chunk == 8 ? kFusedBins8 : kFusedBins4;
+        else if (l.tables)
+            G.kind = l.model == REWL_MODEL_ISING2D ? kFusedTablesIsing : kFusedTablesAT;
+        else
+            return fail(REWL_EINVAL, "internal: a launch group without a persistent form");
+        G.first_task = task;
+        task += G.nslots;
+        slot = std::max(slot, l.smem_per_warp);
+    }
+    F.ngroups = (int)order.size();
+    F.ntasks = task;
+    F.slot_bytes = (slot + 15) & ~15;
+    int warps = 4;
+    while (warps > 1 && (size_t)warps * F.slot_bytes > 200 * 1024) warps >>= 1;
+    if ((size_t)F.slot_bytes > 220 * 1024) return fail(REWL_EINVAL, "a walker needs %d bytes of shared memory", F.slot_bytes);
+    e->fused_block = 32 * warps;
+    e->fused_smem = (size_t)warps * F.slot_bytes;
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUDA_TRY(cudaFuncSetAttribute(k_sweep_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    int per_sm = 0;
+    if (e->desc.observables)
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_fused<true>, e->fused_block, e->fused_smem));
+    else
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_fused<false>, e->fused_block, e->fused_smem));
+    const int need = (task + warps - 1) / warps;
+    e->fused_grid = std::max(1, std::min(need, std::max(1, per_sm) * nsm));
+    if (int rc = e->fused_counter.alloc(1)) return rc;
+    e->fused = true;
+    return REWL_OK;
+}
+
 int plan_launches(rewl_engine* e)
 {
     const int nsm = sm_count(e);
@@ -2237,7 +2305,7 @@ int plan_launches(rewl_engine* e)
         }
         const int n = (int)l.slots.size();
         if (l.bins) {
-            int G = e->desc.walkers_per_warp;
+            int G = e->desc.persistent ? 1 : e->desc.walkers_per_warp;
             if (G == 0) {
                 // one walker per warp while the SM sub-partitions outnumber the walkers
                 // (the chain is latency-bound); pack walkers into warps beyond that
@@ -2261,7 +2329,8 @@ int plan_launches(rewl_engine* e)
             const size_t ising_smem = (size_t)(((maxnb + 1) & ~1) * 8 + sizeof(Stage) + ((maxN + 15) & ~15) + (corr ? 8 * maxL : 0));
             // Ising windows live in shared memory unless they do not fit there (or the
             // global-table kernel is asked for)
-            l.tables = l.model != REWL_MODEL_ISING2D || e->sweep_variant == 4 || ising_smem > 200 * 1024;
+            l.tables = l.model != REWL_MODEL_ISING2D || e->sweep_variant == 4 || ising_smem > 200 * 1024 ||
+                       e->desc.persistent;             // the persistent launch has the global-table form only
             if (!l.tables) {
                 l.nbcap = (maxnb + 1) & ~1;
                 l.smem_per_warp = (int)ising_smem;
@@ -2299,6 +2368,7 @@ int plan_launches(rewl_engine* e)
     CUDA_TRY(allow_bins_smem<1>());
     CUDA_TRY(allow_bins_smem<2>());
     CUDA_TRY(allow_bins_smem<4>());
+    if (e->desc.persistent) return plan_fused(e, nsm);
     if (e->launches.size() > 1) {
         CUDA_TRY(cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming));
         for (size_t gi = 0; gi < e->launches.size(); ++gi) {
@@ -2423,6 +2493,23 @@ int launch_sweeps_once(rewl_engine* e, int nsweeps)
 {
     const DevPtrs P = e->ptrs();
     CUDA_TRY(record_timing(e));
+    if (e->fused) {
+        FusedParams F = e->fused_p;
+        F.P = P;
+        F.nsweeps = nsweeps;
+        F.counter = e->fused_counter.p;
+        CUDA_TRY(cudaMemsetAsync(e->fused_counter.p, 0, sizeof(unsigned int), e->stream));
+        if (e->desc.observables) k_sweep_fused<true><<<e->fused_grid, e->fused_block, e->fused_smem, e->stream>>>(F);
+        else k_sweep_fused<false><<<e->fused_grid, e->fused_block, e->fused_smem, e->stream>>>(F);
+        CUDA_TRY(cudaGetLastError());
+        e->kernel_launches++;
+        e->launches_total++;
+        CUDA_TRY(record_timing(e));
+        e->sweeps_total += nsweeps;
+        e->sweeps_since_check += nsweeps;
+        e->flips_total += (int64_t)nsweeps * e->flips_per_sweep;
+        return REWL_OK;
+    }
     // several launch groups (models, lattice sizes, kernel shapes) run concurrently, each on
     // its own stream forked from and joined back into the engine stream; they touch disjoint
     // walkers
@@ -3501,6 +3588,7 @@ int rewl_restore(rewl_engine* e, const void* buffer, size_t bytes)
 int rewl_autotune(rewl_engine* e, int32_t sweeps)
 {
     if (!e || sweeps < 0) return fail(REWL_EINVAL, "bad arguments");
+    if (e->fused) { e->tuned = true; return REWL_OK; }     // one walker per warp, grid sized to residency
     cudaSetDevice(e->desc.device);
     size_t bytes = 0;
     if (int rc = rewl_snapshot_size(e, &bytes)) return rc;

@@ -59,6 +59,7 @@ class _BatchDesc(C.Structure):
                 ("one_over_t", C.c_int32), ("reduce_logdos", C.c_int32), ("rng_mode", C.c_int32),
                 ("device", C.c_int32), ("warps_per_block", C.c_int32), ("walkers_per_warp", C.c_int32),
                 ("observables", C.c_int32), ("graphs", C.c_int32), ("autotune", C.c_int32),
+                ("persistent", C.c_int32),
                 ("instances", C.c_void_p)]
 
 
@@ -115,6 +116,7 @@ class Batch:
     observables: int = 0            # 1: per-bin moments; 2: also the G(q_min) correlators
     graphs: int = 0                 # 1: replay each check interval as one captured CUDA graph
     autotune: int = 0               # 1: time the launch groups' kernel shapes before the first cycle
+    persistent: int = 0             # 1: all launch groups in one persistent work-stealing launch per phase
 
 
 @dataclass
@@ -223,7 +225,7 @@ class Engine:
         b.num_instances = n
         for name in ("sweeps_per_exchange", "sweeps_per_check", "flatness_mode", "flatness_param", "lnf_initial",
                      "lnf_final", "mask_mode", "one_over_t", "reduce_logdos", "rng_mode", "device",
-                     "warps_per_block", "walkers_per_warp", "observables", "graphs", "autotune"):
+                     "warps_per_block", "walkers_per_warp", "observables", "graphs", "autotune", "persistent"):
             setattr(b, name, getattr(batch, name))
         b.instances = C.cast(self._inst, C.c_void_p)
         self._desc = b

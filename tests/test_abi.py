@@ -59,6 +59,7 @@ BAD = [
     dict(window_overlap=1.0), dict(bin_width=3.0), dict(J=0.5), dict(energy_max=-200.0),
     dict(sweeps_per_check=15), dict(sweeps_per_exchange=0), dict(lnf_initial=0.0), dict(flatness_mode=5),
     dict(mask_mode=3), dict(rng_mode=9), dict(warps_per_block=3), dict(walkers_per_warp=3), dict(init_mode=2),
+    dict(persistent=2), dict(persistent=1, rng_mode=1), dict(persistent=1, walkers_per_warp=2), dict(lnf_initial=65.0),
     dict(num_windows=40, window_overlap=0.0, energy_min=-128.0, energy_max=-120.0),
 ]
 

@@ -22,11 +22,14 @@ INSTANCES = [
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("graphs,autotune", [(0, 0), (1, 0), (1, 1)], ids=["eager", "graphs", "graphs_autotuned"])
-def test_mixed_batch_instances_match_their_oracles(engine_lib, oracle_lib, graphs, autotune):
+@pytest.mark.parametrize("graphs,autotune,persistent", [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 0, 1), (1, 1, 1)],
+                         ids=["eager", "graphs", "graphs_autotuned", "persistent", "persistent_graphs"])
+def test_mixed_batch_instances_match_their_oracles(engine_lib, oracle_lib, graphs, autotune, persistent):
     """The launch groups (two bin-tracking shapes, the general Ising kernel, Ashkin-Teller) run
     concurrently on their own streams; with graphs each check interval replays as one captured
-    graph; the autotuner times the groups' shapes first.  None of it may change a trajectory."""
+    graph; the autotuner times the groups' shapes first.  With `persistent` every group's walkers
+    are tasks of one work-stealing launch (the bin width 8 instance on the global-table form).
+    None of it may change a trajectory."""
     rg, po = engine_lib, oracle_lib
     inss, orcs = [], []
     for name, model, L, K, sig, emin, emax, bw, nwin, R, seed in INSTANCES:
@@ -42,7 +45,8 @@ def test_mixed_batch_instances_match_their_oracles(engine_lib, oracle_lib, graph
                         semantics=po.SEM_ENGINE, seed=seed)
         orcs.append(po.Oracle(cfg, fields=fields))
     b = rg.Batch(instances=inss, sweeps_per_exchange=SE, sweeps_per_check=SC, flatness_param=0.8,
-                 lnf_initial=1.0, lnf_final=LNF_FINAL, mask_mode=rg.MASK_VISITED, graphs=graphs, autotune=autotune)
+                 lnf_initial=1.0, lnf_final=LNF_FINAL, mask_mode=rg.MASK_VISITED, graphs=graphs, autotune=autotune,
+                 persistent=persistent)
     eng = rg.Engine(b)
     try:
         def compare(tag):
