@@ -856,7 +856,7 @@ def run_gpu(args):
         st1 = eng.status()
         kern_ms, kern_launches = eng.sweep_kernel_time()
         shapes = np.asarray(eng.launch_shapes()).tolist()
-        groups = max(1, len(shapes))
+        groups = 1 if WORKLOAD.get("persistent") else max(1, len(shapes))    # launches per sweep phase
     total_ms = sum(step_ms)
     flips = st1.attempted_flips - st0.attempted_flips
     launches = st1.kernel_launches - st0.kernel_launches
