@@ -66,7 +66,7 @@ typedef struct rewl_instance_desc {
     double energy_max;
     double bin_width;             /* Ising: power of two; Ashkin-Teller: 1/n or power of two */
     int32_t num_windows;          /* glazier windows (src/REWL/glazier.hpp:70-115) */
-    int32_t replicas_per_window;  /* REWL_Parameters::replicas_per_window */
+    int32_t replicas_per_window;  /* REWL_Parameters::replicas_per_window, 1..64 */
     double window_overlap;        /* REWL_Parameters::window_overlap */
     int32_t init_mode;            /* 0: spins uniform +-1 from the seed; 1: all +1 */
     int32_t reserved;

@@ -766,7 +766,8 @@ template <class M> static void exchange(Sim<M>& S)
                 const double a = lo.logdos[S.lbin(lo, Eh)] - lo.logdos[S.lbin(lo, El)];
                 const double b = hi.logdos[S.lbin(hi, El)] - hi.logdos[S.lbin(hi, Eh)];
                 const double delta = std::max(0., a) + std::max(0., b);
-                const uint32_t word = philox_word(S.key, 0x80000000u, (uint64_t)(32 + r),
+                // after the R - 1 pairing words: counter 32 + r while R <= 32, 64 + r above
+                const uint32_t word = philox_word(S.key, 0x80000000u, (uint64_t)((R <= 32 ? 32 : 64) + r),
                                                   STREAM_EXCH, (uint32_t)((S.exch_round << 8) ^ (uint64_t)lw));
                 const float thr = neglog_u32(word);
                 const int64_t d = (int64_t)std::llround(delta * QSCALE);

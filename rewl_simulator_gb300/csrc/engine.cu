@@ -76,7 +76,7 @@ int fail(int code, const char* fmt, ...)
                         __FILE__, __LINE__);                                           \
     } while (0)
 
-constexpr int kMaxReplicas = 32;
+constexpr int kMaxReplicas = 64;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 enum : int { ERR_BOUNDS = 1, ERR_ADJUST = 2, ERR_REPLAY_EXHAUSTED = 4, ERR_RANGE = 8, ERR_COUNT = 16 };
@@ -1498,7 +1498,8 @@ __device__ void exchange_pair(const DevPtrs& P, const int32_t* pairs, int k, uin
             const int64_t a = gl[bl_h] - gl[bl_l];
             const int64_t c = gh[bh_l] - gh[bh_h];
             const int64_t d = (a > 0 ? a : 0) + (c > 0 ? c : 0);
-            const uint32_t word = philox_word(I.seed, xuid, (uint64_t)(32 + r), kStreamExchange, w3);
+            // acceptance words follow the R - 1 pairing words: counter 32 + r while R <= 32, 64 + r above
+            const uint32_t word = philox_word(I.seed, xuid, (uint64_t)((R <= 32 ? 32 : 64) + r), kStreamExchange, w3);
             accept = d < accept_threshold(neglog_u32(word));
         }
         if (accept) { P.slot_cfg[lo] = ch; P.slot_cfg[hi] = cl; ++accn; }

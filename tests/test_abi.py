@@ -55,7 +55,7 @@ def _create(engine_lib, **overrides):
 
 
 BAD = [
-    dict(L=1), dict(L=200), dict(model=7), dict(num_windows=0), dict(replicas_per_window=33),
+    dict(L=1), dict(L=200), dict(model=7), dict(num_windows=0), dict(replicas_per_window=65),
     dict(window_overlap=1.0), dict(bin_width=3.0), dict(J=0.5), dict(energy_max=-200.0),
     dict(sweeps_per_check=15), dict(sweeps_per_exchange=0), dict(lnf_initial=0.0), dict(flatness_mode=5),
     dict(mask_mode=3), dict(rng_mode=9), dict(warps_per_block=3), dict(walkers_per_warp=3), dict(init_mode=2),

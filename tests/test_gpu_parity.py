@@ -313,6 +313,8 @@ FLAT_CASES = [
     ("ising_L8_3x8", 0, 8, -128.0, 132.0, 4.0, 3, 8, 50, 100, 11, 12, 0.0, 0.0, 0, 0.8, 0, 0, 0, 3, False),
     ("ising_L8_3x8_2perwarp", 0, 8, -128.0, 132.0, 4.0, 3, 8, 50, 100, 11, 12, 0.0, 0.0, 0, 0.8, 0, 0, 2, 3, False),
     ("ising_L16_4x8", 0, 16, -512.0, 516.0, 4.0, 4, 8, 100, 200, 17, 10, 0.0, 0.0, 0, 0.8, 0, 0, 0, 2, False),
+    # more than 32 replicas per window (the exchange's acceptance words then start at counter 64)
+    ("ising_L6_2x40", 0, 6, -72.0, 76.0, 4.0, 2, 40, 50, 100, 11, 20, 0.0, 0.0, 0, 0.8, 0, 0, 0, 5, False),
     # the reference's classic rule (max - min) / min <= 0.3 (rewl_histograms.hpp:131-152)
     ("ising_L8_max_min_ratio", 0, 8, -128.0, 132.0, 4.0, 3, 2, 50, 100, 11, 20, 0.0, 0.0, 1, 0.3, 0, 0, 0, 7, False),
     # the reference's default build: 1/t with the all-visited rule (rewl_histograms.hpp:115-130,
