@@ -2309,8 +2309,10 @@ int plan_launches(rewl_engine* e)
             int G = e->desc.persistent ? 1 : e->desc.walkers_per_warp;
             if (G == 0) {
                 // one walker per warp while the SM sub-partitions outnumber the walkers
-                // (the chain is latency-bound); pack walkers into warps beyond that
-                G = n <= 4 * nsm ? 1 : (n <= 16 * nsm ? 2 : 4);
+                // (the chain is latency-bound); two per warp beyond that (measured at L = 64: two
+                // per warp beat four from 2048 to 4096 walkers, 3.77e10 against 3.43e10 flips/s at
+                // 3072); four only for still larger batches
+                G = n <= 4 * nsm ? 1 : (n <= 32 * nsm ? 2 : 4);
             }
             l.walkers_per_warp = G;
             l.nbcap = (maxnb + 1) & ~1;
