@@ -899,14 +899,16 @@ def run_gpu(args):
     sm_mhz = clocks.get("sm_mhz") or sm_max_mhz
     roofline = {"bound": WORKLOAD["bound"], "kernel": WORKLOAD["kernel"], "avg_launch_ms": avg_launch_ms,
                 "flips_per_launch": flips_per_launch, "launch_shapes": shapes}
-    if WORKLOAD["model"] == "ising2d":
+    if WORKLOAD["model"] != "mixed":
         # the serial accept chain of one walker: cycles per attempted flip against the design's floor
         walker_flips = WORKLOAD["sweeps_per_exchange"] * ndof(WORKLOAD)
         cycles = avg_launch_ms * 1e-3 * sm_mhz * 1e6 / walker_flips
+        kind = "chain floor: dependent shared load (29) + 64-bit compare/select (11), measured on a GB300"
+        if WORKLOAD["model"] != "ising2d":
+            kind += "; this kernel's dependent loads come from L1/L2 (tables of tens of thousands of bins)"
         roofline.update({"unit": "cycles/flip", "achieved": cycles, "peak": CHAIN_FLOOR_CYCLES,
                          "frac": CHAIN_FLOOR_CYCLES / cycles, "walkers_per_warp": int(shapes[0][2]) if shapes else 1,
-                         "peak_kind": "chain floor: dependent shared load (29) + 64-bit compare/select (11), "
-                                      "measured on a GB300",
+                         "peak_kind": kind,
                          "note": "per walker: launch time x median SM clock / flips of one walker; frac = floor / "
                                  "achieved"})
     else:

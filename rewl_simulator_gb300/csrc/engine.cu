@@ -1064,6 +1064,11 @@ cudaError_t allow_bins_smem()
 // derived at its end from the change of g against a copy taken at its start
 // (every visit adds the same ln f), and the chain loads both possible proposals
 // of the next step one step ahead, so a load's latency overlaps a decision.
+#ifndef REWL_TABLE_REACH
+#define REWL_TABLE_REACH 512
+#endif
+constexpr int kTableReach = REWL_TABLE_REACH;        // bins either side prefetched per chunk
+
 struct TableStage {
     longlong2 du[32];        // per site: {proposal, proposal after its left neighbour flipped in this chunk}
     long long T[32];         // acceptance thresholds of the chunk's sites
@@ -1223,6 +1228,15 @@ __device__ __forceinline__ void sweep_tables_warp(const SweepParams& p, const in
             const int8_t* B = NP == 1 ? A : sp + (plane ^ 1) * N;
             const uint64_t A0 = ((sweeps0 + (uint64_t)sw) * (uint64_t)NP + (uint64_t)pass) * (uint64_t)N;
             for (int c0 = 0; c0 < N; c0 += C) {
+                {
+                    // bring the lines of g within kTableReach bins of the walker's bin into L1
+                    // (the chunk's proposals mostly fall there), one line per lane per 512 bins
+                    const int bcur = __shfl_sync(kFull, c.b, 0);
+                    for (int k = lane * 16 - kTableReach; k <= kTableReach; k += 32 * 16) {
+                        const int bb = bcur + k;
+                        if ((unsigned)bb < (unsigned)nb) asm volatile("prefetch.global.L1 [%0];" ::"l"(gg + bb));
+                    }
+                }
                 int ai = 0, sg[NM];
                 for (int m = 0; m < NM; ++m) sg[m] = 0;
                 if (lane < C) {
