@@ -8,6 +8,7 @@
 // A batch of 4096 is 4096 x 256 x 256 per hidden GEMM, i.e. latency-bound work.
 // The tiles are therefore small (128 x 64 on tcgen05, 64 x 64 on mma.sync) so
 // that a layer spans many blocks, and every GEMM of a step runs on one stream.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -200,34 +201,37 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g)
 // The same GEMM on the 5th-generation tensor cores (tcgen05), the default.
 //
 // One CTA computes a 128 x 64 tile of C.  Its K range is cut into blocks of 64
-// that stream through a ring of four shared-memory stages by cp.async (16-byte
-// copies, zero-filled outside the matrix), three blocks ahead of the one being
-// multiplied.  Tiles are kept in tcgen05's canonical layouts without swizzle:
-// "core matrices" of 8 rows x 16 B (128 contiguous bytes), the 8 core matrices
-// along K of an 8-wide group of rows (M or N) side by side (LBO = 128 B), groups
-// 1024 B apart (SBO).  An operand stored with K contiguous uses the K-major form
-// (a core row = 8 consecutive k of one row); one stored transposed, with M or N
-// contiguous, uses the MN-major form (a core row = 8 consecutive rows at one k)
-// and the transpose bit of the instruction descriptor, so every 16-byte chunk is
-// copied as it lies in global memory.  One thread issues four tcgen05.mma
-// (M 128, N 64, K 16 each) per block from shared-memory descriptors into an
-// FP32 accumulator in tensor memory (64 columns, allocated per CTA) and commits
-// them to the stage's mbarrier, which releases the stage for the block four
-// ahead.  The epilogue reads the accumulator back with tcgen05.ld (warp w owns
-// rows 32w..32w+31, one row per thread) and applies the same epilogues as above.
+// that stream through a ring of four shared-memory stages, loaded by the tensor
+// memory accelerator (cp.async.bulk.tensor, 2-D tensor maps over A and B, rows
+// beyond the matrix zero-filled) three blocks ahead of the one being multiplied.
+// Tiles are kept in tcgen05's canonical layouts without swizzle, built from
+// "core matrices" of 8 rows x 16 B (128 contiguous bytes):
+//  * an operand stored with K contiguous (K-major: a core row = 8 consecutive k
+//    of one row) is loaded as 8 boxes of 8 k x R rows, one per 8-wide column of
+//    k, each landing R x 16 B: core matrices along K are R x 16 B apart (LBO),
+//    8-row groups 128 B apart (SBO);
+//  * an operand stored with M or N contiguous (MN-major: a core row = 8
+//    consecutive rows at one k) is loaded as R / 8 boxes of 8 rows x 64 k, each
+//    landing 1024 B: core matrices along K 128 B apart (LBO), 8-row groups 1024 B
+//    (SBO), with the transpose bit of the instruction descriptor.
+// One thread issues the copies (arming the stage's "full" mbarrier with the
+// stage's byte count) and, once a stage is full, four tcgen05.mma (M 128, N 64,
+// K 16 each) from shared-memory descriptors into an FP32 accumulator in tensor
+// memory (64 columns, allocated per CTA), committed to the stage's "empty"
+// mbarrier, which releases the stage for the block four ahead.  The epilogue reads
+// the accumulator back with tcgen05.ld (warp w owns rows 32w..32w+31, one row per
+// thread) and applies the same epilogues as above.
 //
 // Every wait on an mbarrier is bounded: on a timeout the block records
-// kTcTimeout in g_tc_error, waits once more (bounded) for its MMAs, frees its
-// tensor memory and skips the epilogue.  Rows of A beyond M and K beyond the
-// split's end are zero-filled, so M need only be a multiple of 64.
+// kTcTimeout in g_tc_error, waits once more (bounded) for the copies it issued
+// and its MMAs, frees its tensor memory and skips the epilogue.  K splits are
+// whole 64-wide blocks (gemm() checks it), so no box reaches another split's K.
 // ---------------------------------------------------------------------------
 namespace tc {
 constexpr int BM = 128, BN = 64, BK = 64, STAGES = 4;
 constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 64;   // + mbarriers and the tensor-memory address
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 128;  // + full / empty mbarriers and the tensor-memory address
 constexpr uint32_t kTmemCols = 64;                     // FP32 accumulator: 128 lanes x 64 columns
-constexpr uint32_t kLBO = 128;                         // next core matrix along K
-constexpr uint32_t kSBO = 1024;                        // next 8-row group
 // instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1),
 // A / B MN-major (transposed) in bits 15 / 16, N >> 3 in bits 17-22, M >> 4 in bits 24-28
 __host__ __device__ constexpr uint32_t idesc(bool a_mn, bool b_mn)
@@ -239,6 +243,7 @@ constexpr int kSpinLimit = 1 << 18;
 constexpr int kTcTimeout = 1;
 static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256 && BM == 128, "tcgen05.mma cta_group::1 kind::f16 shape");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(STAGE_BYTES % 1024 == 0 && A_BYTES % 1024 == 0, "stages and tiles on 1024-byte boundaries");
 }  // namespace tc
 
 __device__ int g_tc_error;
@@ -247,14 +252,11 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)_
 
 // shared-memory matrix descriptor: start >> 4 (bits 0-13), LBO >> 4 (16-29), SBO >> 4 (32-45),
 // descriptor version 1 (bits 46-47), base offset 0, no swizzle (bits 61-63 = 0)
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
 {
-    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(tc::kLBO >> 4) << 16) | ((uint64_t)(tc::kSBO >> 4) << 32) |
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
            (1ull << 46);
 }
-
-// byte offset of element (r, k) of a tile in the canonical K-major layout
-__device__ __forceinline__ int core_off(int r, int k) { return (r >> 3) * tc::kSBO + (k >> 3) * tc::kLBO + (r & 7) * 16 + (k & 7) * 2; }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
 {
@@ -267,41 +269,45 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
     return false;
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool in)
+// one 2-D box of the tensor map at (x, y) (x along the contiguous dimension, a multiple of 8
+// elements: 16 bytes) into shared memory at dst, completing `bytes` on the mbarrier bar
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar)
 {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" :: "r"(dst), "l"(src), "r"(in ? 16 : 0) : "memory");
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n"
+                 :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
-// Copy R rows x BK columns of K starting at (r0, k0) into a stage at shared address dst.
-// KMAJ: row r, column k at src[r * ld + k], K-major layout.  !KMAJ: at src[k * ld + r],
-// MN-major layout.  Chunks with rows >= rmax or k >= kmax are filled with zeros.
+// The boxes of one operand tile (R rows from r0, K block from k0) into shared memory at dst.
+// KMAJ: the map's contiguous dimension is K (boxes of 8 k x R rows); otherwise it is the rows
+// (boxes of 8 rows x BK k).
 template <int R, bool KMAJ>
-__device__ __forceinline__ void issue_tile(uint32_t dst, const bf16* src, int ld, int r0, int rmax, int k0, int kmax, int tid)
+__device__ __forceinline__ void load_tile(uint32_t dst, const CUtensorMap* map, int r0, int k0, uint32_t bar)
 {
+    if (KMAJ) {
 #pragma unroll
-    for (int c = tid; c < R * (tc::BK / 8); c += 128) {
-        if (KMAJ) {
-            // a quarter-warp covers 8 rows of one 16-byte column: 128 contiguous shared bytes
-            const int r = (c & 7) | ((c >> 6) << 3), kq = (c >> 3) & 7;
-            const int gr = r0 + r, gk = k0 + kq * 8;
-            const bool in = gr < rmax && gk < kmax;
-            cp_async16(dst + core_off(r, kq * 8), in ? src + (size_t)gr * ld + gk : src, in);
-        } else {
-            // consecutive threads take consecutive 8-row groups of one k: coalesced
-            const int mg = c % (R / 8), k = c / (R / 8);
-            const int gr = r0 + mg * 8, gk = k0 + k;
-            const bool in = gr < rmax && gk < kmax;
-            cp_async16(dst + mg * tc::kSBO + (k >> 3) * tc::kLBO + (k & 7) * 16, in ? src + (size_t)gk * ld + gr : src, in);
-        }
+        for (int c = 0; c < tc::BK / 8; ++c) tma_load_2d(dst + c * (R * 16), map, k0 + 8 * c, r0, bar);
+    } else {
+#pragma unroll
+        for (int g = 0; g < R / 8; ++g) tma_load_2d(dst + g * 1024, map, r0 + 8 * g, k0, bar);
     }
 }
 
+// descriptor of the K = 16 slice kk of an R-row operand tile at addr (layouts above)
+template <int R, bool KMAJ>
+__device__ __forceinline__ uint64_t tile_desc(uint32_t addr, int kk)
+{
+    return KMAJ ? smem_desc(addr + kk * 2 * (R * 16), R * 16, 128) : smem_desc(addr + kk * 256, 128, 1024);
+}
+
 template <bool A_KM, bool B_NK, int EPI>
-__global__ void __launch_bounds__(128) k_gemm_tc(const GemmArgs g)
+__global__ void __launch_bounds__(128) k_gemm_tc(const GemmArgs g, const __grid_constant__ CUtensorMap tmA,
+                                                 const __grid_constant__ CUtensorMap tmB)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + tc::STAGES * tc::STAGE_BYTES);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + tc::STAGES);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + tc::STAGES * tc::STAGE_BYTES);
+    uint64_t* empty = full + tc::STAGES;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(empty + tc::STAGES);
+    int* status = reinterpret_cast<int*>(tslot + 1);        // thread 0's outcome: MMAs committed, or -1
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.y * tc::BM, n0 = blockIdx.x * tc::BN;
     const int kb = blockIdx.z * g.k_per_split, ke = min(kb + g.k_per_split, g.K);
@@ -312,8 +318,10 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const GemmArgs g)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        for (int s = 0; s < tc::STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(bar + s)) : "memory");
+        for (int s = 0; s < 2 * tc::STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(full + s)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" :: "l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" :: "l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -322,57 +330,53 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const GemmArgs g)
 
     constexpr int S = tc::STAGES;
     constexpr uint32_t kId = tc::idesc(A_KM, !B_NK);
-    const uint32_t sbase = smem_u32(sm);
-    auto issue = [&](int t) {                           // block t into stage t % S (an empty group past the end)
-        if (t < nk) {
-            const uint32_t As = sbase + (t % S) * tc::STAGE_BYTES;
+    if (tid == 0) {
+        const uint32_t sbase = smem_u32(sm);
+        auto load = [&](int t) {                        // block t into stage t % S
+            const uint32_t As = sbase + (t % S) * tc::STAGE_BYTES, fb = smem_u32(full + t % S);
             const int k0 = kb + t * tc::BK;
-            issue_tile<tc::BM, !A_KM>(As, g.A, g.lda, m0, g.M, k0, ke, tid);
-            issue_tile<tc::BN, B_NK>(As + tc::A_BYTES, g.B, g.ldb, n0, g.N, k0, ke, tid);
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    };
-#pragma unroll
-    for (int t = 0; t < S - 1; ++t) issue(t);
-
-    bool ok = true;
-    int issued = 0;                                     // K blocks whose MMAs were committed
-    for (int t = 0; t < nk; ++t) {
-        if (t >= 1 && t + S - 1 < nk) {                 // block t+S-1 reuses the stage of block t-1
-            const int u = t - 1;
-            ok = __syncthreads_and(mbar_wait(smem_u32(bar + u % S), (uint32_t)((u / S) & 1)));
-            if (!ok) break;
-        }
-        issue(t + S - 1);
-        asm volatile("cp.async.wait_group %0;\n" :: "n"(S - 1) : "memory");     // block t has landed
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");           // ... and is seen by the tensor cores
-        __syncthreads();
-        if (tid == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" :: "r"(fb), "r"(tc::STAGE_BYTES) : "memory");
+            load_tile<tc::BM, !A_KM>(As, &tmA, m0, k0, fb);
+            load_tile<tc::BN, B_NK>(As + tc::A_BYTES, &tmB, n0, k0, fb);
+        };
+        int loaded = 0, issued = 0;                     // blocks whose copies / MMAs were issued
+        bool ok = true;
+        for (; loaded < min(S - 1, nk); ++loaded) load(loaded);
+        for (int t = 0; t < nk; ++t) {
+            if (loaded < nk) {                          // block t+S-1 reuses the stage of block t-1
+                if (t >= 1 && !mbar_wait(smem_u32(empty + (t - 1) % S), (uint32_t)(((t - 1) / S) & 1))) { ok = false; break; }
+                load(loaded++);
+            }
+            if (!mbar_wait(smem_u32(full + t % S), (uint32_t)((t / S) & 1))) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const uint32_t As = sbase + (t % S) * tc::STAGE_BYTES, Bs = As + tc::A_BYTES;
 #pragma unroll
             for (int kk = 0; kk < tc::BK / 16; ++kk) {
-                const uint64_t ad = smem_desc(As + kk * 2 * tc::kLBO);
-                const uint64_t bd = smem_desc(Bs + kk * 2 * tc::kLBO);
+                const uint64_t ad = tile_desc<tc::BM, !A_KM>(As, kk);
+                const uint64_t bd = tile_desc<tc::BN, B_NK>(Bs, kk);
                 const uint32_t accumulate = (t > 0 || kk > 0) ? 1u : 0u;
                 asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
                              :: "r"(tmem), "l"(ad), "l"(bd), "r"(kId), "r"(accumulate) : "memory");
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" :: "r"(smem_u32(bar + t % S)) : "memory");
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" :: "r"(smem_u32(empty + t % S)) : "memory");
+            issued = t + 1;
         }
-        issued = t + 1;
+        if (!ok) {
+            // no copy outlives the block: wait (bounded) for the copies not yet consumed
+            for (int u = issued; u < loaded; ++u) mbar_wait(smem_u32(full + u % S), (uint32_t)((u / S) & 1));
+        }
+        if (issued > 0) {                               // the last commit covers every earlier MMA
+            const int t = issued - 1;
+            ok = mbar_wait(smem_u32(empty + t % S), (uint32_t)((t / S) & 1)) && ok;
+        }
+        if (!ok) atomicOr(&g_tc_error, tc::kTcTimeout);
+        *status = ok ? issued : -1;
     }
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");      // no copy outlives the block
-    if (issued > 0) {                                   // the last commit covers every earlier MMA
-        const int t = issued - 1;
-        const bool all = __syncthreads_and(mbar_wait(smem_u32(bar + t % S), (uint32_t)((t / S) & 1)));
-        if ((!ok || !all) && tid == 0) atomicOr(&g_tc_error, tc::kTcTimeout);
-        ok = ok && all;
-    }
+    __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 
-    if (ok && issued > 0) {
+    if (*status > 0) {
         const int row = m0 + warp * 32 + lane;
 #pragma unroll
         for (int c0 = 0; c0 < tc::BN; c0 += 16) {
@@ -430,6 +434,40 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const GemmArgs g)
     }
 }
 
+// cuTensorMapEncodeTiled from the driver, found once through the runtime (no link-time
+// dependence on libcuda)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled()
+{
+    static const EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return (EncodeTiledFn) nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// A 2-D BF16 map over a matrix of `outer` rows of `inner` contiguous elements (row pitch ld
+// elements) with boxes of 8 x box_outer; reads outside the matrix return zeros.
+bool encode_operand(CUtensorMap* map, const bf16* p, int inner, int outer, int ld, int box_outer)
+{
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn || (reinterpret_cast<uintptr_t>(p) & 15) || (ld & 7) || (inner & 7)) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(bf16)};
+    const cuuint32_t box[2] = {8, (cuuint32_t)box_outer};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(p), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // REWL_MLP_GEMM=mma_sync selects the mma.sync kernel (kept for comparison)
 bool use_tcgen05()
 {
@@ -445,7 +483,13 @@ cudaError_t launch_gemm(cudaStream_t st, const GemmArgs& g, int splits)
 {
     if (use_tcgen05()) {
         static_assert(tc::BN == kBN, "tile widths agree");
-        k_gemm_tc<A_KM, B_NK, EPI><<<dim3(g.N / tc::BN, (g.M + tc::BM - 1) / tc::BM, splits), 128, tc::SMEM_BYTES, st>>>(g);
+        // A: [M][K] (K-major, boxes 8 k x 128 rows) or [K][M] (boxes 8 rows x 64 k); B likewise with N
+        CUtensorMap ma, mb;
+        if (splits > 1 && g.k_per_split % tc::BK) return cudaErrorInvalidValue;     // a box would reach the next split
+        const bool ok = (A_KM ? encode_operand(&ma, g.A, g.M, g.K, g.lda, tc::BK) : encode_operand(&ma, g.A, g.K, g.M, g.lda, tc::BM)) &&
+                        (B_NK ? encode_operand(&mb, g.B, g.K, g.N, g.ldb, tc::BN) : encode_operand(&mb, g.B, g.N, g.K, g.ldb, tc::BK));
+        if (!ok) return cudaErrorInvalidValue;
+        k_gemm_tc<A_KM, B_NK, EPI><<<dim3(g.N / tc::BN, (g.M + tc::BM - 1) / tc::BM, splits), 128, tc::SMEM_BYTES, st>>>(g, ma, mb);
     } else {
         k_gemm<A_KM, B_NK, EPI><<<dim3(g.N / kBN, g.M / kBM, splits), 128, 0, st>>>(g);
     }
@@ -457,6 +501,7 @@ cudaError_t launch_gemm(cudaStream_t st, const GemmArgs& g, int splits)
 // enqueues work, makes no attribute call.
 cudaError_t prepare_tc_kernels()
 {
+    if (use_tcgen05() && !encode_tiled()) return cudaErrorNotSupported;   // found here, not while a caller captures
     const void* kernels[] = {
         reinterpret_cast<const void*>(k_gemm_tc<false, true, EPI_BIAS_GELU>),
         reinterpret_cast<const void*>(k_gemm_tc<false, true, EPI_BIAS_F32>),
@@ -515,7 +560,14 @@ __global__ void k_sum_parts(const float* parts, int nparts, size_t stride, size_
     dst[i] = s;
 }
 
-int weight_splits(int B) { return B >= 4096 ? 16 : (B >= 1024 ? 4 : 1); }
+// K splits of a weight gradient over a batch of B rows: whole 64-row blocks per split (the
+// tensor-core GEMM's K block), 16 from 4096 rows, 4 from 1024
+int weight_splits(int B)
+{
+    if (B >= 4096 && B % (64 * 16) == 0) return 16;
+    if (B >= 1024 && B % (64 * 4) == 0) return 4;
+    return 1;
+}
 
 // loss gradient of the mean squared error mean((out[:,0] - y)^2); each row's share of the loss
 // goes to rows[b] (summed in a fixed order by k_loss_sum)
