@@ -671,13 +671,18 @@ __device__ __forceinline__ void sts64(char* base, int off, long long v) { *reint
 
 // The sweeps of one warp's G walkers (launch position warp_index; its shared memory starts at
 // warp_base, one region of p.smem_per_warp bytes per walker).
-template <int G, int C, bool OBS>
+template <int G, int C, bool OBS, bool LEAN>
 __device__ __forceinline__ void sweep_bins_warp(const SweepParams& p, const int warp_index, unsigned char* warp_base)
 {
     constexpr int P = 32 / G;
     constexpr int SPL = (C + P - 1) / P;          // sites per lane in a chunk
     constexpr int BPL = (C + P - 1) / P;          // Philox blocks per lane in a batch of 4C sites
     constexpr int kAhead = 4;                     // per-site inputs are read this many sites early
+    // LEAN: each step reads g at the next proposal after its own write (no candidate prefetch,
+    // no staleness select): five fewer ALU instructions per step and a dependent shared-memory
+    // load on the chain, which pays where enough warps share an SM to hide it
+    constexpr bool kLean = LEAN;
+    static_assert(!LEAN || G > 1, "the lean chain is for warps of several walkers");
     static_assert(C % 4 == 0 && C >= 4 && C <= 32 && P >= 4, "chunk");
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -824,7 +829,8 @@ __device__ __forceinline__ void sweep_bins_warp(const SweepParams& p, const int 
     int bp = bc + E_[0].x;                              // site 0: proposal (left neighbour unprocessed)
     long long LD = lds64(sm, bp);                       // g at the proposed bin
     int q0 = bc + E_[1].x, q1 = bp + E_[1].y;           // site 1 if site 0 is rejected / accepted
-    long long l0 = lds64(sm, q0), l1 = lds64(sm, q1);
+    long long l0 = 0, l1 = 0;
+    if (!kLean) { l0 = lds64(sm, q0); l1 = lds64(sm, q1); }
     long long gcT = gcv - lnf + T_[0];                  // g at the current bin + threshold
 
     const int nch = N / C;
@@ -883,8 +889,12 @@ __device__ __forceinline__ void sweep_bins_warp(const SweepParams& p, const int 
             }
             gcT = sel + Tr[j + 1];                     // gnew + threshold of site j+1
             bp = a ? q1 : q0;
-            const long long lt = a ? l1 : l0;
-            LD = bp == bnew ? gnew : lt;               // the prefetch read the bin just committed
+            if (kLean) {
+                LD = lds64(sm, bp);                    // read after this step's write: current
+            } else {
+                const long long lt = a ? l1 : l0;
+                LD = bp == bnew ? gnew : lt;           // the prefetch read the bin just committed
+            }
             const int2 ev = (j + 2 < C) ? Er[j + 2] : E_[j + 2 - C];
             int e0 = ev.x, e1 = ev.y;
             if (j + 2 == C - 1) {                      // a row's last site sees the row start
@@ -893,8 +903,10 @@ __device__ __forceinline__ void sweep_bins_warp(const SweepParams& p, const int 
             }
             q0 = bnew + e0;
             q1 = bp + e1;
-            l0 = lds64(sm, q0);
-            l1 = lds64(sm, q1);
+            if (!kLean) {
+                l0 = lds64(sm, q0);
+                l1 = lds64(sm, q1);
+            }
             bc = bnew;
             gcv = gnew;
         }
@@ -1011,50 +1023,55 @@ __device__ __forceinline__ void sweep_bins_warp(const SweepParams& p, const int 
     }
 }
 
-template <int G, int C, bool OBS>
+template <int G, int C, bool OBS, bool LEAN>
 __global__ void __launch_bounds__(128, 1) k_sweep_ising_bins(const SweepParams p)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wib = threadIdx.x >> 5;
-    sweep_bins_warp<G, C, OBS>(p, blockIdx.x * (blockDim.x >> 5) + wib, smem + (size_t)wib * G * p.smem_per_warp);
+    sweep_bins_warp<G, C, OBS, LEAN>(p, blockIdx.x * (blockDim.x >> 5) + wib, smem + (size_t)wib * G * p.smem_per_warp);
 }
 
-template <int G, bool OBS>
+template <int G, bool OBS, bool LEAN>
 void launch_bins_t(int C, dim3 grid, dim3 block, size_t smem, cudaStream_t st, const SweepParams& sp)
 {
     switch (C) {
-    case 32: k_sweep_ising_bins<G, 32, OBS><<<grid, block, smem, st>>>(sp); break;
-    case 24: k_sweep_ising_bins<G, 24, OBS><<<grid, block, smem, st>>>(sp); break;
-    case 16: k_sweep_ising_bins<G, 16, OBS><<<grid, block, smem, st>>>(sp); break;
-    case 8: k_sweep_ising_bins<G, 8, OBS><<<grid, block, smem, st>>>(sp); break;
-    default: k_sweep_ising_bins<G, 4, OBS><<<grid, block, smem, st>>>(sp); break;
+    case 32: k_sweep_ising_bins<G, 32, OBS, LEAN><<<grid, block, smem, st>>>(sp); break;
+    case 24: k_sweep_ising_bins<G, 24, OBS, LEAN><<<grid, block, smem, st>>>(sp); break;
+    case 16: k_sweep_ising_bins<G, 16, OBS, LEAN><<<grid, block, smem, st>>>(sp); break;
+    case 8: k_sweep_ising_bins<G, 8, OBS, LEAN><<<grid, block, smem, st>>>(sp); break;
+    default: k_sweep_ising_bins<G, 4, OBS, LEAN><<<grid, block, smem, st>>>(sp); break;
     }
 }
 
+// lean: the chain without the candidate prefetch (several walkers per warp, enough warps per SM
+// to hide the shared-memory latency it exposes; observables off)
 template <int G>
-void launch_bins(int C, dim3 grid, dim3 block, size_t smem, cudaStream_t st, const SweepParams& sp)
+void launch_bins(int C, dim3 grid, dim3 block, size_t smem, cudaStream_t st, const SweepParams& sp, bool lean)
 {
-    if (sp.P.obs) launch_bins_t<G, true>(C, grid, block, smem, st, sp);
-    else launch_bins_t<G, false>(C, grid, block, smem, st, sp);
+    if (sp.P.obs) launch_bins_t<G, true, false>(C, grid, block, smem, st, sp);
+    else if (G > 1 && lean) launch_bins_t<G, false, (G > 1)>(C, grid, block, smem, st, sp);
+    else launch_bins_t<G, false, false>(C, grid, block, smem, st, sp);
 }
 
-template <int G, bool OBS>
+template <int G, bool OBS, bool LEAN>
 cudaError_t allow_bins_smem_t()
 {
     cudaError_t e = cudaSuccess;
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 32, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 24, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 16, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 8, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 4, OBS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 32, OBS, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 24, OBS, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 16, OBS, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 8, OBS, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    e = e != cudaSuccess ? e : cudaFuncSetAttribute(k_sweep_ising_bins<G, 4, OBS, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     return e;
 }
 
 template <int G>
 cudaError_t allow_bins_smem()
 {
-    const cudaError_t e = allow_bins_smem_t<G, false>();
-    return e != cudaSuccess ? e : allow_bins_smem_t<G, true>();
+    cudaError_t e = allow_bins_smem_t<G, false, false>();
+    e = e != cudaSuccess ? e : allow_bins_smem_t<G, true, false>();
+    if (G > 1) e = e != cudaSuccess ? e : allow_bins_smem_t<G, false, (G > 1)>();
+    return e;
 }
 
 // Ashkin-Teller: sweep = sigma pass then tau pass (wang_landau.hpp:109-119); the
@@ -1396,7 +1413,7 @@ struct FusedParams {
 template <int C, bool OBS>
 __device__ __noinline__ void fused_bins(const SweepParams& p, int unit, unsigned char* base)
 {
-    sweep_bins_warp<1, C, OBS>(p, unit, base);
+    sweep_bins_warp<1, C, OBS, false>(p, unit, base);
 }
 
 template <class Model, bool OBS>
@@ -1814,6 +1831,7 @@ struct rewl_engine {
     int64_t kernel_launches = 0;        // sweep-kernel launches since the last timing read
     int64_t launches_total = 0;         // every engine kernel since creation
     int sweep_variant = 3;              // REWL_SWEEP_VARIANT: 3 all-lane Ising resolver (default), 2 lane-0, 4 global tables
+    int bins_lean = -1;                 // REWL_BINS_LEAN: 1 / 0 forces the lean bin-tracking chain on / off (-1: by occupancy)
 
     DBuf<InstDev> d_inst;
     DBuf<WinDev> d_win;
@@ -2445,9 +2463,13 @@ int launch_group(rewl_engine* e, Launch& l, cudaStream_t stream, int nsweeps, co
         const int warps = (sp.nslots + G - 1) / G;
         const int blocks = (warps + l.wpb - 1) / l.wpb;
         const size_t smem = (size_t)l.wpb * G * l.smem_per_warp;
-        if (G == 1) launch_bins<1>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp);
-        else if (G == 2) launch_bins<2>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp);
-        else launch_bins<4>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp);
+        // the lean chain from 5 warps per SM on (measured at L = 64, two walkers per warp: 2048
+        // walkers 3.78e10 against 3.55e10 flips/s, 3072 4.62e10 against 3.78e10; 1024 walkers,
+        // 3.4 warps per SM, 2.15e10 against 2.43e10)
+        const bool lean = e->bins_lean < 0 ? warps >= 5 * sm_count(e) : e->bins_lean == 1;
+        if (G == 1) launch_bins<1>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp, false);
+        else if (G == 2) launch_bins<2>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp, lean);
+        else launch_bins<4>(l.chunk, blocks, 32 * l.wpb, smem, stream, sp, lean);
     } else {
         const int blocks = (sp.nslots + l.wpb - 1) / l.wpb;
         const size_t smem = (size_t)l.wpb * l.smem_per_warp;
@@ -2704,6 +2726,9 @@ int rewl_create(const rewl_batch_desc* desc, rewl_engine** out)
         const int k = std::atoi(v);
         e->sweep_variant = (k == 2 || k == 4) ? k : 3;
     }
+    // REWL_BINS_LEAN: 1 / 0 forces the lean chain of the bin-tracking kernel on / off for warps
+    // of several walkers (tests; by default it is taken from 5 warps per SM on)
+    if (const char* v = std::getenv("REWL_BINS_LEAN")) e->bins_lean = std::atoi(v) == 1 ? 1 : 0;
     int rc = build_host(e);               // descriptor validation and layout: host only
     if (rc) { delete e; return rc; }
     int ndev = 0;

@@ -439,3 +439,32 @@ def test_nearby_seeds_give_unrelated_walker_streams(engine_lib, oracle_lib):
         assert not np.array_equal(tabs[0], tabs[3]) and not np.array_equal(tabs[1], tabs[2])
         for o in orcs:
             o.close()
+
+
+LEAN_CASES = [c for c in CASES if c[0] in ("ising_L8_3x2", "ising_L16_4x3", "ising_L64_2x2")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("walkers_per_warp", [2, 4])
+@pytest.mark.parametrize("case", LEAN_CASES, ids=[c[0] for c in LEAN_CASES])
+def test_lean_chain_matches_oracle(engine_lib, oracle_lib, monkeypatch, case, walkers_per_warp):
+    """The bin-tracking kernel's lean chain (the next proposal read after each step's write, no
+    candidate prefetch), which the engine takes for warps of several walkers from 5 warps per SM
+    on, forced on for small cases: bit for bit against the oracle."""
+    monkeypatch.setenv("REWL_BINS_LEAN", "1")
+    test_engine_matches_oracle_ising(engine_lib, oracle_lib, case, walkers_per_warp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [c for c in FLAT_CASES if c[0].endswith("2perwarp")], ids=lambda c: c[0])
+def test_lean_chain_through_flat_events(engine_lib, oracle_lib, monkeypatch, case):
+    monkeypatch.setenv("REWL_BINS_LEAN", "1")
+    test_engine_matches_oracle_through_flat_events(engine_lib, oracle_lib, case)
+
+
+@pytest.mark.gpu
+def test_benchmark_layout_32_walkers_per_window(engine_lib, oracle_lib):
+    """Ising L = 64, 64 windows x 32 walkers (2048 walkers, two per warp: the lean chain by
+    occupancy), one check interval of its own sweep and exchange intervals, against the oracle."""
+    test_benchmark_layouts_match_oracle(engine_lib, oracle_lib,
+                                        ("ising_L64_64x32", 0, 64, 0.0, -8192.0, 8196.0, 4.0, 64, 32, 500, 1000, 0, 1))
