@@ -1001,23 +1001,25 @@ def main():
     ap.add_argument("--at-spread-runs", type=int, default=4)
     ap.add_argument("--at-warm", type=float, default=0.0, metavar="CAP",
                     help="only measure the Ashkin-Teller L=48 warm-start arm (each arm capped at CAP seconds)")
-    ap.add_argument("--tta-pair", default="", metavar="L,WINDOWS,WALKERS[,CAP]",
+    ap.add_argument("--tta-pair", default="", metavar="L,WINDOWS,WALKERS[,CAP[,gpu]]",
                     help="only measure Ising time to max |d ln g| <= 1e-2 in this layout on the GPU and on all host "
-                         "cores (reference semantics), each capped at CAP seconds (default 150)")
+                         "cores (reference semantics), each capped at CAP seconds (default 150); 'gpu': the GPU only")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.tta_pair:
         import rewl_simulator_gb300 as rg
         rg.build()
-        v = [float(x) for x in args.tta_pair.split(",")]
+        fields = args.tta_pair.split(",")
+        gpu_only = fields[-1] == "gpu"
+        v = [float(x) for x in (fields[:-1] if gpu_only else fields)]
         SMALL_TTA.update(L=int(v[0]), num_windows=int(v[1]), replicas_per_window=int(v[2]),
                          cap_seconds=v[3] if len(v) > 3 else 150.0)
         gpu = gpu_small_tta(rg, 0)
-        cpu = cpu_small_tta(os.cpu_count() or 1)
+        cpu = None if gpu_only else cpu_small_tta(os.cpu_count() or 1)
         print(json.dumps({"tta_pair": {"gpu": gpu, "cpu": cpu,
                                        "cpu_over_gpu": cpu["seconds"] / gpu["seconds"]
-                                       if "0.01" in gpu["seconds_to"] and "0.01" in cpu["seconds_to"] else None}}),
+                                       if cpu and "0.01" in gpu["seconds_to"] and "0.01" in cpu["seconds_to"] else None}}),
               flush=True)
         return 0
     if args.at_warm:
