@@ -501,6 +501,9 @@ def track_accuracy(ws, eng, exact, max_seconds: float, burn_in: int = 0, stall_c
             if err <= tol and str(tol) not in hit:
                 hit[str(tol)] = round(t_sim[0], 2)
                 flips_at[str(tol)] = st.attempted_flips
+                # progress on stderr, so that a long run cut short still leaves its record
+                print(json.dumps({"tolerance": tol, "seconds": hit[str(tol)], "flips": st.attempted_flips}),
+                      file=sys.stderr, flush=True)
         t_mark[0] = time.perf_counter()
         return t_sim[0] > max_seconds or err <= stop_at
 
