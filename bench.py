@@ -387,7 +387,7 @@ def _sample_text(n, total):
 # on a GB300 and its 16 Grace cores: 16 x 64 GPU 1.5 s; 4 x 64 GPU 4.3 s, CPU 32.5 s; 4 x 8 GPU
 # 20.5 s, CPU 17.7 s -- the GPU's advantage is the number of walkers it runs at once.
 SMALL_TTA = dict(L=16, num_windows=16, replicas_per_window=64, sweeps_per_exchange=500, sweeps_per_check=1000,
-                 tolerance=1e-2, cap_seconds=150.0)
+                 tolerance=1e-2, cap_seconds=150.0, seed=5)
 TTA_TOLERANCES = [1.0, 0.5, 0.3, 0.2, 0.15, 0.1, 0.08, 0.05, 0.03, 0.02, 0.01]
 
 
@@ -412,7 +412,7 @@ def cpu_small_tta(threads: int):
              num_windows=s["num_windows"], replicas_per_window=s["replicas_per_window"], window_overlap=0.75,
              sweeps_per_exchange=s["sweeps_per_exchange"], sweeps_per_check=s["sweeps_per_check"], lnf_initial=1.0,
              lnf_final=1e-12, one_over_t=1, init_mode=1)
-    orc = po.Oracle(_port_config(po, w, threads, seed=5))
+    orc = po.Oracle(_port_config(po, w, threads, seed=s["seed"]))
     exact = exact_lng(L)
     hit, t_sim, cycles, best, flips = {}, 0.0, 0, float("inf"), 0
     per_cycle = s["sweeps_per_check"] * s["num_windows"] * s["replicas_per_window"] * N
@@ -525,7 +525,7 @@ def gpu_small_tta(rg, device: int):
     from rewl_simulator_gb300 import warmstart as ws
     s = SMALL_TTA
     t0 = time.perf_counter()
-    eng = rg.Engine(ising_batch(rg, s["L"], s["num_windows"], s["replicas_per_window"], 1.0, 1e-12, 5, device,
+    eng = rg.Engine(ising_batch(rg, s["L"], s["num_windows"], s["replicas_per_window"], 1.0, 1e-12, s["seed"], device,
                                 sweeps_per_exchange=s["sweeps_per_exchange"], sweeps_per_check=s["sweeps_per_check"]))
     out = track_accuracy(ws, eng, exact_lng(s["L"]), s["cap_seconds"], t_setup=time.perf_counter() - t0,
                          stop_at=s["tolerance"])
@@ -1004,6 +1004,7 @@ def main():
     ap.add_argument("--at-spread-runs", type=int, default=4)
     ap.add_argument("--at-warm", type=float, default=0.0, metavar="CAP",
                     help="only measure the Ashkin-Teller L=48 warm-start arm (each arm capped at CAP seconds)")
+    ap.add_argument("--tta-seed", type=int, default=5, help="instance seed of the --tta-pair runs")
     ap.add_argument("--tta-pair", default="", metavar="L,WINDOWS,WALKERS[,CAP[,gpu]]",
                     help="only measure Ising time to max |d ln g| <= 1e-2 in this layout on the GPU and on all host "
                          "cores (reference semantics), each capped at CAP seconds (default 150); 'gpu': the GPU only")
@@ -1017,7 +1018,7 @@ def main():
         gpu_only = fields[-1] == "gpu"
         v = [float(x) for x in (fields[:-1] if gpu_only else fields)]
         SMALL_TTA.update(L=int(v[0]), num_windows=int(v[1]), replicas_per_window=int(v[2]),
-                         cap_seconds=v[3] if len(v) > 3 else 150.0)
+                         cap_seconds=v[3] if len(v) > 3 else 150.0, seed=args.tta_seed)
         gpu = gpu_small_tta(rg, 0)
         cpu = None if gpu_only else cpu_small_tta(os.cpu_count() or 1)
         print(json.dumps({"tta_pair": {"gpu": gpu, "cpu": cpu,
