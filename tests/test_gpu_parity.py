@@ -145,6 +145,9 @@ AT_CASES = [
     ("at_L4_rf", 4, 0.5, 0.5, 0.05, 2, 2, 20, 40, 7, 4, 1),
     ("at_L6_clean_bw025", 6, 0.25, 0.0, 0.25, 3, 2, 10, 20, 3, 4, 1),
     ("at_L8_rf_bw05", 8, 0.5, 0.3, 0.5, 2, 2, 5, 10, 13, 3, 1),
+    # odd rows: the chunk is a whole row of 5 / 7 sites (row wrap inside an odd chunk)
+    ("at_L5_rf", 5, 0.5, 0.5, 0.05, 2, 2, 20, 40, 5, 4, 1),
+    ("at_L7_clean_bw025", 7, 0.25, 0.0, 0.25, 2, 2, 10, 20, 9, 3, 1),
 ]
 
 
