@@ -7,7 +7,7 @@ L = 64 periodic, J = 1, energy levels -8192..8192 step 4 (bins of width 4 over
 spins, replica exchange every 500 sweeps, flatness (min >= 0.8 mean over the valid
 levels) checked every 1000 sweeps, ln f from 1 with the reference's default 1/t
 schedule (ONE_OVER_T_ALGORITHM), walkers started from all spins +1 as the
-reference's are, int64 logDoS in 2^-40 units.  Inputs are synthetic.
+reference's are, int64 logDoS in 2^-36 units.  Inputs are synthetic.
 
 A step is one check interval: 2 x (500 sweeps of all 512 walkers + one replica
 exchange round) + the flatness / averaging / ln f kernel, i.e. 2,097,152,000

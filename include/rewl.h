@@ -160,14 +160,14 @@ int rewl_import_disorder(rewl_engine* eng, int32_t instance, const double* field
 int rewl_generate_fields(uint64_t seed, double strength, int32_t distribution, int64_t num_sites, double* out);
 
 /* Set the logDoS of every replica of a window (warm start); values are rounded
- * to the engine's 2^-40 grid.  No reference counterpart (the reference starts at 0,
+ * to the engine's 2^-36 grid and must satisfy |g| <= 2^24 nats (2^60 units).  No reference counterpart (the reference starts at 0,
  * src/REWL/rewl_histograms.hpp:42-50). */
 int rewl_set_logdos(rewl_engine* eng, int32_t instance, int32_t window, const double* logdos);
 
 /* Set ln f of a window (REWL_Walker::incrementer, src/REWL/rewl_walker.hpp:21), (0, 64].
  * Sweep launches are sized so that one launch cannot carry a logDoS entry past int64: a
  * large ln f on a large lattice splits an exchange interval into several launches (same
- * results).  A logDoS entry reaching 2^62 units (4.2e6 nats) without a flat event stops the
+ * results).  A logDoS entry reaching 2^62 units (6.7e7 nats) without a flat event stops the
  * engine with REWL_ESTATE, as does a per-stage count passing 2^32 - 1. */
 int rewl_set_lnf(rewl_engine* eng, int32_t instance, int32_t window, double lnf);
 

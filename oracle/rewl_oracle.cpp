@@ -36,7 +36,7 @@
 //     timed CPU baseline.
 //   * ENGINE: the semantics of the CUDA engine: one Philox4x32-10 draw per attempt
 //     (Salmon et al., SC'11), acceptance dg < -ln(u) with a deterministic float
-//     log, logDoS held on a 2^-40 grid (averaged values are rounded back onto it),
+//     log, logDoS held on a 2^-36 grid (averaged values are rounded back onto it),
 //     exact integer energies and bins, Philox pairing for the exchange.  The GPU
 //     engine must agree with this bit for bit.
 //
@@ -142,8 +142,8 @@ static inline float neglog_u32(uint32_t x)
     return ::fmaf((float)k, 0.693147182f, q);
 }
 
-// Smallest integer d (>= 1) with fl32(d * 2^-40) >= thr, for thr > 0.  Then
-// "float(dg) < thr" is exactly "d < T" for dg = d * 2^-40.
+// Smallest integer d (>= 1) with fl32(d * 2^-36) >= thr, for thr > 0.  Then
+// "float(dg) < thr" is exactly "d < T" for dg = d * 2^-36.
 static inline int64_t accept_threshold(float thr)
 {
     uint32_t b; std::memcpy(&b, &thr, 4);
@@ -153,13 +153,13 @@ static inline int64_t accept_threshold(float thr)
     int64_t A; int s; bool inclusive;
     if (m == 0x800000) { A = 4 * m - 1; s = e - 2; inclusive = true; }
     else { A = 2 * m - 1; s = e - 1; inclusive = (m & 1) == 0; }
-    const int sh = s + 40;
+    const int sh = s + 36;
     if (sh >= 0) { const int64_t D = A << sh; return inclusive ? D : D + 1; }
     return (A >> (-sh)) + 1;
 }
 
-static constexpr int QBITS = 40;
-static constexpr double QSCALE = 1099511627776.0;      // 2^40
+static constexpr int QBITS = 36;
+static constexpr double QSCALE = 68719476736.0;        // 2^36
 
 // ----------------------------------------------------------------------------
 // Lattice helpers: neighbour order (x,y-1),(x-1,y),(x+1,y),(x,y+1).
@@ -447,7 +447,7 @@ template <class M> struct alignas(128) Walker
     std::vector<double> logdos;
     std::vector<double> obs;           // AoS running averages [bin][num_obs] (reference layout)
     double lnf = 1.0;
-    int64_t lnf_u = 0;                 // engine semantics: ln f in 2^-40 units
+    int64_t lnf_u = 0;                 // engine semantics: ln f in 2^-36 units
     uint64_t sweeps_done = 0;          // engine semantics: attempt counter base
     std::mt19937_64 gen;               // reference semantics
     std::uniform_real_distribution<double> U{0., 1.};
@@ -870,7 +870,7 @@ template <class M> static int flat_step(Sim<M>& S)
             {
                 if (S.c.one_over_t && !S.oot[w] && (double)k.lnf_u <= QSCALE / (double)t) S.oot[w] = 1;
                 k.lnf_u = S.oot[w] ? (int64_t)(((uint64_t)1 << QBITS) + t / 2) / (int64_t)t : (k.lnf_u >> 1);
-                if (k.lnf_u < 1) k.lnf_u = 1;           // smallest increment of the 2^-40 grid
+                if (k.lnf_u < 1) k.lnf_u = 1;           // smallest increment of the 2^-36 grid
                 k.lnf = (double)k.lnf_u / QSCALE;
             }
         }

@@ -5,13 +5,13 @@
 //   walker slots  s = first_slot(instance) + window * R + replica
 //       slot_cfg[s]      configuration currently held by the slot (an exchange
 //                        swaps two entries instead of moving lattices)
-//       slot_tab[s]      offset of the slot's tables: g (int64, 2^-40 units),
+//       slot_tab[s]      offset of the slot's tables: g (int64, 2^-36 units),
 //                        H (uint32 per-stage counts), visits (uint64 cumulative)
 //       slot_sweeps[s]   sweeps done (Philox attempt counter base)
 //       slot_flavour[s]  Ashkin-Teller which_to_update
 //   configurations c: spins (int8; Ising N, Ashkin-Teller sigma plane then tau
 //       plane), energy (int64 units of 2^-escale), magnetisations (int32 x3)
-//   windows: ln f (int64 2^-40 units), done / 1/t flags, counters, valid-bin mask
+//   windows: ln f (int64 2^-36 units), done / 1/t flags, counters, valid-bin mask
 //
 // Kernels
 //   k_init          one thread per walker: initial spins from Philox, then the
@@ -81,12 +81,13 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 enum : int { ERR_BOUNDS = 1, ERR_ADJUST = 2, ERR_REPLAY_EXHAUSTED = 4, ERR_RANGE = 8, ERR_COUNT = 16 };
 // |logDoS| at which a window is reported (REWL_ESTATE) instead of risking int64 overflow: 2^62
-// units (4.2e6 nats).  Every kernel that adds to g checks the values it wrote against it, and
+// units (6.7e7 nats).  Every kernel that adds to g checks the values it wrote against it, and
 // every kernel returns without work once the error word is set, so at most one launch's growth
 // lies beyond the limit.  The host splits sweep launches so that one launch adds at most
 // kLaunchGrowth to any bin (ln f bound x sweeps x degrees of freedom, plus one exchange visit):
 // 2^62 + 2^62 - 2^58 stays below 2^63 with room for the acceptance thresholds (< 2^45).
 constexpr long long kLogdosLimit = 1LL << 62;
+constexpr double kSetLogdosMax = 16777216.0;                // 2^60 units: the largest |g| rewl_set_logdos takes
 constexpr long long kLaunchGrowth = (1LL << 62) - (1LL << 58);
 
 // Any device error stops further work: a kernel that finds the error word set returns at once.
@@ -426,7 +427,7 @@ __device__ __forceinline__ void resolve_chunk_all_lanes(int& E, int& b, long lon
 // Ising sweeps.  One warp per walker; lattice and logDoS staged in shared memory
 // for the whole launch.  Per-stage counts are not kept in the loop: within a
 // launch every visit adds the same ln f, so the counts added to bin k are
-// (g_end[k] - g_start[k]) / ln f exactly (ln f >= one 2^-40 unit always).
+// (g_end[k] - g_start[k]) / ln f exactly (ln f >= one 2^-36 unit always).
 template <bool REPLAY, int VARIANT>
 __global__ void __launch_bounds__(256) k_sweep_ising(const SweepParams p)
 {
@@ -1706,7 +1707,7 @@ __global__ void __launch_bounds__(256) k_flat(const FlatParams fp)
         if (fp.one_over_t && !oot && t > 0 && __ll2double_rn(lnf) <= __ddiv_rn(kLogdosScale, __ull2double_rn(t))) oot = 1;
         if (oot && t > 0) lnf = (long long)((((unsigned long long)1 << kLogdosBits) + t / 2) / t);
         else lnf = lnf >> 1;
-        if (lnf < 1) lnf = 1;                  // the 2^-40 grid's smallest increment
+        if (lnf < 1) lnf = 1;                  // the 2^-36 grid's smallest increment
         P.win_lnf[w] = lnf;
         P.win_oot[w] = oot;
         P.win_done[w] = (__ll2double_rn(lnf) / kLogdosScale) < fp.lnf_final ? 1 : 0;
@@ -1807,7 +1808,7 @@ struct rewl_engine {
     int64_t sweeps_total = 0, cycles = 0, flat_events = 0, flips_total = 0;
     int64_t flips_per_sweep = 0;
     // sweep launches are split so that one launch adds at most kLaunchGrowth to a bin: an upper
-    // bound of every window's ln f (2^-40 units; k_flat only lowers it, except the 1/t rule,
+    // bound of every window's ln f (2^-36 units; k_flat only lowers it, except the 1/t rule,
     // which never exceeds 1) and the largest number of degrees of freedom of a walker
     int64_t lnf_bound_u = 0, ndof_max = 0;
     // rewl_batch_desc.persistent: every launch group in one work-stealing launch (k_sweep_fused)
@@ -2427,7 +2428,7 @@ int check_device_error(rewl_engine* e)
     if (h[0] & ERR_ADJUST) return fail(REWL_EINVAL, "a walker could not reach its window");
     if (h[0] & ERR_REPLAY_EXHAUSTED) return fail(REWL_EINVAL, "replay uniform stream exhausted");
     if (h[0] & ERR_RANGE)
-        return fail(REWL_ESTATE, "a window's logDoS passed 2^62 units (4.2e6 nats) without a flat event: "
+        return fail(REWL_ESTATE, "a window's logDoS passed 2^62 units (6.7e7 nats) without a flat event: "
                                  "a replica is trapped away from part of its window");
     if (h[0] & ERR_COUNT)
         return fail(REWL_ESTATE, "a per-stage histogram count passed 2^32 - 1 without a flat event");
@@ -2892,7 +2893,8 @@ int rewl_set_logdos(rewl_engine* e, int32_t ii, int32_t w, const double* logdos)
     const int nb = e->h_wins[wi].nb;
     std::vector<int64_t> q(nb);
     for (int b = 0; b < nb; ++b) {
-        if (!std::isfinite(logdos[b]) || std::fabs(logdos[b]) > 1e6) return fail(REWL_EINVAL, "logdos values must be finite and |g| <= 1e6");
+        // a quarter of the 2^62-unit ceiling (1.68e7 nats): room for a first stage to follow
+        if (!std::isfinite(logdos[b]) || std::fabs(logdos[b]) > kSetLogdosMax) return fail(REWL_EINVAL, "logdos values must be finite and |g| <= 2^60 units (1.68e7 nats)");
         q[b] = (int64_t)std::nearbyint(logdos[b] * kLogdosScale);
     }
     cudaSetDevice(e->desc.device);

@@ -9,7 +9,7 @@
 // entropy change (src/REWL/wang_landau.hpp:68-73).  Here that test is rewritten
 // as dg < -ln(u) with a deterministic float -ln (explicit IEEE roundings only,
 // identical on host and device), and because logDoS is held as an int64 count of
-// 2^-40 units, "float(d * 2^-40) < thr" becomes the integer test d < T(thr).
+// 2^-36 units, "float(d * 2^-36) < thr" becomes the integer test d < T(thr).
 #pragma once
 #include <stdint.h>
 
@@ -21,8 +21,8 @@
 
 namespace rewl {
 
-static constexpr int kLogdosBits = 40;                       // logDoS unit = 2^-40
-static constexpr double kLogdosScale = 1099511627776.0;      // 2^40
+static constexpr int kLogdosBits = 36;                       // logDoS unit = 2^-36
+static constexpr double kLogdosScale = 68719476736.0;        // 2^36
 
 enum : uint32_t {
     kStreamWL = 0x574C0001u,      // per-attempt acceptance uniforms
@@ -160,8 +160,8 @@ REWL_HD float neglog_u32(uint32_t x)
     return RW_FMA(RW_I2F(k), 0.693147182f, q);
 }
 
-// Smallest integer d >= 1 with float(d * 2^-40) >= thr (thr > 0, finite, normal):
-// for any int64 d, float(d * 2^-40) < thr  <=>  d < accept_threshold(thr).
+// Smallest integer d >= 1 with float(d * 2^-36) >= thr (thr > 0, finite, normal):
+// for any int64 d, float(d * 2^-36) < thr  <=>  d < accept_threshold(thr).
 // thr = m 2^e; the rounding boundary below thr is (2m-1) 2^(e-1) (ties to the
 // even neighbour), or (4m-1) 2^(e-2) when thr is a power of two.
 REWL_HD int64_t accept_threshold(float thr)

@@ -4,9 +4,9 @@ overflow int64.
 The bin-tracking Ising sweep rejects proposals outside the window through guard bins that
 hold INT64_MAX, so no value of g at the current bin can let a walker step out of its window's
 table.  Every kernel that adds to g checks the values it wrote against 2^62 grid units
-(4.2e6 nats) and, once one passes, the engine stops with REWL_ESTATE: every later kernel
+(6.7e7 nats) and, once one passes, the engine stops with REWL_ESTATE: every later kernel
 returns without work.  Sweep launches are split so that one launch adds at most
-2^62 - 2^58 units to a bin (here ln f = 64 nats at L = 16: at most 240 sweeps per launch), so
+2^62 - 2^58 units to a bin (here ln f = 64 nats at L = 32: at most 960 sweeps per launch), so
 the largest value ever stored stays below 2^63.
 """
 import numpy as np
@@ -14,22 +14,23 @@ import pytest
 
 from rewl_simulator_gb300.engine import REWL_ESTATE
 
-UNITS = 2.0 ** 40                 # logDoS grid: 2^-40 nats
-LIMIT = 2.0 ** 62 / UNITS         # 4.19e6 nats
-INT64_TOP = 2.0 ** 63 / UNITS     # 8.39e6 nats
+UNITS = 2.0 ** 36                 # logDoS grid: 2^-36 nats
+LIMIT = 2.0 ** 62 / UNITS         # 6.71e7 nats
+INT64_TOP = 2.0 ** 63 / UNITS     # 1.34e8 nats
+START = 2.0 ** 24                 # nats: the largest logDoS rewl_set_logdos takes (2^60 units)
 
 
 @pytest.mark.gpu
 def test_logdos_past_the_limit_stops_the_engine_before_int64_overflow(engine_lib):
     rg = engine_lib
-    L, N = 16, 256
+    L, N = 32, 1024
     ins = rg.Instance(model=rg.MODEL_ISING2D, L=L, energy_min=-2.0 * N, energy_max=2.0 * N + 4, bin_width=4.0,
-                      num_windows=16, replicas_per_window=2, seed=21)
+                      num_windows=64, replicas_per_window=2, seed=21)
     b = rg.Batch(instances=[ins], sweeps_per_exchange=500, sweeps_per_check=1000, lnf_initial=1.0, lnf_final=1e-6)
     with rg.Engine(b) as eng:
         wins = eng.windows[0]
         for w, (lo, hi, nb) in enumerate(wins):
-            eng.set_logdos(0, w, np.full(nb, 1e6))
+            eng.set_logdos(0, w, np.full(nb, START))
             eng.set_lnf(0, w, 64.0)                       # 64 nats per visit: g climbs fast
         walkers = [(eng.walker_id(0, w, r), w) for w in range(len(wins)) for r in range(2)]
 
@@ -41,14 +42,14 @@ def test_logdos_past_the_limit_stops_the_engine_before_int64_overflow(engine_lib
                 E = float(out["state"][0])
                 assert lo <= E < hi, (wk, w, E, lo, hi)
                 g = out["logdos"]
-                assert np.isfinite(g).all() and g.min() >= 1e6 - 1e-6      # only grows: no wrap
+                assert np.isfinite(g).all() and g.min() >= START - 1e-6    # only grows: no wrap
                 top = max(top, float(g.max()))
             return top
 
         stopped = None
         for k in range(40):
             try:
-                eng.run_sweeps(1000)
+                eng.run_sweeps(3000)
             except rg.REWLError as err:
                 stopped = err
                 break
@@ -66,16 +67,16 @@ def test_logdos_past_the_limit_stops_the_engine_before_int64_overflow(engine_lib
 
 @pytest.mark.gpu
 def test_large_lnf_splits_launches_without_changing_results(engine_lib, oracle_lib):
-    """ln f = 32 nats on L = 24 allows at most (2^62 - 2^58) / (32 x 2^40) / 576 = 213 sweeps per
+    """ln f = 64 nats on L = 64 allows at most (2^62 - 2^58) / (64 x 2^36) / 4096 = 240 sweeps per
     launch: an exchange interval of 500 sweeps becomes three launches, bit for bit the oracle's
     run."""
     rg, po = engine_lib, oracle_lib
-    L, N = 24, 576
+    L, N = 64, 4096
     ins = rg.Instance(model=0, L=L, energy_min=-2.0 * N, energy_max=2.0 * N + 4, bin_width=4.0, num_windows=4,
                       replicas_per_window=2, seed=5)
-    b = rg.Batch(instances=[ins], sweeps_per_exchange=500, sweeps_per_check=1000, lnf_initial=32.0, lnf_final=1e-6)
+    b = rg.Batch(instances=[ins], sweeps_per_exchange=500, sweeps_per_check=1000, lnf_initial=64.0, lnf_final=1e-6)
     cfg = po.Config(model=0, L=L, nwin=4, R=2, sweeps_per_exchange=500, sweeps_per_check=1000, emin=-2.0 * N,
-                    emax=2.0 * N + 4, bw=4.0, lnf0=32.0, lnf_final=1e-6, semantics=po.SEM_ENGINE, seed=5)
+                    emax=2.0 * N + 4, bw=4.0, lnf0=64.0, lnf_final=1e-6, semantics=po.SEM_ENGINE, seed=5)
     orc = po.Oracle(cfg)
     with rg.Engine(b) as eng:
         st0 = eng.status()

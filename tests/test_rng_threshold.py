@@ -36,8 +36,8 @@ def f32(x: float) -> float:
 
 
 def _float_lt(d: int, thr: float) -> bool:
-    """float(d * 2^-40) < thr with IEEE round-to-nearest-even (numpy float32)."""
-    return bool(np.float32(np.float64(d) * 2.0**-40) < np.float32(thr))
+    """float(d * 2^-36) < thr with IEEE round-to-nearest-even (numpy float32)."""
+    return bool(np.float32(np.float64(d) * 2.0**-36) < np.float32(thr))
 
 
 def test_accept_threshold_exact(oracle_lib):
