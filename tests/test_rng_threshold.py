@@ -91,3 +91,18 @@ def test_seeds_two_and_three_no_longer_run_identically(oracle_lib):
         orc.close()
     assert not np.array_equal(runs[0][0], runs[1][1]) and not np.array_equal(runs[0][1], runs[1][0])
     assert not np.array_equal(runs[0][0], runs[1][0])
+
+
+def test_engine_and_oracle_share_the_logdos_unit():
+    """The engine (rng.cuh) and the oracle restate the logDoS unit separately: they must agree,
+    and the tests above check the boundary at that unit."""
+    import re
+    from conftest import ROOT
+    rng = (ROOT / "rewl_simulator_gb300" / "csrc" / "rng.cuh").read_text()
+    orc = (ROOT / "oracle" / "rewl_oracle.cpp").read_text()
+    bits = int(re.search(r"kLogdosBits = (\d+);", rng).group(1))
+    scale = float(re.search(r"kLogdosScale = ([0-9.]+);", rng).group(1))
+    qbits = int(re.search(r"QBITS = (\d+);", orc).group(1))
+    qscale = float(re.search(r"QSCALE = ([0-9.]+);", orc).group(1))
+    assert bits == qbits == 36 and scale == qscale == 2.0 ** bits
+    assert f"const int sh = s + {bits};" in orc
