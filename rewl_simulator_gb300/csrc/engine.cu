@@ -1082,10 +1082,9 @@ cudaError_t allow_bins_smem()
 // derived at its end from the change of g against a copy taken at its start
 // (every visit adds the same ln f), and the chain loads both possible proposals
 // of the next step one step ahead, so a load's latency overlaps a decision.
-#ifndef REWL_TABLE_REACH
-#define REWL_TABLE_REACH 512
-#endif
-constexpr int kTableReach = REWL_TABLE_REACH;        // bins either side prefetched per chunk
+// bins either side of the walker's bin prefetched into L1 per chunk (measured on the Ashkin-Teller
+// benchmark: 256 / 384 / 512 / 768 / 1024 bins 43.5 / 43.3 / 43.4 / 43.9 / 44.1 ms per launch)
+constexpr int kTableReach = 512;
 
 struct TableStage {
     longlong2 du[32];        // per site: {proposal, proposal after its left neighbour flipped in this chunk}
